@@ -1,0 +1,300 @@
+/*
+ * zgpu.h -- C ABI of the GB300 walk engine (Walk on Spheres / Walk on Stars fused
+ * with the boundary geometric queries they issue every step).
+ *
+ * Plain C: handles, POD structs, pointers and sizes.  No C++ or torch types cross
+ * this boundary.  Every entry point returns a zgpu_status; the message of the most
+ * recent failure on the calling thread is available from zgpu_last_error().
+ *
+ * Each entry point names the interface of rohan-sawhney/zombie it replaces
+ * (paths relative to that project).
+ */
+#ifndef ZGPU_H
+#define ZGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZGPU_ABI_VERSION 1
+
+/* ------------------------------------------------------------------------- */
+/* status codes                                                               */
+/* ------------------------------------------------------------------------- */
+typedef enum zgpu_status {
+    ZGPU_OK = 0,
+    ZGPU_ERR_INVALID_ARG = 1,
+    ZGPU_ERR_OUT_OF_MEMORY = 2,
+    ZGPU_ERR_CUDA = 3,
+    ZGPU_ERR_TIMEOUT_BUDGET = 4,       /* a device-side iteration budget ran out */
+    ZGPU_ERR_UNSUPPORTED_CALLBACK = 5, /* host std::function callbacks cannot run on the device */
+    ZGPU_ERR_UNSUPPORTED = 6,
+    ZGPU_ERR_DEVICE_STATE = 7          /* a kernel reported an internal error word */
+} zgpu_status;
+
+/* memory space of caller-owned arrays */
+enum { ZGPU_MEM_HOST = 0, ZGPU_MEM_DEVICE = 1 };
+
+/* boundary kinds (FcpwDirichlet/Neumann/RobinBoundaryHandler) */
+enum { ZGPU_BOUNDARY_ABSORBING = 0, ZGPU_BOUNDARY_NEUMANN = 1, ZGPU_BOUNDARY_ROBIN = 2 };
+
+/* SampleType (point_estimation/common.h:139-143) */
+enum { ZGPU_SAMPLE_IN_DOMAIN = 0, ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY = 1, ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY = 2 };
+
+/* EstimationQuantity (point_estimation/common.h:145-149) */
+enum { ZGPU_ESTIMATE_SOLUTION = 0, ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT = 1, ZGPU_ESTIMATE_SKIP = 2 };
+
+/* field kinds of the device-evaluable PDE descriptor */
+enum { ZGPU_FIELD_ZERO = 0, ZGPU_FIELD_CONSTANT = 1, ZGPU_FIELD_ANALYTIC = 2, ZGPU_FIELD_GRID = 3 };
+
+/* solvers */
+enum { ZGPU_SOLVER_WALK_ON_SPHERES = 0, ZGPU_SOLVER_WALK_ON_STARS = 1 };
+
+#define ZGPU_MAX_TERMS 8
+
+/*
+ * Closed-form field used as a manufactured solution:
+ *   u(x) = sum_k c[k] * exp(a[k].x) * cos(b[k].x + phi[k]) + sum_i q[i] x_i^2 + sum_i l[i] x_i + d
+ * Its gradient and Laplacian are closed form, so Dirichlet data g = u, Robin data
+ * h = du/dn + kappa u and source f = -Lap(u) + sigma u are evaluated on the device.
+ */
+typedef struct zgpu_analytic {
+    int32_t n_terms;
+    float c[ZGPU_MAX_TERMS];
+    float a[ZGPU_MAX_TERMS][3];
+    float b[ZGPU_MAX_TERMS][3];
+    float phi[ZGPU_MAX_TERMS];
+    float q[3];
+    float l[3];
+    float d;
+} zgpu_analytic;
+
+/* A dense grid field (utils/dense_grid.h): row-major values over [grid_min, grid_max]. */
+typedef struct zgpu_grid {
+    const float* values;   /* device or host pointer, see zgpu_pde.memory */
+    int32_t shape[3];
+    float grid_min[3];
+    float grid_max[3];
+    int32_t bilinear;      /* 1: (bi/tri)linear lookup, 0: nearest */
+} zgpu_grid;
+
+/*
+ * Device-evaluable replacement for PDE<T,DIM> (core/pde.h:19-45), whose members are
+ * host std::functions.  Each field is ZERO, CONSTANT (value), ANALYTIC (derived from
+ * `solution`) or GRID.  The *_aligned values are those returned when the reference
+ * passes returnBoundaryNormalAlignedValue = true (double-sided problems).
+ */
+typedef struct zgpu_pde {
+    float absorption_coeff;                  /* sigma >= 0 in  -Lap u + sigma u = f */
+    int32_t is_source_constant;
+    int32_t are_robin_conditions_pure_neumann;
+    int32_t are_robin_coeffs_nonnegative;
+    zgpu_analytic solution;
+    int32_t source_kind;       float source_value;
+    int32_t dirichlet_kind;    float dirichlet_value;    float dirichlet_value_aligned;
+    int32_t robin_kind;        float robin_value;        float robin_value_aligned;
+    int32_t robin_coeff_kind;  float robin_coeff_value;  float robin_coeff_value_aligned;
+    zgpu_grid source_grid;
+    zgpu_grid dirichlet_grid;
+    zgpu_grid robin_grid;
+    int32_t memory;            /* memory space of the grid value arrays */
+} zgpu_pde;
+
+/* WalkSettings (point_estimation/common.h:19-91): same fields, same order. */
+typedef struct zgpu_walk_settings {
+    float epsilon_shell_for_absorbing_boundary;
+    float epsilon_shell_for_reflecting_boundary;
+    float silhouette_precision;
+    float russian_roulette_threshold;
+    float splitting_threshold;
+    int32_t max_walk_length;
+    int32_t steps_before_applying_tikhonov;
+    int32_t steps_before_using_maximal_spheres;
+    int32_t solve_double_sided;
+    int32_t use_gradient_control_variates;
+    int32_t use_gradient_antithetic_variates;
+    int32_t use_cosine_sampling_for_derivatives;
+    int32_t ignore_absorbing_boundary_contribution;
+    int32_t ignore_reflecting_boundary_contribution;
+    int32_t ignore_source_contribution;
+    int32_t print_logs;
+} zgpu_walk_settings;
+
+/*
+ * SamplePoint (point_estimation/common.h:151-195) as structure of arrays.
+ * pt/normal are [n*dim] floats.  seed[i] replaces the per-point pcg32 member: walk w
+ * of point i draws from pcg32(seed[i], stream = w + statistics n[i]).
+ * first_sphere_radius is read and written (WoSt precomputes it on the first call).
+ * Optional arrays may be NULL (normal -> 0, type -> IN_DOMAIN, dist_to_reflecting -> inf,
+ * estimate_normal_aligned -> 0, estimation_quantity -> SOLUTION).
+ */
+typedef struct zgpu_sample_points {
+    int64_t n;
+    int32_t memory;
+    const float* pt;
+    const float* normal;
+    const int32_t* type;
+    const int32_t* estimation_quantity;
+    const float* dist_to_absorbing;
+    const float* dist_to_reflecting;
+    const int32_t* n_walks;
+    const uint64_t* seed;
+    float* first_sphere_radius;
+    const int32_t* estimate_normal_aligned;
+    const int32_t* scene_id;   /* batched many-solve: index into the scene table, NULL -> 0 */
+} zgpu_sample_points;
+
+/*
+ * SampleStatistics (point_estimation/common.h:200-395) as structure of arrays,
+ * accumulated across calls (progressive estimation, as the reference): every solve
+ * merges its walks into these arrays with the parallel Welford merge of
+ * SampleStatistics::merge (common.h:268-310), in FP64.
+ * gradient_mean/gradient_m2 are [n*dim] and may be NULL when no point asks for gradients.
+ */
+typedef struct zgpu_sample_statistics {
+    int32_t memory;
+    double* solution_mean;
+    double* solution_m2;
+    int32_t* n_solution_estimates;
+    int64_t* total_walk_length;
+    int64_t* total_splits;
+    double* gradient_mean;
+    double* gradient_m2;
+    int32_t* n_gradient_estimates;
+} zgpu_sample_statistics;
+
+/* launch and engine options that have no counterpart in the reference */
+typedef struct zgpu_solve_options {
+    int32_t block_size;        /* 0 -> autotuned / default */
+    int32_t blocks_per_sm;     /* 0 -> occupancy-derived */
+    int32_t use_graph;         /* capture prepare+walk+finalize in a CUDA graph and replay */
+    int64_t step_budget;       /* per-walk-state hard cap on device loop iterations (0 -> max_walk_length+1) */
+} zgpu_solve_options;
+
+/* counters returned by a solve */
+typedef struct zgpu_solve_report {
+    uint64_t total_steps;      /* executed walk-loop iterations (the walk-steps/s numerator) */
+    uint64_t total_walks;
+    uint64_t escaped_walks;
+    uint64_t exceeded_walks;
+    uint64_t rr_terminated;
+    float kernel_ms;           /* CUDA-event time of the walk kernel */
+    float total_ms;            /* CUDA-event time of prepare + walk + finalize */
+    uint32_t error_word;       /* nonzero: device-side internal error (stack overflow, budget) */
+} zgpu_solve_report;
+
+typedef struct zgpu_context zgpu_context;
+typedef struct zgpu_boundary zgpu_boundary;
+
+/*
+ * GeometricQueries<DIM> (core/geometric_queries.h:58-124) populated by
+ * populateGeometricQueriesFor{Dirichlet,Neumann,Robin}Boundary
+ * (utils/fcpw_geometric_queries.h:1062-1389): the std::function members become the
+ * device queries of the two boundary handles.  Either handle may be NULL (empty part).
+ */
+typedef struct zgpu_geometric_queries {
+    int32_t dim;
+    int32_t domain_is_watertight;
+    float domain_min[3];
+    float domain_max[3];
+    zgpu_boundary* absorbing;
+    zgpu_boundary* reflecting;
+} zgpu_geometric_queries;
+
+/* ---------------------------- context ------------------------------------ */
+int zgpu_abi_version(void);
+const char* zgpu_last_error(void);
+/* creates a context (CUDA stream + cached scratch) on `device` */
+int zgpu_context_create(int device, zgpu_context** out);
+int zgpu_context_destroy(zgpu_context* ctx);
+int zgpu_context_synchronize(zgpu_context* ctx);
+/* the CUDA stream (cudaStream_t) every kernel of this context is launched on */
+void* zgpu_context_stream(zgpu_context* ctx);
+
+/* ---------------------------- boundaries --------------------------------- */
+/*
+ * Builds a boundary acceleration structure on the device.  Replaces
+ * FcpwDirichletBoundaryHandler::buildAccelerationStructure (utils/fcpw_geometric_queries.h:84-88),
+ * FcpwNeumannBoundaryHandler::buildAccelerationStructure (:100-105, silhouettes from
+ * computeSilhouettes :631) and FcpwRobinBoundaryHandler::buildAccelerationStructure
+ * (:117-124, adjacency :745-799 / :892-973, ReflectanceBvh reflectance_boundary_bvh/bvh.h).
+ * positions: [n_vertices*dim] host floats; indices: [n_prims*dim] host ints.
+ * min/max_robin_coeff: [n_prims] (ROBIN only, else NULL).
+ * solve_double_sided/silhouette_precision feed getIgnoreCandidateSilhouetteCallback (:1029-1038).
+ * bvh_width: 4 or 8 (0 -> 4).
+ */
+int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
+                         const int* indices, int n_prims, int kind,
+                         const float* min_robin_coeff, const float* max_robin_coeff,
+                         int solve_double_sided, float silhouette_precision, int bvh_width,
+                         zgpu_boundary** out);
+int zgpu_boundary_destroy(zgpu_boundary* b);
+/* FcpwRobinBoundaryHandler::updateCoefficientValues (utils/fcpw_geometric_queries.h:126-128) */
+int zgpu_boundary_update_robin_coefficients(zgpu_boundary* b, const float* min_robin_coeff,
+                                            const float* max_robin_coeff);
+/* statistics of the built tree: nodes, depth, bytes (for the roofline bookkeeping) */
+int zgpu_boundary_info(zgpu_boundary* b, int64_t* n_nodes, int32_t* depth, int64_t* node_bytes,
+                       int64_t* prim_bytes);
+/* Aggregate::signedVolume (used by computeAbsorbing/ReflectingBoundarySignedVolume) */
+int zgpu_boundary_signed_volume(zgpu_boundary* b, float* out);
+
+/* ---------------------- batched geometric queries ------------------------- */
+/* All arrays live in `memory`; n queries; vectors are [n*dim].                */
+
+/* computeDistToAbsorbingBoundary / projectToAbsorbingBoundary
+ * (utils/fcpw_geometric_queries.h:1069-1096; reflecting twins :1150-1177):
+ * closest point, its normal, (signed) distance and the caller's primitive index. */
+int zgpu_query_closest_point(zgpu_boundary* b, int64_t n, const float* x, int compute_signed,
+                             float* out_pt, float* out_normal, float* out_dist, int32_t* out_prim,
+                             int memory);
+/* intersectAbsorbingBoundary / intersectReflectingBoundary (:1097-1115, :1178-1196):
+ * first hit within t_max; origins on the boundary are offset along -normal. */
+int zgpu_query_intersect(zgpu_boundary* b, int64_t n, const float* origin, const float* normal,
+                         const float* dir, const float* t_max, const int32_t* on_boundary,
+                         int32_t* out_hit, float* out_pt, float* out_normal, float* out_dist,
+                         int32_t* out_prim, int memory);
+/* intersect...AllHits (:1116-1136, :1197-1217): number of hits within t_max */
+int zgpu_query_count_hits(zgpu_boundary* b, int64_t n, const float* origin, const float* dir,
+                          const float* t_max, int32_t* out_count, int memory);
+/* computeStarRadiusForReflectingBoundary (Neumann :1249-1270, Robin :1272-1291) */
+int zgpu_query_star_radius(zgpu_boundary* b, int64_t n, const float* x, const float* min_radius,
+                           const float* max_radius, float silhouette_precision,
+                           const int32_t* flip_normal_orientation, float* out_radius, int memory);
+/* intersectsWithReflectingBoundary (:1218-1226): 1 when the segment xi->xj is occluded */
+int zgpu_query_occluded(zgpu_boundary* b, int64_t n, const float* xi, const float* xj,
+                        const float* ni, const float* nj, const int32_t* offset_i,
+                        const int32_t* offset_j, int32_t* out_occluded, int memory);
+/* sampleReflectingBoundary (:1227-1242): a boundary point inside the ball with its pdf */
+int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, const float* radius,
+                               const float* rand_nums, int32_t* out_found, float* out_pt,
+                               float* out_normal, float* out_pdf, int memory);
+
+/* ------------------------------- solve ----------------------------------- */
+/*
+ * WalkOnSpheres<T,DIM>::solve (point_estimation/walk_on_spheres.h:38-44, batch over points
+ * :132-168) and WalkOnStars<T,DIM>::solve (point_estimation/walk_on_stars.h:40-46, :151-187).
+ * Runs every walk of every point in one persistent wavefront kernel and merges the walk
+ * estimates into `stats`.  options/report may be NULL.
+ */
+int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries,
+               const zgpu_pde* pde, const zgpu_walk_settings* settings,
+               const zgpu_sample_points* points, zgpu_sample_statistics* stats,
+               const zgpu_solve_options* options, zgpu_solve_report* report);
+
+/*
+ * Batched many-solve: `n_scenes` independent problems in one launch.  points->scene_id
+ * selects the row of queries/pdes/settings for every point.
+ */
+int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
+                       const zgpu_geometric_queries* queries, const zgpu_pde* pdes,
+                       const zgpu_walk_settings* settings, const zgpu_sample_points* points,
+                       zgpu_sample_statistics* stats, const zgpu_solve_options* options,
+                       zgpu_solve_report* report);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZGPU_H */

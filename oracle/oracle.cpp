@@ -1,0 +1,304 @@
+// oracle.cpp -- TEST INFRASTRUCTURE, NOT PRODUCT CODE (see oracle_core.h).
+//
+// C entry points of the CPU oracle for ctypes (tests/, smoke(), bench.py CPU baseline).
+// Mirrors the product C ABI shapes (include/zgpu.h) so tests can call both the same way.
+#include <chrono>
+#include <cstdio>
+#include "oracle_walk.h"
+
+using namespace orc;
+
+namespace {
+
+struct Handle {
+    int dim = 2;
+    void* b = nullptr;
+};
+
+std::atomic<uint64_t> gNodes{0}, gPrims{0};
+
+template <int D>
+Boundary<D>* makeBoundary(const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
+                          const float* kmax, int doubleSided, float silPrec, int useBvh) {
+    Boundary<D>* b = new Boundary<D>();
+    b->kind = kind;
+    b->pos.resize(nV);
+    for (int i = 0; i < nV; i++) b->pos[i] = load<D>(pos + (size_t)i * D);
+    b->idx.resize(nP);
+    for (int i = 0; i < nP; i++) for (int k = 0; k < D; k++) b->idx[i][k] = idx[(size_t)i * D + k];
+    b->kmin.assign(nP, 0.0f);
+    b->kmax.assign(nP, 0.0f);
+    if (kind == ZGPU_BOUNDARY_ROBIN && kmin && kmax) {
+        for (int i = 0; i < nP; i++) { b->kmin[i] = kmin[i]; b->kmax[i] = kmax[i]; }
+    }
+    if (kind == ZGPU_BOUNDARY_ABSORBING) {
+        for (int i = 0; i < nP; i++) { b->kmin[i] = kMaxFloat; b->kmax[i] = kMaxFloat; }
+    }
+    b->buildAdjacency(doubleSided != 0, silPrec);
+    b->useBvh = useBvh != 0;
+    b->buildBvh();
+    return b;
+}
+
+template <int D>
+void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde, const zgpu_walk_settings* ws,
+               const zgpu_sample_points* pts, zgpu_sample_statistics* st, int nThreads, uint64_t* stepsOut) {
+    Queries<D> q;
+    q.absorbing = gq->absorbing ? (const Boundary<D>*)((Handle*)gq->absorbing)->b : nullptr;
+    q.reflecting = gq->reflecting ? (const Boundary<D>*)((Handle*)gq->reflecting)->b : nullptr;
+    for (int i = 0; i < D; i++) { q.domainMin[i] = gq->domain_min[i]; q.domainMax[i] = gq->domain_max[i]; }
+    int64_t n = pts->n;
+    std::atomic<int64_t> next{0};
+    std::atomic<uint64_t> steps{0};
+    auto work = [&]() {
+        uint64_t localSteps = 0;
+        while (true) {
+            int64_t begin = next.fetch_add(16);
+            if (begin >= n) break;
+            int64_t end = std::min(n, begin + 16);
+            for (int64_t i = begin; i < end; i++) {
+                int eq = pts->estimation_quantity ? pts->estimation_quantity[i] : ZGPU_ESTIMATE_SOLUTION;
+                if (eq == ZGPU_ESTIMATE_SKIP) continue;
+                Solver<D> s{q, Pde<D>{pde}, *ws};
+                int nPrev = st->n_solution_estimates[i];
+                s.streamBase = (uint64_t)nPrev;
+                Vec<D> p = load<D>(pts->pt + i * D);
+                Vec<D> nrm = pts->normal ? load<D>(pts->normal + i * D) : Vec<D>();
+                int type = pts->type ? pts->type[i] : ZGPU_SAMPLE_IN_DOMAIN;
+                bool aligned = pts->estimate_normal_aligned ? pts->estimate_normal_aligned[i] != 0 : false;
+                float fsr = pts->first_sphere_radius ? pts->first_sphere_radius[i] : 0.0f;
+                PointStats ps;
+                if (solver == ZGPU_SOLVER_WALK_ON_SPHERES)
+                    s.wosEstimate(p, type, pts->dist_to_absorbing[i], pts->n_walks[i], pts->seed[i], nPrev > 0, aligned, fsr, ps);
+                else
+                    s.wostEstimate(p, nrm, type, pts->dist_to_absorbing[i], pts->n_walks[i], pts->seed[i], nPrev > 0, aligned, fsr, ps);
+                if (pts->first_sphere_radius) pts->first_sphere_radius[i] = fsr;
+                localSteps += ps.steps;
+                // SampleStatistics::merge (common.h:268-310) in FP64
+                if (ps.n > 0) {
+                    int n1 = nPrev, n2 = ps.n, nt = n1 + n2;
+                    if (n1 == 0) { st->solution_mean[i] = ps.mean; st->solution_m2[i] = ps.m2; }
+                    else {
+                        double delta = ps.mean - st->solution_mean[i];
+                        st->solution_mean[i] += delta * ((double)n2 / nt);
+                        st->solution_m2[i] += ps.m2 + delta * delta * ((double)n1 * n2 / nt);
+                    }
+                    st->n_solution_estimates[i] = nt;
+                }
+                st->total_walk_length[i] += ps.walkLength;
+                st->total_splits[i] += ps.splits;
+            }
+        }
+        steps += localSteps;
+    };
+    if (nThreads <= 1) {
+        work();
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nThreads; t++) th.emplace_back(work);
+        for (auto& t : th) t.join();
+    }
+    if (stepsOut) *stepsOut = steps.load();
+}
+
+}  // namespace
+
+
+extern "C" int orc_hardware_threads() { return (int)std::thread::hardware_concurrency(); }
+
+extern "C" void* orc_boundary_create(int dim, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
+                          const float* kmax, int doubleSided, float silPrec, int useBvh) {
+    Handle* h = new Handle();
+    h->dim = dim;
+    if (dim == 2) h->b = makeBoundary<2>(pos, nV, idx, nP, kind, kmin, kmax, doubleSided, silPrec, useBvh);
+    else h->b = makeBoundary<3>(pos, nV, idx, nP, kind, kmin, kmax, doubleSided, silPrec, useBvh);
+    return h;
+}
+
+extern "C" void orc_boundary_destroy(void* hp) {
+    Handle* h = (Handle*)hp;
+    if (!h) return;
+    if (h->dim == 2) delete (Boundary<2>*)h->b; else delete (Boundary<3>*)h->b;
+    delete h;
+}
+
+// silhouette flags as built (for tests): hasAdj and ignore bits per primitive feature
+extern "C" void orc_boundary_flags(void* hp, int* hasAdj, int* ignore) {
+    Handle* h = (Handle*)hp;
+    if (h->dim == 2) {
+        auto* b = (Boundary<2>*)h->b;
+        for (int i = 0; i < b->nPrims(); i++) for (int j = 0; j < 2; j++) { hasAdj[i * 2 + j] = b->hasAdj[i][j]; ignore[i * 2 + j] = b->ignore[i][j]; }
+    } else {
+        auto* b = (Boundary<3>*)h->b;
+        for (int i = 0; i < b->nPrims(); i++) for (int j = 0; j < 3; j++) { hasAdj[i * 3 + j] = b->hasAdj[i][j]; ignore[i * 3 + j] = b->ignore[i][j]; }
+    }
+}
+
+extern "C" double orc_signed_volume(void* hp) {
+    Handle* h = (Handle*)hp;
+    return h->dim == 2 ? ((Boundary<2>*)h->b)->signedVolume() : ((Boundary<3>*)h->b)->signedVolume();
+}
+
+#define ORC_DISPATCH(h, body2, body3) \
+    if ((h)->dim == 2) { auto* b = (Boundary<2>*)(h)->b; constexpr int D = 2; (void)b; (void)D; body2; } \
+    else { auto* b = (Boundary<3>*)(h)->b; constexpr int D = 3; (void)b; (void)D; body3; }
+
+template <int D>
+static void closestImpl(const Boundary<D>* b, int64_t n, const float* x, float* pt, float* nrm, float* d, int* prim) {
+    for (int64_t i = 0; i < n; i++) {
+        Vec<D> p, nn; float dd; int pi = -1;
+        bool ok = b->closestPoint(load<D>(x + i * D), p, nn, dd, pi);
+        if (!ok) { p = Vec<D>(); nn = Vec<D>(); dd = kMaxFloat; }
+        if (pt) store<D>(p, pt + i * D);
+        if (nrm) store<D>(nn, nrm + i * D);
+        if (d) d[i] = dd;
+        if (prim) prim[i] = pi;
+    }
+}
+extern "C" int orc_closest_point(void* hp, int64_t n, const float* x, float* pt, float* nrm, float* d, int* prim) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h, closestImpl<2>(b, n, x, pt, nrm, d, prim), closestImpl<3>(b, n, x, pt, nrm, d, prim));
+    return 0;
+}
+
+template <int D>
+static void intersectImpl(const Boundary<D>* b, int64_t n, const float* o, const float* nrmIn, const float* dir,
+                          const float* tmax, const int* onb, int* hit, float* pt, float* nrm, float* dist, int* prim) {
+    for (int64_t i = 0; i < n; i++) {
+        Vec<D> origin = load<D>(o + i * D);
+        if (onb && onb[i]) origin = offsetPointAlongDirection<D>(origin, -load<D>(nrmIn + i * D));
+        Vec<D> p, nn; float t = kMaxFloat; int pi = -1;
+        bool ok = b->intersect(origin, load<D>(dir + i * D), tmax[i], p, nn, t, pi);
+        hit[i] = ok;
+        if (!ok) { p = Vec<D>(); nn = Vec<D>(); t = kMaxFloat; pi = -1; }
+        if (pt) store<D>(p, pt + i * D);
+        if (nrm) store<D>(nn, nrm + i * D);
+        if (dist) dist[i] = t;
+        if (prim) prim[i] = pi;
+    }
+}
+extern "C" int orc_intersect(void* hp, int64_t n, const float* o, const float* nrmIn, const float* dir, const float* tmax,
+                  const int* onb, int* hit, float* pt, float* nrm, float* dist, int* prim) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h, intersectImpl<2>(b, n, o, nrmIn, dir, tmax, onb, hit, pt, nrm, dist, prim),
+                    intersectImpl<3>(b, n, o, nrmIn, dir, tmax, onb, hit, pt, nrm, dist, prim));
+    return 0;
+}
+
+extern "C" int orc_count_hits(void* hp, int64_t n, const float* o, const float* dir, const float* tmax, int* out) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h,
+        for (int64_t i = 0; i < n; i++) out[i] = b->countHits(load<D>(o + i * D), load<D>(dir + i * D), tmax[i]),
+        for (int64_t i = 0; i < n; i++) out[i] = b->countHits(load<D>(o + i * D), load<D>(dir + i * D), tmax[i]));
+    return 0;
+}
+
+extern "C" int orc_star_radius(void* hp, int64_t n, const float* x, const float* minR, const float* maxR, float prec,
+                    const int* flip, float* out) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h,
+        for (int64_t i = 0; i < n; i++) out[i] = b->starRadius(load<D>(x + i * D), minR[i], maxR[i], prec, flip && flip[i]),
+        for (int64_t i = 0; i < n; i++) out[i] = b->starRadius(load<D>(x + i * D), minR[i], maxR[i], prec, flip && flip[i]));
+    return 0;
+}
+
+template <int D>
+static void occludedImpl(const Boundary<D>* b, int64_t n, const float* xi, const float* xj, const float* ni,
+                         const float* nj, const int* oi, const int* oj, int* out) {
+    for (int64_t k = 0; k < n; k++) {
+        Vec<D> p1 = load<D>(xi + k * D), p2 = load<D>(xj + k * D);
+        if (oi && oi[k]) p1 = offsetPointAlongDirection<D>(p1, -load<D>(ni + k * D));
+        if (oj && oj[k]) p2 = offsetPointAlongDirection<D>(p2, -load<D>(nj + k * D));
+        out[k] = b->occluded(p1, p2);
+    }
+}
+extern "C" int orc_occluded(void* hp, int64_t n, const float* xi, const float* xj, const float* ni, const float* nj,
+                 const int* oi, const int* oj, int* out) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h, occludedImpl<2>(b, n, xi, xj, ni, nj, oi, oj, out), occludedImpl<3>(b, n, xi, xj, ni, nj, oi, oj, out));
+    return 0;
+}
+
+template <int D>
+static void sampleImpl(const Boundary<D>* b, int64_t n, const float* x, const float* r, const float* u, int* found,
+                       float* pt, float* nrm, float* pdf) {
+    for (int64_t k = 0; k < n; k++) {
+        Vec<D> p, nn; float pp = 0.0f;
+        bool ok = b->sample(load<D>(x + k * D), r[k], u + k * D, p, nn, pp);
+        found[k] = ok;
+        if (!ok) { p = Vec<D>(); nn = Vec<D>(); pp = 0.0f; }
+        store<D>(p, pt + k * D); store<D>(nn, nrm + k * D); pdf[k] = pp;
+    }
+}
+extern "C" int orc_sample(void* hp, int64_t n, const float* x, const float* r, const float* u, int* found, float* pt, float* nrm,
+               float* pdf) {
+    Handle* h = (Handle*)hp;
+    ORC_DISPATCH(h, sampleImpl<2>(b, n, x, r, u, found, pt, nrm, pdf), sampleImpl<3>(b, n, x, r, u, found, pt, nrm, pdf));
+    return 0;
+}
+
+// Green's function helpers for identity tests (distributions.h)
+extern "C" float orc_greens_norm(int dim, int yukawa, float lambda, float R) {
+    if (dim == 2) {
+        std::unique_ptr<GreensFnBall<2>> g(yukawa ? (GreensFnBall<2>*)new YukawaGreensFnBall<2>(lambda) : new HarmonicGreensFnBall<2>());
+        g->updateBall(Vec<2>(), R); return g->norm();
+    }
+    std::unique_ptr<GreensFnBall<3>> g(yukawa ? (GreensFnBall<3>*)new YukawaGreensFnBall<3>(lambda) : new HarmonicGreensFnBall<3>());
+    g->updateBall(Vec<3>(), R); return g->norm();
+}
+extern "C" float orc_greens_evaluate(int dim, int yukawa, float lambda, float R, float r) {
+    if (dim == 2) {
+        std::unique_ptr<GreensFnBall<2>> g(yukawa ? (GreensFnBall<2>*)new YukawaGreensFnBall<2>(lambda) : new HarmonicGreensFnBall<2>());
+        g->updateBall(Vec<2>(), R); return g->evaluate(r);
+    }
+    std::unique_ptr<GreensFnBall<3>> g(yukawa ? (GreensFnBall<3>*)new YukawaGreensFnBall<3>(lambda) : new HarmonicGreensFnBall<3>());
+    g->updateBall(Vec<3>(), R); return g->evaluate(r);
+}
+// draws n radii from GreensFnBall::sampleVolume(dir, ...) with pcg32(seed, 0)
+extern "C" void orc_greens_sample_radii(int dim, int yukawa, float lambda, float R, uint64_t seed, int n, float* out) {
+    Pcg32 rng(seed, 0);
+    float r, pdf;
+    if (dim == 2) {
+        std::unique_ptr<GreensFnBall<2>> g(yukawa ? (GreensFnBall<2>*)new YukawaGreensFnBall<2>(lambda) : new HarmonicGreensFnBall<2>());
+        g->updateBall(Vec<2>(), R);
+        Vec<2> d; d[0] = 1.0f;
+        for (int i = 0; i < n; i++) { g->sampleVolume(d, rng, r, pdf); out[i] = r; }
+    } else {
+        std::unique_ptr<GreensFnBall<3>> g(yukawa ? (GreensFnBall<3>*)new YukawaGreensFnBall<3>(lambda) : new HarmonicGreensFnBall<3>());
+        g->updateBall(Vec<3>(), R);
+        Vec<3> d; d[0] = 1.0f;
+        for (int i = 0; i < n; i++) { g->sampleVolume(d, rng, r, pdf); out[i] = r; }
+    }
+}
+extern "C" double orc_bessel(int which, double x) {
+    switch (which) { case 0: return bessel::i0(x); case 1: return bessel::i1(x); case 2: return bessel::k0(x); default: return bessel::k1(x); }
+}
+extern "C" void orc_pcg32(uint64_t seed, uint64_t stream, int n, uint32_t* outU, float* outF) {
+    Pcg32 a(seed, stream), b(seed, stream);
+    for (int i = 0; i < n; i++) { if (outU) outU[i] = a.nextUInt(); if (outF) outF[i] = b.nextFloat(); }
+}
+extern "C" void orc_offset_point(int dim, const float* p, const float* n, float* out) {
+    if (dim == 2) store<2>(offsetPointAlongDirection<2>(load<2>(p), load<2>(n)), out);
+    else store<3>(offsetPointAlongDirection<3>(load<3>(p), load<3>(n)), out);
+}
+extern "C" void orc_eval_pde(int dim, const zgpu_pde* pde, int64_t n, const float* x, const float* nrm, float* src, float* dir,
+                  float* rob) {
+    for (int64_t i = 0; i < n; i++) {
+        if (dim == 2) {
+            Pde<2> p{pde}; Vec<2> xx = load<2>(x + i * 2), nn = nrm ? load<2>(nrm + i * 2) : Vec<2>();
+            if (src) src[i] = p.source(xx); if (dir) dir[i] = p.dirichlet(xx, false); if (rob) rob[i] = p.robin(xx, nn, false);
+        } else {
+            Pde<3> p{pde}; Vec<3> xx = load<3>(x + i * 3), nn = nrm ? load<3>(nrm + i * 3) : Vec<3>();
+            if (src) src[i] = p.source(xx); if (dir) dir[i] = p.dirichlet(xx, false); if (rob) rob[i] = p.robin(xx, nn, false);
+        }
+    }
+}
+
+// WalkOnSpheres/WalkOnStars::solve over all points with nThreads std::threads (TBB stand-in)
+extern "C" int orc_solve(int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_walk_settings* ws,
+              const zgpu_sample_points* pts, zgpu_sample_statistics* st, int nThreads, uint64_t* steps) {
+    if (q->dim == 2) solveImpl<2>(solver, q, pde, ws, pts, st, nThreads, steps);
+    else solveImpl<3>(solver, q, pde, ws, pts, st, nThreads, steps);
+    return 0;
+}
+
