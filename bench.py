@@ -1,0 +1,373 @@
+"""Walk-steps/s benchmark of the GB300 walk engine.
+
+Default workload (one GPU): 2D mixed Dirichlet/Neumann Walk on Stars on the star polygon
+r(t) = 1 + 0.3 sin 5t with 4096 FP32 segments (Dirichlet for t in [0, pi), Neumann for
+t in [pi, 2pi)), u = e^x cos y + 0.25 (x^2 + y^2), f = -1, a 256 x 256 grid of interior
+points, 512 walks per point, epsilon shell 1e-3, max 1024 steps.  One step = one
+WalkOnStars::solve over every point (fresh statistics).  Synthetic data only.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mixed_wost_2d|laplace_wos_2d|...]
+  python bench.py --impl reference ...   # the restated reference CPU path on the host cores
+
+For N > 1 (torchrun) every rank solves the full workload with its own seeds (independent
+walks, no collective on the data path; weak scaling), and rank 0 reports the aggregate.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "mixed_wost_2d": dict(fn="mixed_wost_2d", kw=dict(n_segments=4096, grid=256, spp=512, sigma=0.0),
+                          desc="2D mixed Dirichlet/Neumann WoSt, 4096 segments, 256x256 grid, 512 spp, f=-1"),
+    "mixed_wost_2d_screened": dict(fn="mixed_wost_2d", kw=dict(n_segments=4096, grid=256, spp=512, sigma=1.0),
+                                   desc="2D mixed WoSt, screened Poisson sigma=1, 4096 segments, 256x256 grid, 512 spp"),
+    "laplace_wos_2d": dict(fn="laplace_wos_2d", kw=dict(n_segments=1024, grid=128, spp=256),
+                           desc="2D Laplace WoS, 1024 segments, 128x128 grid, 256 spp"),
+    "robin_wost_3d": dict(fn="robin_wost_3d", kw=dict(level=6, n_points=1_000_000, spp=128),
+                          desc="3D Robin WoSt, icosphere L6 (81,920 tris), 1M points, 128 spp, kappa=2"),
+}
+
+# algorithmic bytes per traversal unit under the oracle's binary SAH BVH (leaf 4):
+# node = box + child offsets (2D 24 B, 3D 32 B); segment 16 B, triangle 36 B; reflecting
+# primitives add their silhouette record (2D 32 B, 3D 48 B) in star-radius queries.
+NODE_BYTES = {2: 24, 3: 32}
+PRIM_BYTES = {2: 16, 3: 36}
+SIL_BYTES = {2: 32, 3: 48}
+STATE_BYTES = {2: 48, 3: 72}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, index=0, period_ms=200):
+        self.index = index
+        self.period_ms = period_ms
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          f"-lms={self.period_ms}", f"-i={self.index}"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes_per_step(problem, n_points=None):
+    """Traversal bytes per walk step from the oracle's binary BVH work counters (a seeded
+    sample of the same workload)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from zombie_gb300 import problems as P
+    from zombie_gb300 import _abi as A
+    pr = problem
+    D = pr.dim
+    idx = np.random.default_rng(7).choice(pr.points.shape[0], min(n_points or 256, pr.points.shape[0]), replace=False)
+    pts = pr.points[idx]
+    ab = O.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
+    rf = None
+    if pr.reflecting is not None and len(pr.reflecting[1]):
+        k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32) if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN else None
+        rf = O.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
+                        silhouette_precision=pr.ignore_silhouette_precision)
+    d = ab.closest_point(pts)[2] if ab is not None else \
+        np.linalg.norm(np.minimum(pr.domain_min - pts, pts - pr.domain_max), axis=1).astype(np.float32)
+    n = pts.shape[0]
+    sp = dict(pt=pts, dist_to_absorbing=d, n_walks=np.full(n, 64, np.int32), seed=P.seeds_for(n),
+              first_sphere_radius=np.zeros(n, np.float32))
+    st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+              total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
+    O.counters()
+    steps = O.solve(pr.solver, D, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, sp, st)
+    c = O.counters()
+    total = 0.0
+    for kind, v in c.items():
+        total += v["nodes"] * NODE_BYTES[D] + v["prims"] * PRIM_BYTES[D]
+        if kind == "star_radius":
+            total += v["prims"] * SIL_BYTES[D]
+    per_step = total / max(steps, 1) + 2 * STATE_BYTES[D]
+    return per_step, {k: {kk: vv / max(steps, 1) for kk, vv in v.items()} for k, v in c.items()}
+
+
+def cpu_baseline(problem, budget_s=15.0, threads=None):
+    """The restated reference CPU path (oracle, all host threads) on a bounded sample of the
+    same workload: a random subset of the points with the full walk count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from zombie_gb300 import problems as P
+    from zombie_gb300 import _abi as A
+    pr = problem
+    D = pr.dim
+    threads = threads or os.cpu_count()
+    ab = O.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
+    rf = None
+    if pr.reflecting is not None and len(pr.reflecting[1]):
+        k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32) if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN else None
+        rf = O.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
+                        silhouette_precision=pr.ignore_silhouette_precision)
+    rng = np.random.default_rng(11)
+    order = rng.permutation(pr.points.shape[0])
+    done_steps, t_used, used_pts = 0, 0.0, 0
+    chunk = 64
+    while t_used < budget_s and used_pts < len(order):
+        idx = order[used_pts:used_pts + chunk]
+        pts = pr.points[idx]
+        n = pts.shape[0]
+        d = ab.closest_point(pts)[2] if ab is not None else \
+            np.linalg.norm(np.minimum(pr.domain_min - pts, pts - pr.domain_max), axis=1).astype(np.float32)
+        sp = dict(pt=pts, dist_to_absorbing=d, n_walks=pr.n_walks[idx], seed=P.seeds_for(n, 99),
+                  first_sphere_radius=np.zeros(n, np.float32))
+        st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+                  total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
+        t0 = time.perf_counter()
+        done_steps += O.solve(pr.solver, D, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, sp, st, threads)
+        t_used += time.perf_counter() - t0
+        used_pts += n
+        chunk = min(chunk * 2, 4096)
+    return dict(value=done_steps / t_used, unit="walk-steps/s", cores=threads, kind="port",
+                sample=f"{used_pts} of {pr.points.shape[0]} points x full walks/point, {done_steps} steps in {t_used:.1f} s")
+
+
+def make_problem(name):
+    from zombie_gb300 import problems as P
+    w = WORKLOADS[name]
+    return getattr(P, w["fn"])(**w["kw"]), w["desc"]
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pr, desc = make_problem(args.workload)
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        base = cpu_baseline(pr, budget_s=args.cpu_budget / max(1, args.steps))
+        if i >= args.warmup:
+            vals.append(base["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": "walk-steps/s", "value": v, "unit": "walk-steps/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc},
+            "cpu_baseline": dict(base, value=v),
+            "e2e": {"value": v, "unit": "walk-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from zombie_gb300 import build as B
+    if rank == 0:
+        B.build()
+    if dist:
+        tdist.barrier()
+    from zombie_gb300 import Context
+    from zombie_gb300 import _abi as A
+    from zombie_gb300.api import SampleArrays
+    from zombie_gb300.runner import GpuProblem, summarize
+    pr, desc = make_problem(args.workload)
+    ctx = Context(local)
+    gp = GpuProblem(pr, context=ctx, seed_base=0x5eed + rank)
+    P_all = pr.points.shape[0]
+    dev = gp.device_arrays()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    zero_keys = ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
+                 "first_sphere_radius")
+
+    def reset(arr):
+        for k in zero_keys:
+            arr[k].zero_()
+
+    def step(arr):
+        reset(arr)
+        return gp.solve(arr)
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            step(dev)
+    torch.cuda.synchronize()
+    # L2 flush buffer (inputs are small; flush between timed steps)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    total_steps = 0
+    kernel_ms = []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        walk_ms = 0.0
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                ev0.record(stream)
+                rep = step(dev)
+                ev1.record(stream)
+            ev1.synchronize()
+            walk_ms += ev0.elapsed_time(ev1)
+            kernel_ms.append(rep.kernel_ms)
+            total_steps += rep.total_steps
+        torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+    t = torch.tensor([walk_ms, float(total_steps)], dtype=torch.float64, device="cuda")
+    if dist:
+        tmax = t.clone(); tdist.all_reduce(tmax[0:1], op=tdist.ReduceOp.MAX)
+        tdist.all_reduce(t[1:2], op=tdist.ReduceOp.SUM)
+        walk_ms, total_steps = float(tmax[0]), float(t[1])
+    g = summarize(dev, pr.exact())
+    value = total_steps / (walk_ms / 1e3)
+    ms_per_step = walk_ms / args.steps
+
+    # end to end through the public API with pinned host buffers (copies inside the timed region)
+    h = gp.host_arrays()
+    pinned = {}
+    for k, v in h.arrays.items():
+        tt = torch.from_numpy(np.ascontiguousarray(v).view(np.int64) if v.dtype == np.uint64 else np.ascontiguousarray(v)).pin_memory()
+        pinned[k] = tt.numpy().view(np.uint64) if v.dtype == np.uint64 else tt.numpy()
+    harr = SampleArrays(**pinned)
+    h2d = sum(v.nbytes for k, v in pinned.items())
+    d2h = sum(pinned[k].nbytes for k in ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length",
+                                         "total_splits", "first_sphere_radius"))
+    e2e_steps = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(max(1, args.steps)):
+        for k in zero_keys:
+            harr.arrays[k][:] = 0
+        rep = gp.solve(harr)
+        e2e_steps += rep.total_steps
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_val = e2e_steps / e2e_s
+    if dist:
+        tt = torch.tensor([e2e_s, float(e2e_steps)], dtype=torch.float64, device="cuda")
+        tdist.all_reduce(tt[0:1], op=tdist.ReduceOp.MAX)
+        tdist.all_reduce(tt[1:2], op=tdist.ReduceOp.SUM)
+        e2e_val = float(tt[1]) / float(tt[0])
+
+    line = None
+    if rank == 0:
+        hbm, peak_kind = measured_peaks()
+        per_step_bytes, work = algorithmic_bytes_per_step(pr)
+        mean_kernel_ms = float(np.mean(kernel_ms))
+        steps_per_launch = total_steps / args.steps / (ws if dist else 1)
+        achieved = per_step_bytes * steps_per_launch / (mean_kernel_ms / 1e3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+        if os.path.exists(tp):
+            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+        cpu = cpu_baseline(pr, budget_s=args.cpu_budget) if not args.skip_cpu else None
+        line = {
+            "metric": "walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "points": int(P_all),
+                       "walks_per_point": int(pr.n_walks[0]), "parallelism": f"points x{ws}",
+                       "l2": "256 MiB buffer written between timed steps"},
+            "rmse_vs_exact": g["rmse"], "mean_walk_length": g["mean_walk_length"],
+            "e2e": {"value": e2e_val, "unit": "walk-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": 6 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_step": per_step_bytes, "kernel_ms": mean_kernel_ms},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        tdist.barrier()
+        tdist.destroy_process_group()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

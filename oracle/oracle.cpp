@@ -15,7 +15,7 @@ struct Handle {
     void* b = nullptr;
 };
 
-std::atomic<uint64_t> gNodes{0}, gPrims{0};
+std::atomic<uint64_t> gCounters[15];
 
 template <int D>
 Boundary<D>* makeBoundary(const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
@@ -37,6 +37,7 @@ Boundary<D>* makeBoundary(const float* pos, int nV, const int* idx, int nP, int 
     b->buildAdjacency(doubleSided != 0, silPrec);
     b->useBvh = useBvh != 0;
     b->buildBvh();
+    b->buildCones();
     return b;
 }
 
@@ -90,6 +91,11 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
             }
         }
         steps += localSteps;
+        Counters& c = counters();
+        for (int k = 0; k < 5; k++) {
+            gCounters[k] += c.calls[k]; gCounters[5 + k] += c.nodes[k]; gCounters[10 + k] += c.prims[k];
+            c.calls[k] = c.nodes[k] = c.prims[k] = 0;
+        }
     };
     if (nThreads <= 1) {
         work();
@@ -103,6 +109,11 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
 
 }  // namespace
 
+
+// traversal counters accumulated by orc_solve: calls[5], nodes[5], prims[5]; reset after read
+extern "C" void orc_counters(uint64_t* out) {
+    for (int k = 0; k < 15; k++) out[k] = gCounters[k].exchange(0);
+}
 
 extern "C" int orc_hardware_threads() { return (int)std::thread::hardware_concurrency(); }
 

@@ -68,6 +68,7 @@ def lib():
         L.orc_eval_pde.argtypes = [i32, vp, i64, vp, vp, vp, vp, vp]
         L.orc_solve.argtypes = [i32, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_uint64)]
         L.orc_hardware_threads.restype = i32
+        L.orc_counters.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -155,6 +156,17 @@ class Boundary:
         lib().orc_sample(self.h, n, A.ptr(x), A.ptr(_f32(radius)), A.ptr(_f32(u)), A.ptr(found), A.ptr(pt),
                          A.ptr(nrm), A.ptr(pdf))
         return found, pt, nrm, pdf
+
+
+QUERY_KINDS = ("closest_point", "first_hit", "line_of_sight", "star_radius", "sample")
+
+
+def counters():
+    """Traversal work of the solves since the last call: per query kind calls, nodes, prims."""
+    out = np.zeros(15, np.uint64)
+    lib().orc_counters(A.ptr(out))
+    return {k: dict(calls=int(out[i]), nodes=int(out[5 + i]), prims=int(out[10 + i]))
+            for i, k in enumerate(QUERY_KINDS)}
 
 
 def pcg32(seed, stream, n):

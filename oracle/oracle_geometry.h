@@ -251,6 +251,11 @@ inline float branchWeight(float r2) {
     return std::fabs(1.0f / (4.0f * kPi * r));
 }
 
+// traversal work counters (per thread; summed by the solve driver): per query kind
+// [0] closest point, [1] first ray hit, [2] line of sight, [3] star radius, [4] sampling
+struct Counters { uint64_t calls[5] = {0}, nodes[5] = {0}, prims[5] = {0}; };
+inline Counters& counters() { static thread_local Counters c; return c; }
+
 template <int D>
 struct Box {
     Vec<D> lo = Vec<D>::constant(kMaxFloat), hi = Vec<D>::constant(-kMaxFloat);
@@ -287,7 +292,10 @@ struct Boundary {
     std::vector<std::array<uint8_t, D>> hasAdj, ignore;
     std::vector<float> kmin, kmax;
     // binary SAH BVH
-    struct Node { Box<D> box; int left = -1, right = -1, start = 0, count = 0; float area = 0.0f; };
+    struct Node {
+        Box<D> box; int left = -1, right = -1, start = 0, count = 0; float area = 0.0f;
+        float axis[3] = {0, 0, 0}; float halfAngle = 3.14159265f; float kmax = 0.0f;   // silhouette cone
+    };
     std::vector<Node> nodes;
     std::vector<int> order;
     bool useBvh = true;
@@ -300,11 +308,14 @@ struct Boundary {
 
     void buildAdjacency(bool solveDoubleSided, float silhouettePrecision);
     void buildBvh();
+    void buildCones();
+    bool coneMayHoldSilhouette(const Node& nd, const Vec<D>& x, float prec) const;
     int buildRecursive(int start, int end, std::vector<Vec<D>>& centroids, int depth);
 
     // queries
     bool closestPoint(const Vec<D>& x, Vec<D>& pt, Vec<D>& n, float& d, int& primOut) const;
-    bool intersect(const Vec<D>& o, const Vec<D>& dir, float tMax, Vec<D>& pt, Vec<D>& n, float& t, int& primOut) const;
+    bool intersect(const Vec<D>& o, const Vec<D>& dir, float tMax, Vec<D>& pt, Vec<D>& n, float& t, int& primOut,
+                   int kind = 1) const;
     int countHits(const Vec<D>& o, const Vec<D>& dir, float tMax) const;
     bool occluded(const Vec<D>& a, const Vec<D>& b) const;
     void primStarRadius(int i, const Vec<D>& c, float& r2, bool flip, float precision) const;
@@ -450,7 +461,10 @@ void Boundary<D>::buildBvh() {
 template <int D>
 bool Boundary<D>::closestPoint(const Vec<D>& x, Vec<D>& ptOut, Vec<D>& nOut, float& dOut, int& primOut) const {
     float best = kMaxFloat; int bestPrim = -1; Vec<D> bestPt;
+    Counters& C = counters();
+    C.calls[0]++;
     auto test = [&](int i) {
+        C.prims[0]++;
         Vec<D> p[D]; prim(i, p); Vec<D> q;
         float d = closestPointPrim(p, x, q);
         if (d < best || (d == best && i < bestPrim)) { best = d; bestPrim = i; bestPt = q; }
@@ -464,6 +478,7 @@ bool Boundary<D>::closestPoint(const Vec<D>& x, Vec<D>& ptOut, Vec<D>& nOut, flo
             sp--; int ni = stack[sp]; float d2 = sd[sp];
             if (d2 > best * best) continue;
             const Node& nd = nodes[ni];
+            C.nodes[0]++;
             if (nd.count > 0) { for (int k = 0; k < nd.count; k++) test(order[nd.start + k]); continue; }
             float dl = nodes[nd.left].box.dist2(x), dr = nodes[nd.right].box.dist2(x);
             if (dl <= dr) { stack[sp] = nd.right; sd[sp++] = dr; stack[sp] = nd.left; sd[sp++] = dl; }
@@ -477,9 +492,13 @@ bool Boundary<D>::closestPoint(const Vec<D>& x, Vec<D>& ptOut, Vec<D>& nOut, flo
 
 // first hit (fcpw Aggregate::intersect(ray) at fcpw_geometric_queries.h:1107, :1188)
 template <int D>
-bool Boundary<D>::intersect(const Vec<D>& o, const Vec<D>& dir, float tMax, Vec<D>& ptOut, Vec<D>& nOut, float& tOut, int& primOut) const {
+bool Boundary<D>::intersect(const Vec<D>& o, const Vec<D>& dir, float tMax, Vec<D>& ptOut, Vec<D>& nOut, float& tOut, int& primOut,
+                            int kind) const {
     float best = tMax; int bestPrim = -1;
+    Counters& C = counters();
+    C.calls[kind]++;
     auto test = [&](int i) {
+        C.prims[kind]++;
         Vec<D> p[D]; prim(i, p); float t;
         if (intersectPrim(p, o, dir, best, t)) {
             if (bestPrim < 0 || t < best || (t == best && i < bestPrim)) { best = t; bestPrim = i; }
@@ -493,6 +512,7 @@ bool Boundary<D>::intersect(const Vec<D>& o, const Vec<D>& dir, float tMax, Vec<
         while (sp > 0) {
             int ni = stack[--sp];
             const Node& nd = nodes[ni];
+            C.nodes[kind]++;
             if (!nd.box.rayOverlap(o, invD, best)) continue;
             if (nd.count > 0) { for (int k = 0; k < nd.count; k++) test(order[nd.start + k]); continue; }
             stack[sp++] = nd.right; stack[sp++] = nd.left;
@@ -518,7 +538,7 @@ bool Boundary<D>::occluded(const Vec<D>& a, const Vec<D>& b) const {
     if (len <= 0.0f) return false;
     dir = dir / len;
     Vec<D> pt, n; float t; int pi;
-    return intersect(a, dir, len, pt, n, t, pi);
+    return intersect(a, dir, len, pt, n, t, pi, 2);
 }
 
 // reflectance_boundary_bvh/geometry.h:85-154 (2D) and :169-236 (3D)
@@ -591,15 +611,25 @@ template <int D>
 float Boundary<D>::starRadius(const Vec<D>& x, float minR, float maxR, float precision, bool flip) const {
     if (minR > maxR) return maxR;
     float r2 = maxR < kMaxFloat ? maxR * maxR : kMaxFloat;
+    Counters& C = counters();
+    C.calls[3]++;
     if (!useBvh || nodes.empty()) {
         for (int i = 0; i < nPrims(); i++) primStarRadius(i, x, r2, flip, precision);
+        C.prims[3] += nPrims();
     } else {
         int stack[128]; int sp = 0; stack[sp++] = 0;
         while (sp > 0) {
             int ni = stack[--sp];
             const Node& nd = nodes[ni];
+            C.nodes[3]++;
             if (nd.box.dist2(x) > r2) continue;
-            if (nd.count > 0) { for (int k = 0; k < nd.count; k++) primStarRadius(order[nd.start + k], x, r2, flip, precision); continue; }
+            // subtrees without Robin reflectance only matter through their silhouettes
+            if (nd.kmax <= kFcpwEpsilon && !coneMayHoldSilhouette(nd, x, precision)) continue;
+            if (nd.count > 0) {
+                for (int k = 0; k < nd.count; k++) primStarRadius(order[nd.start + k], x, r2, flip, precision);
+                C.prims[3] += nd.count;
+                continue;
+            }
             float dl = nodes[nd.left].box.dist2(x), dr = nodes[nd.right].box.dist2(x);
             if (dl <= dr) { stack[sp++] = nd.right; stack[sp++] = nd.left; }
             else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
@@ -639,7 +669,10 @@ bool Boundary<D>::sample(const Vec<D>& x, float radius, const float* uIn, Vec<D>
     float u0 = uIn[0];
     float prob = 1.0f;
     int chosen = -1;
+    Counters& C = counters();
+    C.calls[4]++;
     auto primWeight = [&](int i) -> float {
+        C.prims[4]++;
         Vec<D> p[D]; prim(i, p); Vec<D> q;
         float d = closestPointPrim(p, x, q);
         return (d * d <= R2) ? primArea(p) * branchWeight(d * d) : 0.0f;
@@ -653,6 +686,7 @@ bool Boundary<D>::sample(const Vec<D>& x, float radius, const float* uIn, Vec<D>
         if (nodes[0].box.dist2(x) > R2) return false;
         while (true) {
             const Node& nd = nodes[ni];
+            C.nodes[4]++;
             if (nd.count > 0) {
                 float w[8];
                 for (int k = 0; k < nd.count; k++) w[k] = primWeight(order[nd.start + k]);
@@ -677,6 +711,77 @@ bool Boundary<D>::sample(const Vec<D>& x, float radius, const float* uIn, Vec<D>
     ptOut = samplePointOnPrim(p, uu, nOut, primPdf);
     pdfOut = prob * primPdf;
     return true;
+}
+
+// normal cone per node over the faces adjacent to its non-ignored silhouette features
+// (halfAngle < 0: no candidate; pi: an open feature or a degenerate axis) and the max
+// Robin coefficient of the subtree
+template <int D>
+void Boundary<D>::buildCones() {
+    if (nodes.empty() || kind == ZGPU_BOUNDARY_ABSORBING) return;
+    for (auto& nd : nodes) {
+        std::vector<int> stk = {(int)(&nd - &nodes[0])};
+        std::vector<Vec<D>> ns;
+        bool open = false;
+        float km = 0.0f;
+        while (!stk.empty()) {
+            const Node& m = nodes[stk.back()]; stk.pop_back();
+            if (m.count == 0) { stk.push_back(m.left); stk.push_back(m.right); continue; }
+            for (int k = 0; k < m.count; k++) {
+                int i = order[m.start + k];
+                km = std::max(km, kmax[i]);
+                bool any = false;
+                for (int j = 0; j < D; j++) {
+                    if (ignore[i][j]) continue;
+                    if (!hasAdj[i][j]) { open = true; continue; }
+                    ns.push_back(adjN[i][j]);
+                    any = true;
+                }
+                if (any) ns.push_back(normalOf(i));
+            }
+        }
+        nd.kmax = km;
+        if (open) { nd.halfAngle = kPi; continue; }
+        if (ns.empty()) { nd.halfAngle = -1.0f; continue; }
+        double a[3] = {0, 0, 0};
+        for (auto& n : ns) for (int i = 0; i < D; i++) a[i] += n[i];
+        double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        if (l < 1e-6) { nd.halfAngle = kPi; continue; }
+        for (int i = 0; i < 3; i++) nd.axis[i] = (float)(a[i] / l);
+        double h = 0.0;
+        for (auto& n : ns) {
+            double c = 0.0;
+            for (int i = 0; i < D; i++) c += nd.axis[i] * n[i];
+            h = std::max(h, std::acos(std::max(-1.0, std::min(1.0, c))));
+        }
+        nd.halfAngle = (float)std::min((double)kPi, h + 1e-4);
+    }
+}
+
+// all normal/view angles on one side of pi/2 (beyond the silhouette test's precision band)
+// -> every face front-facing or every face back-facing -> no silhouette in the subtree
+template <int D>
+bool Boundary<D>::coneMayHoldSilhouette(const Node& nd, const Vec<D>& x, float prec) const {
+    if (nd.halfAngle < 0.0f) return false;
+    if (nd.halfAngle >= 0.5f * kPi) return true;
+    Vec<D> c, v;
+    float rb2 = 0.0f;
+    for (int i = 0; i < D; i++) {
+        c[i] = 0.5f * (nd.box.lo[i] + nd.box.hi[i]);
+        float h = 0.5f * (nd.box.hi[i] - nd.box.lo[i]);
+        rb2 += h * h;
+        v[i] = x[i] - c[i];
+    }
+    float rb = std::sqrt(rb2) + prec;
+    float dv = norm(v);
+    if (dv <= rb) return true;
+    Vec<D> a;
+    for (int i = 0; i < D; i++) a[i] = nd.axis[i];
+    float theta = std::acos(std::min(std::max(dot(a, v) / dv, -1.0f), 1.0f));
+    float beta = std::asin(std::min(rb / dv, 1.0f));
+    float margin = std::asin(std::min(prec, 1.0f)) + 1e-3f;
+    float spread = beta + nd.halfAngle;
+    return !(theta + spread < 0.5f * kPi - margin || theta - spread > 0.5f * kPi + margin);
 }
 
 // Aggregate::signedVolume (computeSignedVolume, fcpw_geometric_queries.h:431-458)

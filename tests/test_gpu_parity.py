@@ -1,0 +1,281 @@
+"""GPU parity: every query and solver of libzgpu.so against the CPU oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from zombie_gb300 import _abi as A
+from zombie_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(dim, level=3):
+    if dim == 2:
+        return P.star_polygon(1024)
+    pos, idx, _ = P.displaced_icosphere(level, seed=5)
+    return pos, idx
+
+
+def _handler(zgpu, dim, pos, idx, kind, kappa=None, ignore_prec=0.0):
+    from zombie_gb300 import api
+    ic = api.IgnoreCandidateSilhouette(False, ignore_prec)
+    if kind == A.ZGPU_BOUNDARY_ABSORBING:
+        h = api.GpuDirichletBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx)
+    elif kind == A.ZGPU_BOUNDARY_NEUMANN:
+        h = api.GpuNeumannBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx, ic)
+    else:
+        k = np.full(idx.shape[0], kappa, np.float32)
+        h = api.GpuRobinBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx, ic, k, k)
+    return h
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_closest_point_parity(zgpu, oracle, dim):
+    pos, idx = _scene(dim)
+    x = np.random.default_rng(0).uniform(-1.4, 1.4, (20000, dim)).astype(np.float32)
+    g = _handler(zgpu, dim, pos, idx, A.ZGPU_BOUNDARY_ABSORBING)
+    o = oracle.Boundary(dim, pos, idx, use_bvh=False)
+    gp, gn, gd, gi = g.closest_point(x)
+    op, on, od, oi = o.closest_point(x)
+    # FP32 distances agree within 1e-6 relative, or 2.4e-7 absolute (2 ulp at unit scale) for
+    # points within a few 1e-3 of the surface, where x - closest point cancels
+    err = np.abs(gd - od)
+    tol = np.maximum(1e-6 * od, 2.4e-7)
+    assert np.all(err <= tol)
+    same = gi == oi
+    # indices agree except at ties (the other primitive is equally close within tolerance)
+    assert np.all(same | (err <= tol))
+    assert same.mean() > 0.995
+    assert np.allclose(gp[same], op[same], atol=1e-6)
+    assert np.allclose(gn[same], on[same], atol=1e-6)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_ray_intersection_parity(zgpu, oracle, dim):
+    pos, idx = _scene(dim)
+    rng = np.random.default_rng(1)
+    n = 20000
+    o = rng.uniform(-0.6, 0.6, (n, dim)).astype(np.float32)
+    d = rng.normal(size=(n, dim)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tm = rng.uniform(0.05, 2.5, n).astype(np.float32)
+    z = np.zeros_like(o)
+    on = np.zeros(n, np.int32)
+    g = _handler(zgpu, dim, pos, idx, A.ZGPU_BOUNDARY_NEUMANN)
+    ob = oracle.Boundary(dim, pos, idx, kind=A.ZGPU_BOUNDARY_NEUMANN, use_bvh=False)
+    gh, gpt, gn, gt, gi = g.intersect(o, z, d, tm, on)
+    oh, opt, on_, ot, oi = ob.intersect(o, z, d, tm, on)
+    agree = gh == oh
+    assert agree.mean() > 0.9995          # misses only for hits within float noise of tMax
+    both = (gh == 1) & (oh == 1)
+    assert np.all(np.abs(gt[both] - ot[both]) <= 1e-5 * np.maximum(ot[both], 1.0))
+    assert (gi[both] == oi[both]).mean() > 0.999
+    cnt = g.count_hits(o, d, np.full(n, 1e30, np.float32))
+    assert np.array_equal(cnt, ob.count_hits(o, d, np.full(n, 1e30, np.float32)))
+
+
+@pytest.mark.parametrize("dim,kind,kappa", [(2, A.ZGPU_BOUNDARY_NEUMANN, None), (2, A.ZGPU_BOUNDARY_ROBIN, 2.0),
+                                            (3, A.ZGPU_BOUNDARY_NEUMANN, None), (3, A.ZGPU_BOUNDARY_ROBIN, 2.0)])
+def test_star_radius_parity(zgpu, oracle, dim, kind, kappa):
+    pos, idx = _scene(dim)
+    rng = np.random.default_rng(2)
+    n = 8000
+    x = rng.uniform(-0.7, 0.7, (n, dim)).astype(np.float32)
+    mn = np.full(n, 1e-3, np.float32)
+    mx = rng.uniform(0.05, 2.0, n).astype(np.float32)
+    fl = np.zeros(n, np.int32)
+    g = _handler(zgpu, dim, pos, idx, kind, kappa)
+    k = None if kappa is None else np.full(idx.shape[0], kappa, np.float32)
+    ob = oracle.Boundary(dim, pos, idx, kind=kind, kmin=k, kmax=k, silhouette_precision=0.0, use_bvh=False)
+    gr = g.star_radius(x, mn, mx, 1e-3, fl)
+    orr = ob.star_radius(x, mn, mx, 1e-3, fl)
+    rel = np.abs(gr - orr) / np.maximum(orr, 1e-30)
+    assert np.mean(rel <= 1e-5) > 0.999
+    assert np.all(gr <= np.maximum(mx, mn) * (1 + 1e-6))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_line_of_sight_parity(zgpu, oracle, dim):
+    pos, idx = _scene(dim)
+    rng = np.random.default_rng(3)
+    n = 20000
+    a = rng.uniform(-0.8, 0.8, (n, dim)).astype(np.float32)
+    b = rng.uniform(-0.8, 0.8, (n, dim)).astype(np.float32)
+    z = np.zeros_like(a)
+    off = np.zeros(n, np.int32)
+    g = _handler(zgpu, dim, pos, idx, A.ZGPU_BOUNDARY_NEUMANN)
+    ob = oracle.Boundary(dim, pos, idx, kind=A.ZGPU_BOUNDARY_NEUMANN, use_bvh=False)
+    assert (g.occluded(a, b, z, z, off, off) == ob.occluded(a, b, z, z, off, off)).mean() > 0.9995
+
+
+def test_boundary_sampling_is_unbiased(zgpu):
+    pos, idx = P.star_polygon(1024)
+    g = _handler(zgpu, 2, pos, idx, A.ZGPU_BOUNDARY_NEUMANN)
+    x = np.array([[0.1, -0.5]], np.float32)
+    R, N = 0.6, 400000
+    u = np.random.default_rng(4).random((N, 2)).astype(np.float32)
+    found, pt, _, pdf = g.sample(np.repeat(x, N, 0), np.full(N, R, np.float32), u)
+    d = np.linalg.norm(pt - x, axis=1)
+    G = np.log(R / np.maximum(d, 1e-4)) / (2 * np.pi)
+    val = np.where((found == 1) & (d < R), G * pt[:, 1] / np.maximum(pdf, 1e-30), 0.0)
+    a = pos[idx[:, 0]].astype(np.float64)
+    c = pos[idx[:, 1]].astype(np.float64)
+    t = (np.arange(256) + 0.5) / 256
+    zz = a[:, None, :] + (c - a)[:, None, :] * t[None, :, None]
+    dz = np.linalg.norm(zz - x, axis=2)
+    Gq = np.where(dz < R, np.log(R / np.maximum(dz, 1e-4)) / (2 * np.pi), 0.0)
+    quad = ((Gq * zz[:, :, 1]).mean(1) * np.linalg.norm(c - a, axis=1)).sum()
+    assert abs(val.mean() - quad) <= 4 * val.std() / np.sqrt(N) + 1e-5
+
+
+# ------------------------------------------------------------------------- solvers
+def _gpu_and_oracle(zgpu, oracle, pr):
+    from zombie_gb300.runner import GpuProblem, summarize
+    import test_oracle_solvers as T
+    gp = GpuProblem(pr)
+    arr = gp.host_arrays()
+    rep = gp.solve(arr)
+    g = summarize(arr, pr.exact())
+    st, steps = T.run_oracle(oracle, pr, seeds=gp.seeds)
+    return g, st, steps, rep
+
+
+def _cross_z(g, st):
+    n = st["n_solution_estimates"].astype(np.float64)
+    se_o = np.sqrt(st["solution_m2"] / np.maximum(n - 1, 1) / np.maximum(n, 1))
+    se = np.sqrt(g["se"] ** 2 + se_o ** 2)
+    return (g["mean"] - st["solution_mean"]) / np.maximum(se, 1e-12)
+
+
+def _exact_z(g):
+    return g["err"] / np.maximum(g["se"], 1e-12)
+
+
+CASES = {
+    "wos_laplace_2d": lambda: P.laplace_wos_2d(n_segments=1024, grid=40, spp=256),
+    "wost_mixed_2d": lambda: P.mixed_wost_2d(n_segments=4096, grid=32, spp=256),
+    "wost_screened_2d": lambda: P.mixed_wost_2d(n_segments=2048, grid=24, spp=256, sigma=1.0),
+    "wost_robin_3d": lambda: P.robin_wost_3d(level=4, n_points=400, spp=256),
+    "wos_screened_3d": lambda: P.screened_wos_3d(level=4, n_points=400, spp=256),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_solver_matches_oracle_and_exact(zgpu, oracle, case):
+    pr = CASES[case]()
+    g, st, steps, rep = _gpu_and_oracle(zgpu, oracle, pr)
+    assert rep.error_word == 0 and rep.total_steps > 0
+    # the same walks (same pcg32 streams): totals agree closely, per-point estimates agree
+    assert abs(rep.total_steps - steps) <= 0.02 * steps
+    z = _cross_z(g, st)
+    assert np.mean(np.abs(z) > 3) <= 0.01
+    assert abs(z.mean()) <= 4.0 / np.sqrt(len(z)) + 0.05
+    # and both agree with the FP64 manufactured solution
+    ez = _exact_z(g)
+    assert abs(ez.mean()) <= 0.5
+    assert np.mean(np.abs(ez) > 3.5) <= 0.04
+
+
+def test_wos_walks_reproduce_oracle_walks(zgpu, oracle):
+    """With identical pcg32 streams, WoS walks on the GPU follow the oracle's walks: the
+    per-point means agree far below the Monte Carlo error."""
+    pr = P.laplace_wos_2d(n_segments=1024, grid=24, spp=128)
+    g, st, steps, rep = _gpu_and_oracle(zgpu, oracle, pr)
+    close = np.abs(g["mean"] - st["solution_mean"]) <= 1e-3 * g["se"] + 1e-6
+    assert close.mean() > 0.9
+
+
+def test_progressive_accumulation_matches_single_call(zgpu):
+    from zombie_gb300.runner import GpuProblem
+    pr = P.mixed_wost_2d(n_segments=1024, grid=16, spp=64)
+    gp = GpuProblem(pr)
+    a = gp.host_arrays()
+    gp.solve(a)
+    fsr1 = a["first_sphere_radius"].copy()
+    gp.solve(a)
+    assert np.array_equal(fsr1, a["first_sphere_radius"])
+    b = gp.host_arrays(n_walks=128)
+    gp.solve(b)
+    assert np.array_equal(a["n_solution_estimates"], b["n_solution_estimates"])
+    assert np.allclose(a["solution_mean"], b["solution_mean"], atol=1e-9)
+    assert np.allclose(a["solution_m2"], b["solution_m2"], rtol=1e-8, atol=1e-8)
+
+
+def test_device_and_host_memory_paths_agree(zgpu):
+    from zombie_gb300.runner import GpuProblem
+    pr = P.mixed_wost_2d(n_segments=2048, grid=24, spp=64)
+    gp = GpuProblem(pr)
+    h = gp.host_arrays()
+    gp.solve(h)
+    d = gp.device_arrays()
+    gp.solve(d)
+    assert np.array_equal(h["n_solution_estimates"], d["n_solution_estimates"].cpu().numpy())
+    assert np.allclose(h["solution_mean"], d["solution_mean"].cpu().numpy(), atol=1e-12)
+
+
+def test_russian_roulette_and_splitting(zgpu, oracle):
+    pr = P.laplace_wos_2d(n_segments=512, grid=16, spp=256)
+    pr.pde = P.make_pde(pr.solution, sigma=2.0, source=True)
+    pr.settings = P.default_walk_settings(rr=0.9, splitting=1.5)
+    g, st, steps, rep = _gpu_and_oracle(zgpu, oracle, pr)
+    assert rep.error_word == 0
+    assert rep.rr_terminated > 0
+    z = _cross_z(g, st)
+    assert np.mean(np.abs(z) > 3) <= 0.02
+    assert abs(_exact_z(g).mean()) <= 0.5
+
+
+def test_public_api_with_sample_point_lists(zgpu):
+    """The reference's call shape: WalkOnStars(queries).solve(pde, settings, n_walks, pts, stats)."""
+    import zombie_gb300 as Z
+    pr = P.mixed_wost_2d(n_segments=1024, grid=8, spp=64)
+    q = Z.Core.GeometricQueries(True, pr.domain_min, pr.domain_max, dim=2)
+    ab = Z.Utils.FcpwDirichletBoundaryHandler(dim=2)
+    ab.build_acceleration_structure(*pr.absorbing)
+    Z.Utils.populate_geometric_queries_for_dirichlet_boundary(ab, q, dim=2)
+    rf = Z.Utils.FcpwNeumannBoundaryHandler(dim=2)
+    rf.build_acceleration_structure(*pr.reflecting, Z.Utils.get_ignore_candidate_silhouette_callback(False, 0.0))
+    Z.Utils.populate_geometric_queries_for_neumann_boundary(rf, Z.Utils.get_branch_traversal_weight_callback(), q, dim=2)
+    pde = Z.api.PDE.from_c(2, pr.pde)
+    ws = Z.Solvers.WalkSettings(1e-3, 1e-3, 1e-3, 0.0, A.FLT_MAX, 1024, 0, 1024, False, True, True, False, False,
+                                False, False, False)
+    d = q.compute_dist_to_absorbing_boundary(pr.points)
+    pts = [Z.Solvers.SamplePoint(p, np.zeros(2), Z.Solvers.SampleType.InDomain, Z.Solvers.EstimationQuantity.Solution,
+                                 1.0, float(di), float("inf"), seed=i + 1, dim=2) for i, (p, di) in enumerate(zip(pr.points, d))]
+    stats = Z.Solvers.create_sample_statistics_list(len(pts), dim=2)
+    solver = Z.Solvers.WalkOnStars(q, dim=2)
+    calls = []
+    solver.solve(pde, ws, [64] * len(pts), pts, stats, False, lambda n, t: calls.append(n))
+    assert calls == [len(pts)]
+    est = np.array([s.get_estimated_solution() for s in stats])
+    assert all(s.get_solution_estimate_count() == 64 for s in stats)
+    assert all(p.first_sphere_radius > 0 for p in pts)
+    assert np.sqrt(np.mean((est - pr.exact()) ** 2)) < 0.3
+    assert q.inside_domain(pr.points).all()
+
+
+def test_invalid_arguments_return_errors(zgpu):
+    import ctypes as C
+    from zombie_gb300 import _lib
+    from zombie_gb300.api import default_context
+    L = _lib.lib()
+    ctx = default_context()
+    h = C.c_void_p()
+    pos = np.zeros((4, 2), np.float32)
+    idx = np.array([[0, 5]], np.int32)   # vertex index out of range
+    st = L.zgpu_boundary_create(ctx.h, 2, A.ptr(pos), 4, A.ptr(idx), 1, 0, None, None, 0, 1e-3, 4, C.byref(h))
+    assert st == A.ZGPU_ERR_INVALID_ARG and b"out of range" in L.zgpu_last_error()
+    st = L.zgpu_boundary_create(ctx.h, 4, A.ptr(pos), 4, A.ptr(idx), 1, 0, None, None, 0, 1e-3, 4, C.byref(h))
+    assert st == A.ZGPU_ERR_INVALID_ARG
+    st = L.zgpu_solve(ctx.h, 7, None, None, None, None, None, None, None)
+    assert st == A.ZGPU_ERR_INVALID_ARG
+    # dense-grid fields are reported as unsupported, not silently ignored
+    from zombie_gb300.runner import GpuProblem
+    gp = GpuProblem(P.laplace_wos_2d(n_segments=64, grid=4, spp=4))
+    pde = gp.pde.to_c()
+    pde.source_kind = A.ZGPU_FIELD_GRID
+    with pytest.raises(_lib.ZgpuError) as e:
+        gp.solver.solve_arrays(pde, gp.problem.settings, gp.host_arrays())
+    assert e.value.status == A.ZGPU_ERR_UNSUPPORTED

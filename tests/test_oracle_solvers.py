@@ -1,0 +1,112 @@
+"""The oracle's walk estimators against FP64 manufactured solutions (small sizes)."""
+import numpy as np
+import pytest
+
+from zombie_gb300 import _abi as A
+from zombie_gb300 import problems as P
+
+
+def run_oracle(oracle, pr, n_threads=None, seeds=None):
+    D = pr.dim
+    ab = oracle.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
+    rf = None
+    if pr.reflecting is not None and len(pr.reflecting[1]):
+        k = None
+        if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN:
+            k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32)
+        rf = oracle.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
+                             silhouette_precision=pr.ignore_silhouette_precision)
+    n = pr.points.shape[0]
+    if ab is not None:
+        d = ab.closest_point(pr.points)[2]
+    else:
+        m = np.minimum(pr.domain_min - pr.points, pr.points - pr.domain_max)
+        d = np.linalg.norm(m, axis=1).astype(np.float32)
+    pts = dict(pt=pr.points, dist_to_absorbing=d, n_walks=pr.n_walks,
+               seed=P.seeds_for(n) if seeds is None else seeds, first_sphere_radius=np.zeros(n, np.float32))
+    st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+              total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
+    steps = oracle.solve(pr.solver, D, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, pts, st, n_threads)
+    return st, steps
+
+
+def zscores(st, exact):
+    n = st["n_solution_estimates"].astype(np.float64)
+    se = np.sqrt(st["solution_m2"] / np.maximum(n - 1, 1) / np.maximum(n, 1))
+    return (st["solution_mean"] - exact) / np.maximum(se, 1e-12)
+
+
+def test_wos_laplace_2d_matches_analytic(oracle):
+    pr = P.laplace_wos_2d(n_segments=1024, grid=20, spp=512)
+    st, steps = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert steps > 0
+    assert abs(z.mean()) < 4.0 / np.sqrt(len(z)) + 0.1   # epsilon-shell bias is O(1e-3)
+    assert np.mean(np.abs(z) > 3.5) < 0.02
+
+
+def test_wost_mixed_2d_matches_analytic(oracle):
+    pr = P.mixed_wost_2d(n_segments=2048, grid=16, spp=512)
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.35
+    assert np.mean(np.abs(z) > 3.5) < 0.03
+
+
+def test_wost_screened_2d_matches_analytic(oracle):
+    pr = P.mixed_wost_2d(n_segments=2048, grid=12, spp=256, sigma=1.0)
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.45
+    assert np.mean(np.abs(z) > 3.5) < 0.04
+
+
+def test_wost_robin_3d_matches_analytic(oracle):
+    pr = P.robin_wost_3d(level=3, n_points=120, spp=256, kappa=2.0)
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.45
+    assert np.mean(np.abs(z) > 3.5) < 0.04
+
+
+def test_wos_screened_3d_matches_analytic(oracle):
+    pr = P.screened_wos_3d(level=3, n_points=150, spp=256, sigma=4.0)
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.45
+    assert np.mean(np.abs(z) > 3.5) < 0.04
+
+
+def test_progressive_accumulation(oracle):
+    """Two calls of W walks merge (common.h:268-310) into the same moments as one call of 2W."""
+    pr = P.laplace_wos_2d(n_segments=256, grid=10, spp=64)
+    n = pr.points.shape[0]
+    ab = oracle.Boundary(2, *pr.absorbing)
+    d = ab.closest_point(pr.points)[2]
+    seeds = P.seeds_for(n)
+
+    def fresh():
+        return dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+                    total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
+    a = fresh()
+    for _ in range(2):
+        pts = dict(pt=pr.points, dist_to_absorbing=d, n_walks=pr.n_walks, seed=seeds, first_sphere_radius=np.zeros(n, np.float32))
+        oracle.solve(pr.solver, 2, ab, None, pr.domain_min, pr.domain_max, pr.pde, pr.settings, pts, a)
+    b = fresh()
+    pts = dict(pt=pr.points, dist_to_absorbing=d, n_walks=2 * pr.n_walks, seed=seeds, first_sphere_radius=np.zeros(n, np.float32))
+    oracle.solve(pr.solver, 2, ab, None, pr.domain_min, pr.domain_max, pr.pde, pr.settings, pts, b)
+    # walk w of the second call uses stream w + 64 == walk w + 64 of the single call
+    assert np.array_equal(a["n_solution_estimates"], b["n_solution_estimates"])
+    assert np.allclose(a["solution_mean"], b["solution_mean"], rtol=0, atol=1e-9)
+    assert np.allclose(a["solution_m2"], b["solution_m2"], rtol=1e-9, atol=1e-9)
+    assert np.array_equal(a["total_walk_length"], b["total_walk_length"])
+
+
+def test_russian_roulette_and_splitting_stay_unbiased(oracle):
+    pr = P.laplace_wos_2d(n_segments=512, grid=10, spp=512)
+    pr.pde = P.make_pde(pr.solution, sigma=2.0, source=True)   # screened: throughput decays
+    pr.settings = P.default_walk_settings(rr=0.9, splitting=1.5)
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.5
+    assert np.mean(np.abs(z) > 3.5) < 0.04

@@ -1,0 +1,559 @@
+// zgpu_api.cu -- implementation of the C ABI declared in include/zgpu.h.
+//
+// Host-memory arrays are staged through device scratch owned by the context (the
+// end-to-end path); device-memory arrays are used in place.  Every kernel of a context
+// runs on its stream; entry points return after the stream has drained.
+#include <cstdarg>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "zgpu_build.h"
+#include "zgpu_internal.h"
+
+using namespace zg;
+
+namespace {
+
+thread_local std::string gLastError;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    gLastError = buf;
+    return code;
+}
+
+#define ZG_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? ZGPU_ERR_OUT_OF_MEMORY : ZGPU_ERR_CUDA, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+    } while (0)
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+cudaError_t ensure(Buf& b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return cudaSuccess;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t grow = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&b.p, grow);
+    if (e == cudaSuccess) b.bytes = grow;
+    return e;
+}
+
+}  // namespace
+
+struct zgpu_context {
+    int device = 0;
+    int numSMs = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // scratch (indexed by role)
+    enum { kPt, kNormal, kType, kEq, kDist, kNWalks, kSeed, kFsr, kAligned, kMean, kM2, kN, kLen, kSplits,
+           kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
+           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kNumBufs };
+    Buf bufs[kNumBufs];
+    unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
+};
+
+struct zgpu_boundary {
+    zgpu_context* ctx = nullptr;
+    int dim = 2;
+    int kind = 0;
+    int nPrims = 0;
+    int nNodes = 0;
+    int depth = 0;
+    float signedVolume = 0.0f;
+    float4* nodes = nullptr;
+    float4* cones = nullptr;
+    float4* prims = nullptr;
+    float4* sil = nullptr;
+    int* primIndex = nullptr;
+    std::vector<int> primIndexHost;   // leaf slot -> caller index (for coefficient updates)
+    BoundaryView view;
+};
+
+namespace {
+
+// Stages `count` elements of `elem` bytes from caller memory to device; returns the device pointer.
+template <typename T>
+int stageIn(zgpu_context* ctx, int role, const T* src, size_t count, int memory, const T** out) {
+    if (!src) { *out = nullptr; return ZGPU_OK; }
+    if (memory == ZGPU_MEM_DEVICE) { *out = src; return ZGPU_OK; }
+    ZG_CUDA(ensure(ctx->bufs[role], count * sizeof(T)));
+    ZG_CUDA(cudaMemcpyAsync(ctx->bufs[role].p, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    *out = (const T*)ctx->bufs[role].p;
+    return ZGPU_OK;
+}
+template <typename T>
+int stageInOut(zgpu_context* ctx, int role, T* src, size_t count, int memory, T** out) {
+    const T* c = nullptr;
+    int st = stageIn<T>(ctx, role, src, count, memory, &c);
+    *out = const_cast<T*>(c);
+    return st;
+}
+template <typename T>
+int stageOut(zgpu_context* ctx, const T* dev, T* dst, size_t count, int memory) {
+    if (!dst || memory == ZGPU_MEM_DEVICE) return ZGPU_OK;
+    ZG_CUDA(cudaMemcpyAsync(dst, dev, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    return ZGPU_OK;
+}
+template <typename T>
+int scratch(zgpu_context* ctx, int role, size_t count, T** out) {
+    ZG_CUDA(ensure(ctx->bufs[role], count * sizeof(T)));
+    *out = (T*)ctx->bufs[role].p;
+    return ZGPU_OK;
+}
+
+#define ZG_TRY(x) do { int s_ = (x); if (s_ != ZGPU_OK) return s_; } while (0)
+
+int checkBoundary(zgpu_boundary* b, int dim, const char* what) {
+    if (!b) return ZGPU_OK;
+    if (b->dim != dim) return fail(ZGPU_ERR_INVALID_ARG, "%s boundary has dim %d, queries have dim %d", what, b->dim, dim);
+    return ZGPU_OK;
+}
+
+int checkField(int kind, const char* name) {
+    if (kind == ZGPU_FIELD_GRID) return fail(ZGPU_ERR_UNSUPPORTED, "%s: dense-grid fields are not supported by this build", name);
+    if (kind < ZGPU_FIELD_ZERO || kind > ZGPU_FIELD_GRID) return fail(ZGPU_ERR_INVALID_ARG, "%s: unknown field kind %d", name, kind);
+    return ZGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int zgpu_abi_version(void) { return ZGPU_ABI_VERSION; }
+
+const char* zgpu_last_error(void) { return gLastError.c_str(); }
+
+int zgpu_context_create(int device, zgpu_context** out) {
+    if (!out) return fail(ZGPU_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    ZG_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(ZGPU_ERR_INVALID_ARG, "device %d out of range (%d devices)", device, n);
+    ZG_CUDA(cudaSetDevice(device));
+    zgpu_context* c = new zgpu_context();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->hostCounters, sizeof(unsigned long long) * 16);
+    if (e != cudaSuccess) {
+        zgpu_context_destroy(c);
+        return fail(ZGPU_ERR_CUDA, "context creation failed: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return ZGPU_OK;
+}
+
+int zgpu_context_destroy(zgpu_context* c) {
+    if (!c) return ZGPU_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& b : c->bufs) if (b.p) cudaFree(b.p);
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->hostCounters) cudaFreeHost(c->hostCounters);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ZGPU_OK;
+}
+
+int zgpu_context_synchronize(zgpu_context* c) {
+    if (!c) return fail(ZGPU_ERR_INVALID_ARG, "context is NULL");
+    ZG_CUDA(cudaStreamSynchronize(c->stream));
+    return ZGPU_OK;
+}
+
+void* zgpu_context_stream(zgpu_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int n_vertices, const int* indices,
+                         int n_prims, int kind, const float* min_robin, const float* max_robin,
+                         int solve_double_sided, float silhouette_precision, int bvh_width, zgpu_boundary** out) {
+    if (!ctx || !out) return fail(ZGPU_ERR_INVALID_ARG, "context/out is NULL");
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
+    if (kind < ZGPU_BOUNDARY_ABSORBING || kind > ZGPU_BOUNDARY_ROBIN) return fail(ZGPU_ERR_INVALID_ARG, "unknown boundary kind %d", kind);
+    if (bvh_width != 0 && bvh_width != 4) return fail(ZGPU_ERR_UNSUPPORTED, "bvh_width %d not supported (4)", bvh_width);
+    if (n_prims > 0 && (!positions || !indices)) return fail(ZGPU_ERR_INVALID_ARG, "positions/indices are NULL");
+    if (kind == ZGPU_BOUNDARY_ROBIN && n_prims > 0 && (!min_robin || !max_robin))
+        return fail(ZGPU_ERR_INVALID_ARG, "Robin boundary needs min/max Robin coefficients per primitive");
+    HostBoundary hb;
+    std::string err;
+    if (!buildBoundary(dim, positions, n_vertices, indices, n_prims, kind, min_robin, max_robin,
+                       solve_double_sided != 0, silhouette_precision, hb, err))
+        return fail(ZGPU_ERR_INVALID_ARG, "boundary build: %s", err.c_str());
+    if (hb.depth > kMaxWideDepth)
+        return fail(ZGPU_ERR_UNSUPPORTED, "boundary BVH depth %d exceeds the traversal stack (max %d)", hb.depth, kMaxWideDepth);
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    zgpu_boundary* b = new zgpu_boundary();
+    b->ctx = ctx; b->dim = dim; b->kind = kind; b->nPrims = n_prims; b->nNodes = hb.nNodes; b->depth = hb.depth;
+    b->signedVolume = hb.signedVolume;
+    b->primIndexHost = hb.primIndex;
+    auto upload = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
+        if (bytes == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(dst, bytes);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = upload((void**)&b->nodes, hb.nodes.data(), hb.nodes.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->cones, hb.cones.data(), hb.cones.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->prims, hb.prims.data(), hb.prims.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->sil, hb.sil.data(), hb.sil.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->primIndex, hb.primIndex.data(), hb.primIndex.size() * sizeof(int));
+    if (e != cudaSuccess) {
+        zgpu_boundary_destroy(b);
+        return fail(e == cudaErrorMemoryAllocation ? ZGPU_ERR_OUT_OF_MEMORY : ZGPU_ERR_CUDA, "boundary upload: %s",
+                    cudaGetErrorString(e));
+    }
+    b->view.nodes = b->nodes; b->view.cones = b->cones; b->view.prims = b->prims; b->view.sil = b->sil; b->view.primIndex = b->primIndex;
+    b->view.nNodes = b->nNodes; b->view.nPrims = b->nPrims;
+    b->view.stackEntries = stackEntriesForDepth(b->depth);
+    *out = b;
+    return ZGPU_OK;
+}
+
+int zgpu_boundary_destroy(zgpu_boundary* b) {
+    if (!b) return ZGPU_OK;
+    if (b->ctx) cudaSetDevice(b->ctx->device);
+    cudaFree(b->nodes); cudaFree(b->cones); cudaFree(b->prims); cudaFree(b->sil); cudaFree(b->primIndex);
+    delete b;
+    return ZGPU_OK;
+}
+
+int zgpu_boundary_update_robin_coefficients(zgpu_boundary* b, const float* min_robin, const float* max_robin) {
+    if (!b || !min_robin || !max_robin) return fail(ZGPU_ERR_INVALID_ARG, "NULL argument");
+    if (b->kind != ZGPU_BOUNDARY_ROBIN) return fail(ZGPU_ERR_INVALID_ARG, "not a Robin boundary");
+    if (b->nPrims == 0) return ZGPU_OK;
+    int per = b->dim == 2 ? 2 : 3;
+    std::vector<float4> sil((size_t)b->nPrims * per);
+    ZG_CUDA(cudaMemcpy(sil.data(), b->sil, sil.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < b->nPrims; s++) {
+        int i = b->primIndexHost[s];
+        if (b->dim == 2) { sil[(size_t)s * 2 + 1].y = min_robin[i]; sil[(size_t)s * 2 + 1].z = max_robin[i]; }
+        else { sil[(size_t)s * 3 + 1].w = min_robin[i]; sil[(size_t)s * 3 + 2].w = max_robin[i]; }
+    }
+    ZG_CUDA(cudaMemcpy(b->sil, sil.data(), sil.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    return ZGPU_OK;
+}
+
+int zgpu_boundary_info(zgpu_boundary* b, int64_t* n_nodes, int32_t* depth, int64_t* node_bytes, int64_t* prim_bytes) {
+    if (!b) return fail(ZGPU_ERR_INVALID_ARG, "boundary is NULL");
+    if (n_nodes) *n_nodes = b->nNodes;
+    if (depth) *depth = b->depth;
+    if (node_bytes) *node_bytes = (int64_t)b->nNodes * 128;
+    if (prim_bytes) *prim_bytes = (int64_t)b->nPrims * (b->dim == 2 ? 16 : 48);
+    return ZGPU_OK;
+}
+
+int zgpu_boundary_signed_volume(zgpu_boundary* b, float* out) {
+    if (!b || !out) return fail(ZGPU_ERR_INVALID_ARG, "NULL argument");
+    *out = b->signedVolume;
+    return ZGPU_OK;
+}
+
+// ------------------------------------------------------------------ batched queries
+#define ZG_QUERY_PROLOGUE()                                                             \
+    if (!b) return fail(ZGPU_ERR_INVALID_ARG, "boundary is NULL");                       \
+    if (n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative query count");               \
+    if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE)                          \
+        return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space %d", memory);           \
+    zgpu_context* ctx = b->ctx;                                                         \
+    ZG_CUDA(cudaSetDevice(ctx->device));                                                \
+    const int D = b->dim;                                                               \
+    unsigned int* errw = nullptr;                                                       \
+    ZG_TRY(scratch<unsigned int>(ctx, zgpu_context::kCounters, 16, &errw));             \
+    ZG_CUDA(cudaMemsetAsync(errw, 0, sizeof(unsigned int), ctx->stream));
+
+static int queryEpilogue(zgpu_context* ctx, unsigned int* errw) {
+    ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters, errw, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+    ZG_CUDA(cudaStreamSynchronize(ctx->stream));
+    unsigned int e = *(unsigned int*)ctx->hostCounters;
+    if (e) return fail(ZGPU_ERR_DEVICE_STATE, "device error word 0x%x (traversal stack overflow)", e);
+    return ZGPU_OK;
+}
+
+int zgpu_query_closest_point(zgpu_boundary* b, int64_t n, const float* x, int compute_signed, float* out_pt,
+                             float* out_normal, float* out_dist, int32_t* out_prim, int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!x) return fail(ZGPU_ERR_INVALID_ARG, "x is NULL");
+    const float* dx; float *dpt, *dn, *dd; int* dp;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, x, (size_t)n * D, memory, &dx));
+    if (memory == ZGPU_MEM_DEVICE) { dpt = out_pt; dn = out_normal; dd = out_dist; dp = out_prim; }
+    else {
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ1, (size_t)n * D, &dpt));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ2, (size_t)n * D, &dn));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ3, (size_t)n, &dd));
+        ZG_TRY(scratch<int>(ctx, zgpu_context::kQ4, (size_t)n, &dp));
+    }
+    ZG_CUDA(launchClosest(b->view, D, n, dx, compute_signed, dpt, dn, dd, dp, errw, ctx->stream));
+    ZG_TRY(stageOut<float>(ctx, dpt, out_pt, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dn, out_normal, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dd, out_dist, (size_t)n, memory));
+    ZG_TRY(stageOut<int>(ctx, dp, out_prim, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+int zgpu_query_intersect(zgpu_boundary* b, int64_t n, const float* origin, const float* normal, const float* dir,
+                         const float* t_max, const int32_t* on_boundary, int32_t* out_hit, float* out_pt,
+                         float* out_normal, float* out_dist, int32_t* out_prim, int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!origin || !dir || !t_max || !out_hit) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (on_boundary && !normal) return fail(ZGPU_ERR_INVALID_ARG, "on_boundary needs normals");
+    const float *dO, *dN, *dD, *dT; const int* dOnb;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, origin, (size_t)n * D, memory, &dO));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, normal, (size_t)n * D, memory, &dN));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, dir, (size_t)n * D, memory, &dD));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ3, t_max, (size_t)n, memory, &dT));
+    ZG_TRY(stageIn<int>(ctx, zgpu_context::kQ4, on_boundary, (size_t)n, memory, &dOnb));
+    int *dHit, *dPrim; float *dPt, *dNr, *dDist;
+    if (memory == ZGPU_MEM_DEVICE) { dHit = out_hit; dPt = out_pt; dNr = out_normal; dDist = out_dist; dPrim = out_prim; }
+    else {
+        ZG_TRY(scratch<int>(ctx, zgpu_context::kQ5, (size_t)n, &dHit));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ6, (size_t)n * D, &dPt));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ7, (size_t)n * D, &dNr));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ8, (size_t)n, &dDist));
+        ZG_TRY(scratch<int>(ctx, zgpu_context::kQ9, (size_t)n, &dPrim));
+    }
+    ZG_CUDA(launchIntersect(b->view, D, n, dO, dN, dD, dT, dOnb, dHit, dPt, dNr, dDist, dPrim, errw, ctx->stream));
+    ZG_TRY(stageOut<int>(ctx, dHit, out_hit, (size_t)n, memory));
+    ZG_TRY(stageOut<float>(ctx, dPt, out_pt, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dNr, out_normal, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dDist, out_dist, (size_t)n, memory));
+    ZG_TRY(stageOut<int>(ctx, dPrim, out_prim, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+int zgpu_query_count_hits(zgpu_boundary* b, int64_t n, const float* origin, const float* dir, const float* t_max,
+                          int32_t* out_count, int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!origin || !dir || !t_max || !out_count) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    const float *dO, *dD, *dT; int* dOut;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, origin, (size_t)n * D, memory, &dO));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, dir, (size_t)n * D, memory, &dD));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, t_max, (size_t)n, memory, &dT));
+    if (memory == ZGPU_MEM_DEVICE) dOut = out_count; else ZG_TRY(scratch<int>(ctx, zgpu_context::kQ3, (size_t)n, &dOut));
+    ZG_CUDA(launchCountHits(b->view, D, n, dO, dD, dT, dOut, errw, ctx->stream));
+    ZG_TRY(stageOut<int>(ctx, dOut, out_count, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+int zgpu_query_star_radius(zgpu_boundary* b, int64_t n, const float* x, const float* min_radius,
+                           const float* max_radius, float silhouette_precision, const int32_t* flip,
+                           float* out_radius, int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!x || !min_radius || !max_radius || !out_radius) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (b->kind == ZGPU_BOUNDARY_ABSORBING) return fail(ZGPU_ERR_INVALID_ARG, "star radius needs a reflecting boundary");
+    const float *dx, *dmin, *dmax; const int* dflip; float* dout;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, x, (size_t)n * D, memory, &dx));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, min_radius, (size_t)n, memory, &dmin));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, max_radius, (size_t)n, memory, &dmax));
+    ZG_TRY(stageIn<int>(ctx, zgpu_context::kQ3, flip, (size_t)n, memory, &dflip));
+    if (memory == ZGPU_MEM_DEVICE) dout = out_radius; else ZG_TRY(scratch<float>(ctx, zgpu_context::kQ4, (size_t)n, &dout));
+    ZG_CUDA(launchStarRadius(b->view, D, n, dx, dmin, dmax, silhouette_precision, dflip, dout, errw, ctx->stream));
+    ZG_TRY(stageOut<float>(ctx, dout, out_radius, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+int zgpu_query_occluded(zgpu_boundary* b, int64_t n, const float* xi, const float* xj, const float* ni,
+                        const float* nj, const int32_t* offset_i, const int32_t* offset_j, int32_t* out_occluded,
+                        int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!xi || !xj || !out_occluded) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if ((offset_i && !ni) || (offset_j && !nj)) return fail(ZGPU_ERR_INVALID_ARG, "offsets need normals");
+    const float *dxi, *dxj, *dni, *dnj; const int *doi, *doj; int* dout;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, xi, (size_t)n * D, memory, &dxi));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, xj, (size_t)n * D, memory, &dxj));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, ni, (size_t)n * D, memory, &dni));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ3, nj, (size_t)n * D, memory, &dnj));
+    ZG_TRY(stageIn<int>(ctx, zgpu_context::kQ4, offset_i, (size_t)n, memory, &doi));
+    ZG_TRY(stageIn<int>(ctx, zgpu_context::kQ5, offset_j, (size_t)n, memory, &doj));
+    if (memory == ZGPU_MEM_DEVICE) dout = out_occluded; else ZG_TRY(scratch<int>(ctx, zgpu_context::kQ6, (size_t)n, &dout));
+    ZG_CUDA(launchOccluded(b->view, D, n, dxi, dxj, dni, dnj, doi, doj, dout, errw, ctx->stream));
+    ZG_TRY(stageOut<int>(ctx, dout, out_occluded, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, const float* radius,
+                               const float* rand_nums, int32_t* out_found, float* out_pt, float* out_normal,
+                               float* out_pdf, int memory) {
+    ZG_QUERY_PROLOGUE();
+    if (n == 0) return ZGPU_OK;
+    if (!x || !radius || !rand_nums || !out_found || !out_pt || !out_normal || !out_pdf)
+        return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    const float *dx, *dr, *du; int* dfound; float *dpt, *dn, *dpdf;
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, x, (size_t)n * D, memory, &dx));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, radius, (size_t)n, memory, &dr));
+    ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, rand_nums, (size_t)n * D, memory, &du));
+    if (memory == ZGPU_MEM_DEVICE) { dfound = out_found; dpt = out_pt; dn = out_normal; dpdf = out_pdf; }
+    else {
+        ZG_TRY(scratch<int>(ctx, zgpu_context::kQ3, (size_t)n, &dfound));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ4, (size_t)n * D, &dpt));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ5, (size_t)n * D, &dn));
+        ZG_TRY(scratch<float>(ctx, zgpu_context::kQ6, (size_t)n, &dpdf));
+    }
+    ZG_CUDA(launchSample(b->view, D, n, dx, dr, du, dfound, dpt, dn, dpdf, ctx->stream));
+    ZG_TRY(stageOut<int>(ctx, dfound, out_found, (size_t)n, memory));
+    ZG_TRY(stageOut<float>(ctx, dpt, out_pt, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dn, out_normal, (size_t)n * D, memory));
+    ZG_TRY(stageOut<float>(ctx, dpdf, out_pdf, (size_t)n, memory));
+    return queryEpilogue(ctx, errw);
+}
+
+// -------------------------------------------------------------------------- solve
+int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+               const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
+               const zgpu_solve_options* opt, zgpu_solve_report* report) {
+    if (!ctx || !q || !pde || !ws || !pts || !stats) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (solver != ZGPU_SOLVER_WALK_ON_SPHERES && solver != ZGPU_SOLVER_WALK_ON_STARS)
+        return fail(ZGPU_ERR_INVALID_ARG, "unknown solver %d", solver);
+    const int D = q->dim;
+    if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3, got %d", D);
+    ZG_TRY(checkBoundary(q->absorbing, D, "absorbing"));
+    ZG_TRY(checkBoundary(q->reflecting, D, "reflecting"));
+    if (q->reflecting && q->reflecting->kind == ZGPU_BOUNDARY_ABSORBING)
+        return fail(ZGPU_ERR_INVALID_ARG, "reflecting slot holds an absorbing boundary");
+    if (q->absorbing && q->absorbing->kind != ZGPU_BOUNDARY_ABSORBING)
+        return fail(ZGPU_ERR_INVALID_ARG, "absorbing slot holds a reflecting boundary");
+    if (pts->n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative point count");
+    if (pts->memory != stats->memory) return fail(ZGPU_ERR_INVALID_ARG, "points and statistics must share a memory space");
+    if (pts->memory != ZGPU_MEM_HOST && pts->memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    if (pts->n > 0 && (!pts->pt || !pts->dist_to_absorbing || !pts->n_walks || !pts->seed))
+        return fail(ZGPU_ERR_INVALID_ARG, "pt, dist_to_absorbing, n_walks and seed are required");
+    if (!stats->solution_mean || !stats->solution_m2 || !stats->n_solution_estimates || !stats->total_walk_length ||
+        !stats->total_splits)
+        return fail(ZGPU_ERR_INVALID_ARG, "statistics arrays are required");
+    if (ws->max_walk_length <= 0) return fail(ZGPU_ERR_INVALID_ARG, "max_walk_length must be positive");
+    if (!(ws->epsilon_shell_for_absorbing_boundary >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "epsilon shell must be >= 0");
+    if (!(ws->splitting_threshold > 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "splitting threshold must be > 0");
+    if (!(pde->absorption_coeff >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "absorption coefficient must be >= 0");
+    ZG_TRY(checkField(pde->source_kind, "source"));
+    ZG_TRY(checkField(pde->dirichlet_kind, "dirichlet"));
+    ZG_TRY(checkField(pde->robin_kind, "robin"));
+    ZG_TRY(checkField(pde->robin_coeff_kind, "robin_coeff"));
+    if (pde->robin_coeff_kind == ZGPU_FIELD_ANALYTIC) return fail(ZGPU_ERR_UNSUPPORTED, "robin_coeff must be ZERO or CONSTANT");
+    if (pde->solution.n_terms < 0 || pde->solution.n_terms > ZGPU_MAX_TERMS)
+        return fail(ZGPU_ERR_INVALID_ARG, "analytic solution has %d terms (max %d)", pde->solution.n_terms, ZGPU_MAX_TERMS);
+
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    const int64_t n = pts->n;
+    const int mem = pts->memory;
+    cudaStream_t s = ctx->stream;
+    SolveParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.solver = solver;
+    P.hasAbs = q->absorbing && q->absorbing->nPrims > 0;
+    P.hasRefl = q->reflecting && q->reflecting->nPrims > 0;
+    if (P.hasAbs) P.absorbing = q->absorbing->view;
+    if (P.hasRefl) P.reflecting = q->reflecting->view;
+    for (int i = 0; i < 3; i++) { P.domainMin[i] = q->domain_min[i]; P.domainMax[i] = q->domain_max[i]; }
+    P.ws = *ws;
+    P.pde = *pde;
+    P.nPoints = n;
+    using C = zgpu_context;
+    ZG_TRY(stageIn<float>(ctx, C::kPt, pts->pt, (size_t)n * D, mem, &P.pt));
+    ZG_TRY(stageIn<float>(ctx, C::kNormal, pts->normal, (size_t)n * D, mem, &P.normal));
+    ZG_TRY(stageIn<int>(ctx, C::kType, pts->type, (size_t)n, mem, &P.type));
+    ZG_TRY(stageIn<int>(ctx, C::kEq, pts->estimation_quantity, (size_t)n, mem, &P.eq));
+    ZG_TRY(stageIn<float>(ctx, C::kDist, pts->dist_to_absorbing, (size_t)n, mem, &P.distAbs));
+    ZG_TRY(stageIn<int>(ctx, C::kNWalks, pts->n_walks, (size_t)n, mem, &P.nWalks));
+    ZG_TRY(stageIn<uint64_t>(ctx, C::kSeed, pts->seed, (size_t)n, mem, &P.seed));
+    ZG_TRY(stageIn<int>(ctx, C::kAligned, pts->estimate_normal_aligned, (size_t)n, mem, &P.aligned));
+    if (pts->first_sphere_radius) {
+        ZG_TRY(stageInOut<float>(ctx, C::kFsr, pts->first_sphere_radius, (size_t)n, mem, &P.fsr));
+        P.fsrPersistent = 1;
+    } else {
+        ZG_TRY(scratch<float>(ctx, C::kFsr, (size_t)n, &P.fsr));
+        P.fsrPersistent = 0;
+    }
+    ZG_TRY(stageInOut<double>(ctx, C::kMean, stats->solution_mean, (size_t)n, mem, &P.statMean));
+    ZG_TRY(stageInOut<double>(ctx, C::kM2, stats->solution_m2, (size_t)n, mem, &P.statM2));
+    ZG_TRY(stageInOut<int>(ctx, C::kN, stats->n_solution_estimates, (size_t)n, mem, &P.statN));
+    ZG_TRY(stageInOut<long long>(ctx, C::kLen, (long long*)stats->total_walk_length, (size_t)n, mem, &P.statLen));
+    ZG_TRY(stageInOut<long long>(ctx, C::kSplits, (long long*)stats->total_splits, (size_t)n, mem, &P.statSplits));
+    long long* blockSums = nullptr;
+    ZG_TRY(scratch<long long>(ctx, C::kWalkStart, (size_t)n + 1, &P.walkStart));
+    ZG_TRY(scratch<int>(ctx, C::kFlags, (size_t)n, &P.pointFlags));
+    ZG_TRY(scratch<int>(ctx, C::kNPrev, (size_t)n, &P.nPrev));
+    ZG_TRY(scratch<double>(ctx, C::kAccSum, (size_t)n, &P.accSum));
+    ZG_TRY(scratch<double>(ctx, C::kAccSq, (size_t)n, &P.accSq));
+    ZG_TRY(scratch<int>(ctx, C::kAccN, (size_t)n, &P.accN));
+    ZG_TRY(scratch<long long>(ctx, C::kAccLen, (size_t)n, &P.accLen));
+    ZG_TRY(scratch<long long>(ctx, C::kAccSplits, (size_t)n, &P.accSplits));
+    ZG_TRY(scratch<long long>(ctx, C::kBlockSums, scanScratchElems(n), &blockSums));
+    ZG_TRY(scratch<unsigned long long>(ctx, C::kCounters, 16, &P.counters));
+    P.errorWord = (unsigned int*)(P.counters + 8);
+    ZG_CUDA(cudaMemsetAsync(P.counters, 0, 16 * sizeof(unsigned long long), s));
+
+    int threads = opt && opt->block_size > 0 ? opt->block_size : 128;
+    if (threads % 32 != 0 || threads > 128) return fail(ZGPU_ERR_INVALID_ARG, "block_size must be a multiple of 32 and <= 128");
+    P.stackEntries = 8;
+    if (P.hasAbs) P.stackEntries = std::max(P.stackEntries, P.absorbing.stackEntries);
+    if (P.hasRefl) P.stackEntries = std::max(P.stackEntries, P.reflecting.stackEntries);
+    int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
+                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f, threads, P.stackEntries);
+    int blocks = ctx->numSMs * perSM;
+    ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
+
+    ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
+    ZG_CUDA(launchPrepare(P, D, s));
+    ZG_CUDA(launchScan(P.walkStart, n, blockSums, s));
+    ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
+    if (n > 0) ZG_CUDA(launchWalk(P, D, blocks, threads, s));
+    ZG_CUDA(cudaEventRecord(ctx->ev[2], s));
+    ZG_CUDA(launchFinalize(P, D, s));
+    ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
+    ZG_TRY(stageOut<double>(ctx, P.statMean, stats->solution_mean, (size_t)n, mem));
+    ZG_TRY(stageOut<double>(ctx, P.statM2, stats->solution_m2, (size_t)n, mem));
+    ZG_TRY(stageOut<int>(ctx, P.statN, stats->n_solution_estimates, (size_t)n, mem));
+    ZG_TRY(stageOut<long long>(ctx, P.statLen, (long long*)stats->total_walk_length, (size_t)n, mem));
+    ZG_TRY(stageOut<long long>(ctx, P.statSplits, (long long*)stats->total_splits, (size_t)n, mem));
+    if (P.fsrPersistent) ZG_TRY(stageOut<float>(ctx, P.fsr, pts->first_sphere_radius, (size_t)n, mem));
+    ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters, P.counters, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters + 12, P.walkStart + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+    unsigned int errWord = (unsigned int)(ctx->hostCounters[8] & 0xffffffffu);
+    if (report) {
+        std::memset(report, 0, sizeof(*report));
+        report->total_steps = ctx->hostCounters[kCtrSteps];
+        report->escaped_walks = ctx->hostCounters[kCtrEscaped];
+        report->exceeded_walks = ctx->hostCounters[kCtrExceeded];
+        report->rr_terminated = ctx->hostCounters[kCtrRR];
+        report->total_walks = ctx->hostCounters[12];
+        report->error_word = errWord;
+        cudaEventElapsedTime(&report->kernel_ms, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&report->total_ms, ctx->ev[0], ctx->ev[3]);
+    }
+    if (errWord)
+        return fail(ZGPU_ERR_DEVICE_STATE, "device error word 0x%x (1: traversal stack, 2: split stack overflow)", errWord);
+    return ZGPU_OK;
+}
+
+int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_geometric_queries* queries,
+                       const zgpu_pde* pdes, const zgpu_walk_settings* settings, const zgpu_sample_points* points,
+                       zgpu_sample_statistics* stats, const zgpu_solve_options* options, zgpu_solve_report* report) {
+    if (n_scenes == 1 && (!points || !points->scene_id))
+        return zgpu_solve(ctx, solver, queries, pdes, settings, points, stats, options, report);
+    return fail(ZGPU_ERR_UNSUPPORTED, "batched many-solve is not available in this build");
+}
+
+}  // extern "C"

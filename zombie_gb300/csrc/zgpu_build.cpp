@@ -1,0 +1,429 @@
+// zgpu_build.cpp -- boundary preprocessing on the host: feature adjacency and silhouette
+// flags (utils/fcpw_geometric_queries.h:745-799 for 2D vertex tables, :892-973 for 3D
+// edge maps, ignore rule :1029-1038), a binned-SAH binary BVH with leaves of <= 4
+// primitives, and its collapse into the 4-wide, 128-byte node layout of zgpu_scene.cuh.
+#include "zgpu_build.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <array>
+#include <map>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+
+namespace zg {
+namespace {
+
+constexpr float kInf = 3.402823466e+38f;
+constexpr int kEmpty = 0x7fffffff;
+constexpr int kLeafMax = 4;
+
+struct Box {
+    float lo[3] = {kInf, kInf, kInf};
+    float hi[3] = {-kInf, -kInf, -kInf};
+    void grow(const float* p, int D) { for (int i = 0; i < D; i++) { lo[i] = std::min(lo[i], p[i]); hi[i] = std::max(hi[i], p[i]); } }
+    void grow(const Box& b, int D) { grow(b.lo, D); grow(b.hi, D); }
+    float half_area(int D) const {
+        float e[3];
+        for (int i = 0; i < D; i++) e[i] = std::max(0.0f, hi[i] - lo[i]);
+        return D == 2 ? e[0] + e[1] : e[0] * e[1] + e[1] * e[2] + e[2] * e[0];
+    }
+};
+
+struct BNode {
+    Box box;
+    int left = -1, right = -1, first = 0, count = 0;
+    float area = 0.0f;
+};
+
+struct Builder {
+    int D;
+    std::vector<Box> pbox;
+    std::vector<float> cent;   // [n*D]
+    std::vector<float> parea;
+    std::vector<int> order;
+    std::vector<BNode> nodes;
+
+    int build(int start, int end, int depth) {
+        int id = (int)nodes.size();
+        nodes.emplace_back();
+        Box box, cbox;
+        float area = 0.0f;
+        for (int i = start; i < end; i++) {
+            box.grow(pbox[order[i]], D);
+            cbox.grow(&cent[(size_t)order[i] * D], D);
+            area += parea[order[i]];
+        }
+        nodes[id].box = box;
+        nodes[id].area = area;
+        int n = end - start;
+        if (n <= kLeafMax || depth > 40) {
+            nodes[id].first = start;
+            nodes[id].count = n;
+            return id;
+        }
+        constexpr int B = 16;
+        float best = kInf; int bestAxis = -1, bestSplit = -1;
+        for (int ax = 0; ax < D; ax++) {
+            float lo = cbox.lo[ax], hi = cbox.hi[ax];
+            if (!(hi - lo > 1e-12f)) continue;
+            float scale = B / (hi - lo);
+            Box bb[B]; int cnt[B] = {0};
+            for (int i = start; i < end; i++) {
+                int p = order[i];
+                int b = std::min(B - 1, (int)((cent[(size_t)p * D + ax] - lo) * scale));
+                cnt[b]++; bb[b].grow(pbox[p], D);
+            }
+            float lArea[B]; int lCnt[B]; Box acc; int c = 0;
+            for (int b = 0; b < B; b++) { acc.grow(bb[b], D); c += cnt[b]; lArea[b] = acc.half_area(D); lCnt[b] = c; }
+            acc = Box(); c = 0;
+            for (int b = B - 1; b > 0; b--) {
+                acc.grow(bb[b], D); c += cnt[b];
+                if (lCnt[b - 1] == 0 || c == 0) continue;
+                float cost = lArea[b - 1] * lCnt[b - 1] + acc.half_area(D) * c;
+                if (cost < best) { best = cost; bestAxis = ax; bestSplit = b; }
+            }
+        }
+        int mid = start + n / 2;
+        if (bestAxis >= 0) {
+            float lo = cbox.lo[bestAxis], hi = cbox.hi[bestAxis];
+            float scale = B / (hi - lo);
+            auto it = std::partition(order.begin() + start, order.begin() + end, [&](int p) {
+                return std::min(B - 1, (int)((cent[(size_t)p * D + bestAxis] - lo) * scale)) < bestSplit;
+            });
+            mid = (int)(it - order.begin());
+        }
+        if (mid == start || mid == end) {
+            // degenerate split: median along the longest centroid axis
+            int ax = 0;
+            for (int i = 1; i < D; i++) if (cbox.hi[i] - cbox.lo[i] > cbox.hi[ax] - cbox.lo[ax]) ax = i;
+            mid = start + n / 2;
+            std::nth_element(order.begin() + start, order.begin() + mid, order.begin() + end,
+                             [&](int a, int b) { return cent[(size_t)a * D + ax] < cent[(size_t)b * D + ax]; });
+        }
+        int l = build(start, mid, depth + 1);
+        int r = build(mid, end, depth + 1);
+        nodes[id].left = l;
+        nodes[id].right = r;
+        return id;
+    }
+};
+
+int makeLeafRef(int first, int count) { return -(1 + ((first << 3) | (count - 1))); }
+
+struct Collapser {
+    int D;
+    const std::vector<BNode>& bn;
+    std::vector<float4>& out;
+    int maxDepth = 0;
+    std::vector<std::array<int, 4>> kidsOf;   // wide node -> binary node of each child (-1 empty)
+
+    int emit(int b, int depth) {
+        maxDepth = std::max(maxDepth, depth);
+        int id = (int)(out.size() / 8);
+        out.resize(out.size() + 8);
+        kidsOf.push_back({-1, -1, -1, -1});
+        // gather up to 4 children by opening the largest internal child
+        std::vector<int> kids = {bn[b].left, bn[b].right};
+        while ((int)kids.size() < 4) {
+            int pick = -1; float pa = -1.0f;
+            for (int i = 0; i < (int)kids.size(); i++) {
+                const BNode& k = bn[kids[i]];
+                if (k.count == 0) { float a = k.box.half_area(D); if (a > pa) { pa = a; pick = i; } }
+            }
+            if (pick < 0) break;
+            int k = kids[pick];
+            kids.erase(kids.begin() + pick);
+            kids.push_back(bn[k].left);
+            kids.push_back(bn[k].right);
+        }
+        float lo[3][4], hi[3][4], area[4];
+        int child[4];
+        for (int c = 0; c < 4; c++) {
+            for (int i = 0; i < 3; i++) { lo[i][c] = kInf; hi[i][c] = -kInf; }
+            area[c] = 0.0f; child[c] = kEmpty;
+        }
+        for (int c = 0; c < (int)kids.size(); c++) kidsOf[id][c] = kids[c];
+        for (int c = 0; c < (int)kids.size(); c++) {
+            const BNode& k = bn[kids[c]];
+            for (int i = 0; i < D; i++) { lo[i][c] = k.box.lo[i]; hi[i][c] = k.box.hi[i]; }
+            area[c] = k.area;
+            if (k.count > 0) child[c] = makeLeafRef(k.first, k.count);
+        }
+        for (int c = 0; c < (int)kids.size(); c++) {
+            if (bn[kids[c]].count == 0) child[c] = emit(kids[c], depth + 1);
+        }
+        float4* p = &out[(size_t)id * 8];
+        for (int i = 0; i < D; i++) {
+            p[i] = make_float4(lo[i][0], lo[i][1], lo[i][2], lo[i][3]);
+            p[D + i] = make_float4(hi[i][0], hi[i][1], hi[i][2], hi[i][3]);
+        }
+        int4 ci = make_int4(child[0], child[1], child[2], child[3]);
+        std::memcpy(&p[2 * D], &ci, sizeof(int4));
+        p[2 * D + 1] = make_float4(area[0], area[1], area[2], area[3]);
+        return id;
+    }
+};
+
+inline void normal2(const float* a, const float* b, float* n) {
+    float sx = b[0] - a[0], sy = b[1] - a[1];
+    float l = std::sqrt(sx * sx + sy * sy);
+    n[0] = sy / l; n[1] = -sx / l;
+}
+inline void normal3(const float* a, const float* b, const float* c, float* n) {
+    float u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, v[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    float x = u[1] * v[2] - u[2] * v[1], y = u[2] * v[0] - u[0] * v[2], z = u[0] * v[1] - u[1] * v[0];
+    float l = std::sqrt(x * x + y * y + z * z);
+    n[0] = x / l; n[1] = y / l; n[2] = z / l;
+}
+
+// Normal cone over the silhouette candidates of a binary subtree: every normal of a face
+// adjacent to a non-ignored feature lies within halfAngle of axis.  halfAngle < 0: no
+// candidate in the subtree; halfAngle = pi: a feature with a single face (always a
+// silhouette) or a degenerate axis.
+struct Cone { float axis[3] = {0, 0, 0}; float halfAngle = -1.0f; float kmax = 0.0f; };
+
+void coneOf(int D, const std::vector<BNode>& bn, int node, const std::vector<int>& order, const std::vector<float>& nrm,
+            const std::vector<int>& adj, const std::vector<int>& flags, const float* kmaxArr, Cone& out) {
+    std::vector<int> stack = {node};
+    std::vector<const float*> normals;
+    bool open = false;
+    float kmax = 0.0f;
+    while (!stack.empty()) {
+        int b = stack.back(); stack.pop_back();
+        if (bn[b].count == 0) { stack.push_back(bn[b].left); stack.push_back(bn[b].right); continue; }
+        for (int k = 0; k < bn[b].count; k++) {
+            int i = order[bn[b].first + k];
+            if (kmaxArr) kmax = std::max(kmax, kmaxArr[i]);
+            bool any = false;
+            for (int j = 0; j < D; j++) {
+                if (flags[i] & (8 << j)) continue;          // ignored feature
+                if (!(flags[i] & (1 << j))) { open = true; continue; }
+                normals.push_back(&nrm[(size_t)adj[(size_t)i * D + j] * D]);
+                any = true;
+            }
+            if (any) normals.push_back(&nrm[(size_t)i * D]);
+        }
+    }
+    out = Cone();
+    out.kmax = kmax;
+    if (open) { out.halfAngle = 3.14159265f; return; }
+    if (normals.empty()) { out.halfAngle = -1.0f; return; }
+    double a[3] = {0, 0, 0};
+    for (const float* n : normals) for (int i = 0; i < D; i++) a[i] += n[i];
+    double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (l < 1e-6) { out.halfAngle = 3.14159265f; return; }
+    for (int i = 0; i < 3; i++) out.axis[i] = (float)(a[i] / l);
+    double h = 0.0;
+    for (const float* n : normals) {
+        double c = 0.0;
+        for (int i = 0; i < D; i++) c += out.axis[i] * n[i];
+        h = std::max(h, std::acos(std::max(-1.0, std::min(1.0, c))));
+    }
+    out.halfAngle = (float)std::min(3.14159265, h + 1e-4);
+}
+
+}  // namespace
+
+bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
+                   const float* kmax, bool doubleSided, float silPrec, HostBoundary& hb, std::string& err) {
+    hb = HostBoundary();
+    hb.dim = D; hb.kind = kind; hb.nPrims = nP;
+    if (D != 2 && D != 3) { err = "dim must be 2 or 3"; return false; }
+    if (nP < 0 || nV < 0) { err = "negative sizes"; return false; }
+    for (int i = 0; i < nP * D; i++)
+        if (idx[i] < 0 || idx[i] >= nV) { err = "primitive index out of range"; return false; }
+    if (nP == 0) return true;
+    if (nP >= (1 << 27)) { err = "too many primitives"; return false; }
+
+    // ---- per-primitive normals, adjacency, silhouette flags and Robin ranges
+    std::vector<float> nrm((size_t)nP * D);
+    for (int i = 0; i < nP; i++) {
+        const float* a = pos + (size_t)idx[i * D] * D;
+        const float* b = pos + (size_t)idx[i * D + 1] * D;
+        if (D == 2) normal2(a, b, &nrm[(size_t)i * 2]);
+        else normal3(a, b, pos + (size_t)idx[i * D + 2] * D, &nrm[(size_t)i * 3]);
+    }
+    std::vector<int> adj((size_t)nP * D, -1);
+    if (D == 2) {
+        // vertex -> (segment ending at it, segment starting at it)
+        std::vector<int> endsAt(nV, -1), startsAt(nV, -1);
+        for (int i = 0; i < nP; i++) { startsAt[idx[i * 2]] = i; endsAt[idx[i * 2 + 1]] = i; }
+        for (int i = 0; i < nP; i++) { adj[i * 2] = endsAt[idx[i * 2]]; adj[i * 2 + 1] = startsAt[idx[i * 2 + 1]]; }
+    } else {
+        // directed edge (u,v) of face f is shared with the face holding (v,u)
+        std::unordered_map<uint64_t, int> dir;
+        dir.reserve((size_t)nP * 3 * 2);
+        for (int i = 0; i < nP; i++)
+            for (int j = 0; j < 3; j++) {
+                uint64_t u = (uint32_t)idx[i * 3 + j], v = (uint32_t)idx[i * 3 + (j + 1) % 3];
+                dir[(u << 32) | v] = i;
+            }
+        for (int i = 0; i < nP; i++)
+            for (int j = 0; j < 3; j++) {
+                uint64_t u = (uint32_t)idx[i * 3 + j], v = (uint32_t)idx[i * 3 + (j + 1) % 3];
+                auto it = dir.find((v << 32) | u);
+                adj[i * 3 + j] = it == dir.end() ? -1 : it->second;
+            }
+    }
+    std::vector<int> flags(nP, 0);
+    for (int i = 0; i < nP; i++) {
+        int f = 0;
+        for (int j = 0; j < D; j++) {
+            int a = adj[(size_t)i * D + j];
+            if (a < 0) continue;
+            f |= 1 << j;
+            bool ignore;
+            if (D == 2) {
+                const float* n0 = &nrm[(size_t)i * 2];
+                const float* nj = &nrm[(size_t)a * 2];
+                float det = (n0[0] * nj[1] - n0[1] * nj[0]) * (j == 0 ? 1.0f : -1.0f);
+                ignore = !doubleSided && det < silPrec;
+            } else {
+                const float* n0 = &nrm[(size_t)i * 3];
+                const float* nj = &nrm[(size_t)a * 3];
+                const float* pa = pos + (size_t)idx[i * 3 + j] * 3;
+                const float* pb = pos + (size_t)idx[i * 3 + (j + 1) % 3] * 3;
+                float e[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+                float el = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+                float c[3] = {nj[1] * n0[2] - nj[2] * n0[1], nj[2] * n0[0] - nj[0] * n0[2], nj[0] * n0[1] - nj[1] * n0[0]};
+                float angle = std::atan2((e[0] * c[0] + e[1] * c[1] + e[2] * c[2]) / el,
+                                         n0[0] * nj[0] + n0[1] * nj[1] + n0[2] * nj[2]);
+                ignore = !doubleSided && angle < silPrec;
+            }
+            if (ignore) f |= 8 << j;
+        }
+        flags[i] = f;
+    }
+
+    // ---- BVH over primitive boxes
+    Builder bld;
+    bld.D = D;
+    bld.pbox.resize(nP);
+    bld.cent.assign((size_t)nP * D, 0.0f);
+    bld.parea.resize(nP);
+    for (int i = 0; i < nP; i++) {
+        Box b;
+        for (int k = 0; k < D; k++) {
+            const float* p = pos + (size_t)idx[i * D + k] * D;
+            b.grow(p, D);
+            for (int a = 0; a < D; a++) bld.cent[(size_t)i * D + a] += p[a] / D;
+        }
+        bld.pbox[i] = b;
+        const float* a = pos + (size_t)idx[i * D] * D;
+        const float* bb = pos + (size_t)idx[i * D + 1] * D;
+        if (D == 2) {
+            bld.parea[i] = std::hypot(bb[0] - a[0], bb[1] - a[1]);
+        } else {
+            const float* c = pos + (size_t)idx[i * D + 2] * D;
+            float u[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]}, v[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            float x = u[1] * v[2] - u[2] * v[1], y = u[2] * v[0] - u[0] * v[2], z = u[0] * v[1] - u[1] * v[0];
+            bld.parea[i] = 0.5f * std::sqrt(x * x + y * y + z * z);
+        }
+    }
+    bld.order.resize(nP);
+    std::iota(bld.order.begin(), bld.order.end(), 0);
+    bld.nodes.reserve((size_t)2 * nP / kLeafMax + 16);
+    bld.build(0, nP, 0);
+
+    // ---- wide layout
+    if (bld.nodes[0].count > 0) {
+        // tiny scene: a root whose single child is the leaf
+        hb.nodes.resize(8);
+        float lo[3][4], hi[3][4];
+        for (int i = 0; i < 3; i++) for (int c = 0; c < 4; c++) { lo[i][c] = kInf; hi[i][c] = -kInf; }
+        for (int i = 0; i < D; i++) { lo[i][0] = bld.nodes[0].box.lo[i]; hi[i][0] = bld.nodes[0].box.hi[i]; }
+        for (int i = 0; i < D; i++) {
+            hb.nodes[i] = make_float4(lo[i][0], lo[i][1], lo[i][2], lo[i][3]);
+            hb.nodes[D + i] = make_float4(hi[i][0], hi[i][1], hi[i][2], hi[i][3]);
+        }
+        int4 ci = make_int4(makeLeafRef(0, bld.nodes[0].count), kEmpty, kEmpty, kEmpty);
+        std::memcpy(&hb.nodes[2 * D], &ci, sizeof(int4));
+        hb.nodes[2 * D + 1] = make_float4(bld.nodes[0].area, 0, 0, 0);
+        hb.depth = 1;
+    } else {
+        Collapser col{D, bld.nodes, hb.nodes};
+        col.emit(0, 1);
+        hb.depth = col.maxDepth;
+        if (kind != 0) {
+            hb.cones.assign(hb.nodes.size(), make_float4(0, 0, 0, -1));
+            for (size_t w = 0; w < col.kidsOf.size(); w++) {
+                float km[4] = {0, 0, 0, 0};
+                for (int c = 0; c < 4; c++) {
+                    int b = col.kidsOf[w][c];
+                    if (b < 0) continue;
+                    Cone cone;
+                    coneOf(D, bld.nodes, b, bld.order, nrm, adj, flags, kind == 2 ? kmax : nullptr, cone);
+                    hb.cones[w * 8 + c] = make_float4(cone.axis[0], cone.axis[1], cone.axis[2], cone.halfAngle);
+                    km[c] = cone.kmax;
+                }
+                hb.cones[w * 8 + 4] = make_float4(km[0], km[1], km[2], km[3]);
+            }
+        }
+    }
+    hb.nNodes = (int)(hb.nodes.size() / 8);
+    if (kind != 0 && hb.cones.empty()) {
+        // single-leaf scene: an always-visit cone
+        hb.cones.assign(8, make_float4(0, 0, 0, 3.14159265f));
+        float km = 0.0f;
+        if (kind == 2 && kmax) for (int i = 0; i < nP; i++) km = std::max(km, kmax[i]);
+        hb.cones[4] = make_float4(km, 0, 0, 0);
+    }
+
+    // ---- primitives and silhouette data in leaf order
+    hb.primIndex = bld.order;
+    hb.prims.resize((size_t)nP * (D == 2 ? 1 : 3));
+    bool reflecting = kind != 0;
+    if (reflecting) hb.sil.resize((size_t)nP * (D == 2 ? 2 : 3));
+    for (int s = 0; s < nP; s++) {
+        int i = bld.order[s];
+        if (D == 2) {
+            const float* a = pos + (size_t)idx[i * 2] * 2;
+            const float* b = pos + (size_t)idx[i * 2 + 1] * 2;
+            hb.prims[s] = make_float4(a[0], a[1], b[0], b[1]);
+        } else {
+            for (int k = 0; k < 3; k++) {
+                const float* p = pos + (size_t)idx[i * 3 + k] * 3;
+                hb.prims[(size_t)s * 3 + k] = make_float4(p[0], p[1], p[2], 0.0f);
+            }
+        }
+        if (!reflecting) continue;
+        float lo = kind == 2 && kmin ? kmin[i] : 0.0f;
+        float hi = kind == 2 && kmax ? kmax[i] : 0.0f;
+        float fl;
+        int f = flags[i];
+        std::memcpy(&fl, &f, 4);
+        float an[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int j = 0; j < D; j++) {
+            int a = adj[(size_t)i * D + j];
+            if (a >= 0) for (int k = 0; k < D; k++) an[j][k] = nrm[(size_t)a * D + k];
+        }
+        if (D == 2) {
+            hb.sil[(size_t)s * 2] = make_float4(an[0][0], an[0][1], an[1][0], an[1][1]);
+            hb.sil[(size_t)s * 2 + 1] = make_float4(fl, lo, hi, 0.0f);
+        } else {
+            hb.sil[(size_t)s * 3] = make_float4(an[0][0], an[0][1], an[0][2], fl);
+            hb.sil[(size_t)s * 3 + 1] = make_float4(an[1][0], an[1][1], an[1][2], lo);
+            hb.sil[(size_t)s * 3 + 2] = make_float4(an[2][0], an[2][1], an[2][2], hi);
+        }
+    }
+    // signed volume (computeSignedVolume, utils/fcpw_geometric_queries.h:431-458)
+    double vol = 0.0;
+    for (int i = 0; i < nP; i++) {
+        const float* a = pos + (size_t)idx[i * D] * D;
+        const float* b = pos + (size_t)idx[i * D + 1] * D;
+        if (D == 2) {
+            vol += 0.5 * ((double)a[0] * b[1] - (double)a[1] * b[0]);
+        } else {
+            const float* c = pos + (size_t)idx[i * D + 2] * D;
+            vol += (((double)a[1] * b[2] - (double)a[2] * b[1]) * c[0] + ((double)a[2] * b[0] - (double)a[0] * b[2]) * c[1] +
+                    ((double)a[0] * b[1] - (double)a[1] * b[0]) * c[2]) / 6.0;
+        }
+    }
+    hb.signedVolume = (float)vol;
+    return true;
+}
+
+}  // namespace zg

@@ -1,0 +1,86 @@
+// zgpu_internal.h -- declarations shared by the kernels (zgpu_walk.cu) and the C ABI
+// implementation (zgpu_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include "zgpu_scene.cuh"
+
+namespace zg {
+
+// walk completion codes (WalkCompletionCode, point_estimation/common.h:132-137)
+enum : int { kReached = 0, kRussianRoulette = 1, kExceeded = 2, kEscaped = 3 };
+
+// counters[] slots
+enum : int { kCtrNext = 0, kCtrSteps = 1, kCtrEscaped = 2, kCtrExceeded = 3, kCtrRR = 4, kCtrWalks = 5, kCtrCount = 8 };
+
+// per-point flags written by the prepare kernel
+enum : int { kPointBoundaryValue = 1, kPointFlip = 2 };
+
+struct SolveParams {
+    int solver;
+    int hasAbs, hasRefl;
+    BoundaryView absorbing, reflecting;
+    float domainMin[3], domainMax[3];
+    zgpu_walk_settings ws;
+    zgpu_pde pde;
+    int64_t nPoints;
+    // sample points (device)
+    const float* pt;
+    const float* normal;
+    const int* type;
+    const int* eq;
+    const float* distAbs;
+    const int* nWalks;
+    const uint64_t* seed;
+    const int* aligned;
+    float* fsr;
+    int fsrPersistent;          // 1: fsr is the caller's array (reuse when n_prev > 0)
+    // statistics (device, caller-owned)
+    double* statMean;
+    double* statM2;
+    int* statN;
+    long long* statLen;
+    long long* statSplits;
+    // scratch
+    long long* walkStart;       // nPoints + 1
+    int* pointFlags;            // nPoints
+    int* nPrev;                 // nPoints: statN before this call
+    double* accSum;
+    double* accSq;
+    int* accN;
+    long long* accLen;
+    long long* accSplits;
+    unsigned long long* counters;
+    unsigned int* errorWord;
+    float4* splitStack;         // walk threads x kSplitStack x 3 float4
+    int stackEntries;           // shared-memory traversal stack entries per thread
+};
+
+constexpr int kSplitStack = 8;
+
+// kernels / launchers (zgpu_walk.cu)
+cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);
+cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStream_t s);
+cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
+cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
+int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, int stackEntries);
+size_t scanScratchElems(int64_t n);
+
+// batched query kernels
+cudaError_t launchClosest(const BoundaryView& b, int dim, int64_t n, const float* x, int computeSigned,
+                          float* pt, float* nrm, float* dist, int* prim, unsigned int* err, cudaStream_t s);
+cudaError_t launchIntersect(const BoundaryView& b, int dim, int64_t n, const float* o, const float* nrmIn,
+                            const float* dir, const float* tmax, const int* onb, int* hit, float* pt, float* nrm,
+                            float* dist, int* prim, unsigned int* err, cudaStream_t s);
+cudaError_t launchCountHits(const BoundaryView& b, int dim, int64_t n, const float* o, const float* dir,
+                            const float* tmax, int* out, unsigned int* err, cudaStream_t s);
+cudaError_t launchStarRadius(const BoundaryView& b, int dim, int64_t n, const float* x, const float* minR,
+                             const float* maxR, float prec, const int* flip, float* out, unsigned int* err,
+                             cudaStream_t s);
+cudaError_t launchOccluded(const BoundaryView& b, int dim, int64_t n, const float* xi, const float* xj,
+                           const float* ni, const float* nj, const int* oi, const int* oj, int* out,
+                           unsigned int* err, cudaStream_t s);
+cudaError_t launchSample(const BoundaryView& b, int dim, int64_t n, const float* x, const float* r, const float* u,
+                         int* found, float* pt, float* nrm, float* pdf, cudaStream_t s);
+
+}  // namespace zg

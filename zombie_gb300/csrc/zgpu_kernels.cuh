@@ -1,0 +1,725 @@
+// zgpu_kernels.cuh -- the walk engine kernels (instantiated per dimension by
+// zgpu_kernels2.cu / zgpu_kernels3.cu; host dispatch in zgpu_dispatch.cu).
+//
+//  prepare  : per point, the bookkeeping of estimateSolution before its walk loop
+//             (walk_on_spheres.h:321-356, walk_on_stars.h:519-598): boundary points,
+//             epsilon-shell points, the first sphere / star radius, walk counts
+//  scan     : exclusive prefix sum of walk counts -> global walk ids
+//  walk     : persistent wavefront kernel.  Every lane owns one walk; a lane whose walk
+//             finishes refills itself from a global walk counter (one atomic per warp for
+//             all refilling lanes).  One iteration = one step of walk()
+//             (walk_on_spheres.h:229-291, walk_on_stars.h:346-490) fused with the
+//             geometric queries of that step.  Walk estimates are FP32; per-point sums
+//             are FP64 atomics.
+//  finalize : merge of this call's per-point moments into the caller's statistics
+//             (SampleStatistics::merge, common.h:268-310), in FP64.
+#pragma once
+#include "zgpu_internal.h"
+
+namespace zg {
+namespace detail {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+ZG_D bool outsideBox(const SolveParams& P, const float* x, int D) {
+    for (int i = 0; i < D; i++)
+        if (x[i] < P.domainMin[i] || x[i] > P.domainMax[i]) return true;
+    return false;
+}
+
+template <int D>
+ZG_D float bboxDistance(const SolveParams& P, V<D> x) {
+    // default computeDistToAbsorbingBoundary (core/geometric_queries.h:212-217)
+    V<D> m;
+#pragma unroll
+    for (int i = 0; i < D; i++) m[i] = fminf(P.domainMin[i] - x[i], x[i] - P.domainMax[i]);
+    return len(m);
+}
+
+// a pending split walk state, 3 float4 in global scratch (only touched when walks split)
+template <int D>
+ZG_D void storeSplit(float4* slot, V<D> pt, V<D> nrm, V<D> prevDir, float prevDist, float thr, bool onRefl) {
+    float v[12] = {0};
+#pragma unroll
+    for (int i = 0; i < D; i++) { v[i] = pt[i]; v[3 + i] = nrm[i]; v[6 + i] = prevDir[i]; }
+    v[9] = prevDist; v[10] = thr; v[11] = onRefl ? 1.0f : 0.0f;
+    slot[0] = make_float4(v[0], v[1], v[2], v[3]);
+    slot[1] = make_float4(v[4], v[5], v[6], v[7]);
+    slot[2] = make_float4(v[8], v[9], v[10], v[11]);
+}
+
+template <int D, int SOLVER, bool SCREENED>
+struct Walker {
+    const SolveParams& P;
+    DevicePde<D> pde;
+    // walk identity
+    int point;
+    Pcg32 rng;
+    // walk state (WalkState, common.h:93-130)
+    V<D> pt, nrm, prevDir;
+    float prevDist, thr;
+    int wlen;
+    bool onRefl, flip, pointFlip;
+    float totRefl, totSrc;
+    // per-walk accumulation across split states
+    float walkTotal;
+    bool success;
+    int splits;
+    long long lenSum;
+    // loop state
+    float distAbs, fsr;
+    bool firstStep, cpValid;
+    V<D> cpPt, cpN;
+    Greens<D, SCREENED> g;
+    float4* splitSlots;   // this thread's kSplitStack slots of 3 float4
+    int nStack;
+    // counters
+    unsigned long long steps, escaped, exceeded, rr;
+    uint32_t err;
+    TravStack S;
+
+    ZG_D Walker(const SolveParams& p, TravStack s) : P(p), S(s) {
+        pde.p = &P.pde;
+        steps = escaped = exceeded = rr = 0;
+        err = 0;
+        g.sqrtLambda = sqrtf(fmaxf(P.pde.absorption_coeff, 0.0f));
+    }
+
+    ZG_D int findPoint(long long id) const {
+        // largest i with walkStart[i] <= id
+        int64_t lo = 0, hi = P.nPoints;   // walkStart[nPoints] = total > id
+        while (hi - lo > 1) {
+            int64_t mid = (lo + hi) >> 1;
+            if (__ldg(P.walkStart + mid) <= id) lo = mid; else hi = mid;
+        }
+        return (int)lo;
+    }
+
+    ZG_D void closestQuery() {
+        if (P.hasAbs) {
+            ClosestHit<D> h = closestPoint<D>(P.absorbing, pt, S, err);
+            distAbs = h.d;
+            cpPt = h.pt;
+            if (h.slot >= 0) cpN = primNormal<D>(loadPrim<D>(P.absorbing, h.slot));
+            cpValid = true;
+        } else {
+            distAbs = bboxDistance<D>(P, pt);
+            cpValid = false;
+        }
+    }
+
+    ZG_D void resetGreens() {
+        // a new GreensFnBall for every dequeued state (walk_on_spheres.h:376-383, walk_on_stars.h:618-625)
+        g.yukawa = P.pde.absorption_coeff > 0.0f && P.ws.steps_before_applying_tikhonov == 0;
+    }
+
+    ZG_D void start(long long id) {
+        point = findPoint(id);
+        long long w = id - __ldg(P.walkStart + point);
+        rng.seed(__ldg(P.seed + point), (uint64_t)w + (uint64_t)__ldg(P.nPrev + point));
+        pt = vload<D>(P.pt + (size_t)point * D);
+        int type = P.type ? __ldg(P.type + point) : ZGPU_SAMPLE_IN_DOMAIN;
+        int flags = __ldg(P.pointFlags + point);
+        if (SOLVER == ZGPU_SOLVER_WALK_ON_STARS) {
+            V<D> n = P.normal ? vload<D>(P.normal + (size_t)point * D) : vzero<D>();
+            pointFlip = (flags & kPointFlip) != 0;
+            if (pointFlip) n = -n;
+            nrm = n; prevDir = n;
+            prevDist = kFltMax;
+            onRefl = type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY;
+        } else {
+            nrm = vzero<D>(); prevDir = vzero<D>(); prevDist = 0.0f; onRefl = false; pointFlip = false;
+        }
+        flip = pointFlip;
+        thr = 1.0f; wlen = 0; totRefl = 0.0f; totSrc = 0.0f;
+        walkTotal = 0.0f; success = false; splits = 0; lenSum = 0; nStack = 0;
+        distAbs = __ldg(P.distAbs + point);
+        fsr = P.fsr[point];
+        firstStep = true;
+        cpValid = false;
+        resetGreens();
+    }
+
+    __device__ __noinline__ void pushSplit() {
+        if (nStack < kSplitStack) storeSplit<D>(splitSlots + 3 * nStack++, pt, nrm, prevDir, prevDist, thr, onRefl);
+        else err |= kErrSplitOverflow;
+    }
+
+    __device__ __noinline__ void beginSplit() {
+        --nStack;
+        float4 a = splitSlots[3 * nStack], b = splitSlots[3 * nStack + 1], c = splitSlots[3 * nStack + 2];
+        float v[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int i = 0; i < D; i++) { pt[i] = v[i]; nrm[i] = v[3 + i]; prevDir[i] = v[6 + i]; }
+        prevDist = v[9]; thr = v[10]; onRefl = v[11] != 0.0f;
+        wlen = 0; totRefl = 0.0f; totSrc = 0.0f;
+        flip = pointFlip;
+        fsr = 0.0f;
+        firstStep = true;
+        resetGreens();
+        closestQuery();
+        splits++;
+    }
+
+    // weight window (walk_on_spheres.h:193-226, walk_on_stars.h:309-343); true -> terminated
+    ZG_D bool weightWindow() {
+        const float sT = P.ws.splitting_threshold, rT = P.ws.russian_roulette_threshold;
+        if (thr > sT) {
+            float left = thr - sT;
+            thr = sT;
+            for (int guard = 0; left > sT && guard < 1 << 20; guard++) {
+                left -= sT;
+                pushSplit();
+            }
+            if (rng.uniform() < left / sT) pushSplit();
+        } else if (thr < rT) {
+            float survival = thr / rT;
+            if (survival < rng.uniform()) { thr = 0.0f; return true; }
+            thr = rT;
+        }
+        return false;
+    }
+
+    // returns false when the lane's walk is complete
+    __device__ __noinline__ bool terminate(int code) {
+        if (code == kEscaped) {
+            escaped++;
+        } else {
+            if (code == kExceeded) exceeded++;
+            if (code == kRussianRoulette) rr++;
+            float term = 0.0f;
+            bool payTerminal = code == kReached || (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && code == kExceeded);
+            if (payTerminal && !P.ws.ignore_absorbing_boundary_contribution) {
+                // projectToAbsorbingBoundary then pde.dirichlet (walk_on_spheres.h:294-318, walk_on_stars.h:493-516)
+                if (P.hasAbs) {
+                    if (!cpValid) closestQuery();
+                    bool aligned = false;
+                    if (P.ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
+                    term = pde.dirichlet(cpPt, aligned);
+                } else {
+                    term = pde.dirichlet(pt, false);
+                }
+            }
+            walkTotal += thr * term + totRefl + totSrc;
+            lenSum += wlen;
+            success = true;
+        }
+        if (nStack > 0) { beginSplit(); return true; }
+        if (success) {
+            atomicAdd(P.accSum + point, (double)walkTotal);
+            atomicAdd(P.accSq + point, (double)walkTotal * (double)walkTotal);
+            atomicAdd(P.accN + point, 1);
+            atomicAdd(reinterpret_cast<unsigned long long*>(P.accLen + point), (unsigned long long)lenSum);
+            if (splits) atomicAdd(reinterpret_cast<unsigned long long*>(P.accSplits + point), (unsigned long long)splits);
+        }
+        return false;
+    }
+
+    // --------------------------------------------------------------- Walk on Spheres step
+    ZG_D bool stepWoS() {
+        const zgpu_walk_settings& ws = P.ws;
+        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        steps++;
+        g.update(pt, distAbs);
+        if (!ws.ignore_source_contribution) {
+            float src;
+            if (P.pde.is_source_constant) {
+                src = g.norm() * pde.source(pt);
+            } else {
+                V<D> d = sampleSphere<D>(rng);
+                float r = g.sampleRadius(rng);
+                src = g.norm() * pde.source(pt + r * d);
+            }
+            totSrc += thr * src;
+        }
+        V<D> dir = sampleSphere<D>(rng);
+        pt = pt + distAbs * dir;
+        cpValid = false;
+        thr *= g.directionSampledPoissonKernel(pt);
+        if (outsideBox(P, pt.v, D)) return terminate(kEscaped);
+        if (weightWindow()) return terminate(kRussianRoulette);
+        wlen++;
+        if (wlen >= ws.max_walk_length) return terminate(kExceeded);
+        if (P.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        closestQuery();
+        return true;
+    }
+
+    // --------------------------------------------------------------- Walk on Stars step
+    ZG_D bool stepWoSt() {
+        const zgpu_walk_settings& ws = P.ws;
+        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        steps++;
+        float R;
+        if (firstStep && fsr > 0.0f) {
+            R = fsr;
+        } else {
+            flip = false;
+            if (ws.solve_double_sided && onRefl && prevDist > 0.0f && dot(prevDir, nrm) < 0.0f) {
+                nrm = -nrm;
+                flip = true;
+            }
+            if (ws.steps_before_using_maximal_spheres <= wlen) {
+                R = distAbs;
+            } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
+                R = ws.epsilon_shell_for_reflecting_boundary;
+            } else {
+                R = P.hasRefl ? starRadius<D>(P.reflecting, pt, ws.epsilon_shell_for_reflecting_boundary, distAbs,
+                                              ws.silhouette_precision, flip, S, err)
+                              : distAbs;
+                if (P.hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
+                    R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
+            }
+        }
+        g.update(pt, R);
+        V<D> dir = sampleSphere<D>(rng);
+        if (onRefl && dot(nrm, dir) > 0.0f) dir = -dir;
+        V<D> origin = onRefl ? offsetPoint<D>(pt, -nrm) : pt;
+        V<D> hitPt, hitN;
+        float hitDist;
+        bool hit = false;
+        if (P.hasRefl) {
+            RayHit<D> h = intersectRay<D>(P.reflecting, origin, dir, R, false, S, err);
+            if (h.slot >= 0) {
+                hit = true;
+                hitDist = h.t;
+                hitPt = origin + h.t * dir;
+                hitN = primNormal<D>(loadPrim<D>(P.reflecting, h.slot));
+            }
+        }
+        if (!hit) {
+            hitPt = origin + R * dir;
+            hitDist = R;
+            hitN = vzero<D>();
+        }
+        // reflecting boundary contribution (walk_on_stars.h:190-250)
+        if (P.hasRefl && !ws.ignore_reflecting_boundary_contribution) {
+            float u[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) u[i] = rng.uniform();
+            V<D> bpt, bn;
+            float pdf;
+            if (sampleBoundary<D>(P.reflecting, pt, R, u, bpt, bn, pdf)) {
+                V<D> toS = bpt - pt;
+                float dS = len(toS);
+                float alpha = onRefl ? 2.0f : 1.0f;
+                bool aligned = false;
+                if (ws.solve_double_sided) {
+                    toS = (1.0f / dS) * toS;
+                    if (flip) {
+                        aligned = true;
+                    } else if (dot(toS, bn) < -ws.silhouette_precision) {
+                        bool fs = true;
+                        if (alpha > 1.0f) fs = dot(toS, nrm) < -ws.silhouette_precision;
+                        if (fs) aligned = true;
+                    }
+                }
+                V<D> bnA = aligned ? -bn : bn;
+                if (pdf > 0.0f && dS < R) {
+                    V<D> p1 = onRefl ? offsetPoint<D>(pt, -nrm) : pt;
+                    V<D> p2 = offsetPoint<D>(bpt, -bnA);
+                    V<D> seg = p2 - p1;
+                    float sl = len(seg);
+                    bool occluded = false;
+                    if (sl > 0.0f) {
+                        RayHit<D> oh = intersectRay<D>(P.reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
+                        occluded = oh.slot >= 0;
+                    }
+                    if (!occluded) {
+                        float r = fmaxf(kRClamp, dS);
+                        float G = g.evaluate(r);
+                        float h = pde.robin(bpt, bn, ws.solve_double_sided && aligned);
+                        totRefl += thr * alpha * G * h / pdf;
+                    }
+                }
+            }
+        }
+        // source contribution (walk_on_stars.h:253-275)
+        if (!ws.ignore_source_contribution) {
+            float r = g.sampleRadius(rng);
+            if (r <= hitDist) totSrc += thr * g.norm() * pde.source(pt + r * dir);
+        }
+        prevDist = hitDist;
+        prevDir = dir;
+        pt = hitPt;
+        nrm = hitN;
+        onRefl = hit;
+        cpValid = false;
+        // walk step throughput (walk_on_stars.h:278-307)
+        float stepThr;
+        if (onRefl && prevDist > kFltEps) {
+            float kappa = 0.0f;
+            V<D> n = nrm;
+            if (!P.pde.are_robin_conditions_pure_neumann) {
+                bool f2 = false;
+                if (ws.solve_double_sided) { f2 = dot(prevDir, nrm) < 0.0f; if (f2) n = -n; }
+                kappa = pde.robinCoeff(ws.solve_double_sided && f2);
+            }
+            float refl = g.reflectance(prevDist, prevDir, n, kappa);
+            float maxRefl = P.pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
+            stepThr = fminf(fmaxf(refl, 0.0f), maxRefl);
+        } else {
+            stepThr = g.directionSampledPoissonKernel(pt);
+        }
+        thr *= stepThr;
+        if (!onRefl && outsideBox(P, pt.v, D)) return terminate(kEscaped);
+        if (weightWindow()) return terminate(kRussianRoulette);
+        wlen++;
+        if (wlen >= ws.max_walk_length) return terminate(kExceeded);
+        if (P.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        closestQuery();
+        firstStep = false;
+        return true;
+    }
+
+    ZG_D bool step() { return SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES ? stepWoS() : stepWoSt(); }
+};
+
+constexpr int kWalkThreads = 128;
+
+template <int D, int SOLVER, bool SCREENED>
+__global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant__ SolveParams P) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, P.stackEntries};
+    Walker<D, SOLVER, SCREENED> W(P, S);
+    W.splitSlots = P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack;
+    const int lane = threadIdx.x & 31;
+    const long long total = (long long)__ldg(P.walkStart + P.nPoints);
+    bool active = false, exhausted = false;
+    for (;;) {
+        bool need = !active && !exhausted;
+        unsigned m = __ballot_sync(kFull, need);
+        if (m) {
+            int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(P.counters + kCtrNext, (unsigned long long)__popc(m));
+            base = __shfl_sync(kFull, base, leader);
+            if (need) {
+                long long id = (long long)base + __popc(m & ((1u << lane) - 1u));
+                if (id >= total) exhausted = true;
+                else { W.start(id); active = true; }
+            }
+        }
+        if (!__any_sync(kFull, active)) break;
+        if (active) active = W.step();
+    }
+    // warp-reduce the counters, one atomic per warp
+    unsigned long long v[4] = {W.steps, W.escaped, W.exceeded, W.rr};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    uint32_t e = W.err;
+    for (int o = 16; o > 0; o >>= 1) e |= __shfl_xor_sync(kFull, e, o);
+    if (lane == 0) {
+        atomicAdd(P.counters + kCtrSteps, v[0]);
+        if (v[1]) atomicAdd(P.counters + kCtrEscaped, v[1]);
+        if (v[2]) atomicAdd(P.counters + kCtrExceeded, v[2]);
+        if (v[3]) atomicAdd(P.counters + kCtrRR, v[3]);
+        if (e) atomicOr(P.errorWord, e);
+    }
+}
+
+// ------------------------------------------------------------------------- prepare
+constexpr int kQueryThreads = 128;
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_constant__ SolveParams P) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, P.stackEntries};
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nPoints) return;
+    DevicePde<D> pde; pde.p = &P.pde;
+    const zgpu_walk_settings& ws = P.ws;
+    int eq = P.eq ? P.eq[i] : ZGPU_ESTIMATE_SOLUTION;
+    int type = P.type ? P.type[i] : ZGPU_SAMPLE_IN_DOMAIN;
+    int nPrev = P.statN[i];
+    P.nPrev[i] = nPrev;
+    P.accSum[i] = 0.0; P.accSq[i] = 0.0; P.accN[i] = 0; P.accLen[i] = 0; P.accSplits[i] = 0;
+    bool hasPrev = nPrev > 0 && P.fsrPersistent;
+    int flags = 0;
+    long long count = 0;
+    float dAbs = P.distAbs[i];
+    bool aligned = P.aligned ? P.aligned[i] != 0 : false;
+    if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && ws.solve_double_sided && type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && aligned)
+        flags |= kPointFlip;
+    if (eq == ZGPU_ESTIMATE_SKIP) {
+        count = 0;
+    } else if (type == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) {
+        if (nPrev == 0) { flags |= kPointBoundaryValue; P.fsr[i] = 0.0f; }
+        count = 0;
+    } else {
+        count = dAbs <= ws.epsilon_shell_for_absorbing_boundary ? 1 : max(P.nWalks[i], 0);
+        if (!hasPrev) {
+            float r;
+            if (P.solver == ZGPU_SOLVER_WALK_ON_SPHERES) {
+                r = dAbs;
+            } else if (dAbs <= ws.epsilon_shell_for_absorbing_boundary || ws.steps_before_using_maximal_spheres == 0) {
+                r = dAbs;
+            } else if (type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && pde.hasNonZeroRobinCoeff()) {
+                r = ws.epsilon_shell_for_reflecting_boundary;
+            } else {
+                uint32_t err = 0;
+                V<D> x = vload<D>(P.pt + (size_t)i * D);
+                r = P.hasRefl ? starRadius<D>(P.reflecting, x, ws.epsilon_shell_for_reflecting_boundary, dAbs,
+                                              ws.silhouette_precision, (flags & kPointFlip) != 0, S, err)
+                              : dAbs;
+                if (P.hasRefl && ws.epsilon_shell_for_reflecting_boundary <= dAbs)
+                    r = fmaxf(kRadiusShrink * r, ws.epsilon_shell_for_reflecting_boundary);
+                if (err) atomicOr(P.errorWord, err);
+            }
+            P.fsr[i] = r;
+        }
+    }
+    P.pointFlags[i] = flags;
+    P.walkStart[i] = count;
+}
+
+// ------------------------------------------------------------------------- finalize
+template <int D>
+__global__ void finalizeKernel(const __grid_constant__ SolveParams P) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nPoints) return;
+    DevicePde<D> pde; pde.p = &P.pde;
+    int flags = P.pointFlags[i];
+    int n2 = P.accN[i];
+    double mean2 = 0.0, m22 = 0.0;
+    if (flags & kPointBoundaryValue) {
+        float v = 0.0f;
+        if (!P.ws.ignore_absorbing_boundary_contribution) {
+            bool aligned = P.ws.solve_double_sided && P.aligned && P.aligned[i] != 0;
+            v = pde.dirichlet(vload<D>(P.pt + (size_t)i * D), aligned);
+        }
+        n2 = 1; mean2 = v; m22 = 0.0;
+    } else if (n2 > 0) {
+        double s = P.accSum[i], q = P.accSq[i];
+        mean2 = s / n2;
+        m22 = fmax(0.0, q - s * mean2);
+    }
+    if (n2 > 0) {
+        int n1 = P.nPrev[i];
+        int nt = n1 + n2;
+        if (n1 == 0) {
+            P.statMean[i] = mean2;
+            P.statM2[i] = m22;
+        } else {
+            double m1 = P.statMean[i];
+            double delta = mean2 - m1;
+            P.statMean[i] = m1 + delta * ((double)n2 / nt);
+            P.statM2[i] = P.statM2[i] + m22 + delta * delta * ((double)n1 * (double)n2 / nt);
+        }
+        P.statN[i] = nt;
+    }
+    P.statLen[i] += P.accLen[i];
+    P.statSplits[i] += P.accSplits[i];
+}
+
+// ------------------------------------------------------------------------- query kernels
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) closestKernel(BoundaryView b, int64_t n, const float* x, int computeSigned, float* pt, float* nrm,
+                              float* dist, int* prim, unsigned int* errw) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + b.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, b.stackEntries};
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0;
+    V<D> q = vload<D>(x + (size_t)i * D);
+    ClosestHit<D> h = closestPoint<D>(b, q, S, err);
+    V<D> nn = vzero<D>();
+    int idx = -1;
+    float d = h.d;
+    if (h.slot >= 0) {
+        nn = primNormal<D>(loadPrim<D>(b, h.slot));
+        idx = b.primIndex[h.slot];
+        if (computeSigned && dot(q - h.pt, nn) < 0.0f) d = -d;
+    }
+    if (pt) vstore<D>(h.pt, pt + (size_t)i * D);
+    if (nrm) vstore<D>(nn, nrm + (size_t)i * D);
+    if (dist) dist[i] = d;
+    if (prim) prim[i] = idx;
+    if (err) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) intersectKernel(BoundaryView b, int64_t n, const float* o, const float* nrmIn, const float* dir,
+                                const float* tmax, const int* onb, int* hit, float* pt, float* nrm, float* dist,
+                                int* prim, unsigned int* errw) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + b.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, b.stackEntries};
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0;
+    V<D> origin = vload<D>(o + (size_t)i * D);
+    if (onb && onb[i]) origin = offsetPoint<D>(origin, -vload<D>(nrmIn + (size_t)i * D));
+    V<D> d = vload<D>(dir + (size_t)i * D);
+    RayHit<D> h = intersectRay<D>(b, origin, d, tmax[i], false, S, err);
+    bool ok = h.slot >= 0;
+    hit[i] = ok;
+    V<D> p = ok ? origin + h.t * d : vzero<D>();
+    V<D> nn = ok ? primNormal<D>(loadPrim<D>(b, h.slot)) : vzero<D>();
+    if (pt) vstore<D>(p, pt + (size_t)i * D);
+    if (nrm) vstore<D>(nn, nrm + (size_t)i * D);
+    if (dist) dist[i] = ok ? h.t : kFltMax;
+    if (prim) prim[i] = ok ? b.primIndex[h.slot] : -1;
+    if (err) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) countHitsKernel(BoundaryView b, int64_t n, const float* o, const float* dir, const float* tmax,
+                                int* out, unsigned int* errw) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + b.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, b.stackEntries};
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0;
+    out[i] = countHits<D>(b, vload<D>(o + (size_t)i * D), vload<D>(dir + (size_t)i * D), tmax[i], S, err);
+    if (err) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) starRadiusKernel(BoundaryView b, int64_t n, const float* x, const float* minR, const float* maxR,
+                                 float prec, const int* flip, float* out, unsigned int* errw) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + b.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, b.stackEntries};
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0;
+    out[i] = starRadius<D>(b, vload<D>(x + (size_t)i * D), minR[i], maxR[i], prec, flip && flip[i], S, err);
+    if (err) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) occludedKernel(BoundaryView b, int64_t n, const float* xi, const float* xj, const float* ni,
+                               const float* nj, const int* oi, const int* oj, int* out, unsigned int* errw) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + b.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, b.stackEntries};
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t err = 0;
+    V<D> p1 = vload<D>(xi + (size_t)k * D), p2 = vload<D>(xj + (size_t)k * D);
+    if (oi && oi[k]) p1 = offsetPoint<D>(p1, -vload<D>(ni + (size_t)k * D));
+    if (oj && oj[k]) p2 = offsetPoint<D>(p2, -vload<D>(nj + (size_t)k * D));
+    V<D> s = p2 - p1;
+    float l = len(s);
+    int occ = 0;
+    if (l > 0.0f) occ = intersectRay<D>(b, p1, (1.0f / l) * s, l, true, S, err).slot >= 0;
+    out[k] = occ;
+    if (err) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void sampleKernel(BoundaryView b, int64_t n, const float* x, const float* r, const float* u, int* found,
+                             float* pt, float* nrm, float* pdf) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    V<D> p, nn;
+    float pp = 0.0f;
+    float uu[D];
+    for (int i = 0; i < D; i++) uu[i] = u[(size_t)k * D + i];
+    bool ok = sampleBoundary<D>(b, vload<D>(x + (size_t)k * D), r[k], uu, p, nn, pp);
+    if (!ok) { p = vzero<D>(); nn = vzero<D>(); pp = 0.0f; }
+    found[k] = ok;
+    vstore<D>(p, pt + (size_t)k * D);
+    vstore<D>(nn, nrm + (size_t)k * D);
+    pdf[k] = pp;
+}
+
+inline unsigned gridFor(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace detail
+
+
+inline size_t smemBytes(int stackEntries, int threads) { return (size_t)stackEntries * threads * 8; }
+
+// walk kernel launchers, explicitly instantiated per (dimension, solver) in zgpu_walk_<D>d_<solver>.cu
+template <int D, int SOLVER>
+struct WalkLaunch {
+    static cudaError_t walk(const SolveParams& p, int blocks, int threads, cudaStream_t s) {
+        size_t smem = smemBytes(p.stackEntries, threads);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (p.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true><<<blocks, threads, smemBytes(p.stackEntries, threads), s>>>(p);
+        else detail::walkKernel<D, SOLVER, false><<<blocks, threads, smemBytes(p.stackEntries, threads), s>>>(p);
+        return cudaGetLastError();
+    }
+    static int maxBlocksPerSM(bool screened, int threads, int stackEntries) {
+        int n = 0;
+        size_t smem = smemBytes(stackEntries, threads);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const void* f = screened ? (const void*)detail::walkKernel<D, SOLVER, true> : (const void*)detail::walkKernel<D, SOLVER, false>;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smemBytes(stackEntries, threads)) != cudaSuccess) return 1;
+        return n > 0 ? n : 1;
+    }
+};
+
+// per-dimension launchers of the bookkeeping and query kernels, instantiated in zgpu_kernels{2,3}.cu
+template <typename K>
+inline void allowStack(K kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes(kMaxStack, detail::kQueryThreads));
+}
+
+template <int D>
+struct Launch {
+    static cudaError_t prepare(const SolveParams& p, cudaStream_t s) {
+        if (p.nPoints == 0) return cudaSuccess;
+        allowStack(detail::prepareKernel<D>);
+        detail::prepareKernel<D><<<detail::gridFor(p.nPoints, detail::kQueryThreads), detail::kQueryThreads, smemBytes(p.stackEntries, detail::kQueryThreads), s>>>(p);
+        return cudaGetLastError();
+    }
+    static cudaError_t finalize(const SolveParams& p, cudaStream_t s) {
+        if (p.nPoints == 0) return cudaSuccess;
+        detail::finalizeKernel<D><<<detail::gridFor(p.nPoints, 256), 256, 0, s>>>(p);
+        return cudaGetLastError();
+    }
+    static cudaError_t closest(const BoundaryView& b, int64_t n, const float* x, int computeSigned, float* pt, float* nrm,
+                               float* dist, int* prim, unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        allowStack(detail::closestKernel<D>);
+        detail::closestKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, x, computeSigned, pt, nrm, dist, prim, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t intersect(const BoundaryView& b, int64_t n, const float* o, const float* nrmIn, const float* dir,
+                                 const float* tmax, const int* onb, int* hit, float* pt, float* nrm, float* dist, int* prim,
+                                 unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        allowStack(detail::intersectKernel<D>);
+        detail::intersectKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, o, nrmIn, dir, tmax, onb, hit, pt, nrm, dist, prim, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t countHits(const BoundaryView& b, int64_t n, const float* o, const float* dir, const float* tmax,
+                                 int* out, unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        allowStack(detail::countHitsKernel<D>);
+        detail::countHitsKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, o, dir, tmax, out, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t starRadius(const BoundaryView& b, int64_t n, const float* x, const float* minR, const float* maxR,
+                                  float prec, const int* flip, float* out, unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        allowStack(detail::starRadiusKernel<D>);
+        detail::starRadiusKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, x, minR, maxR, prec, flip, out, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t occluded(const BoundaryView& b, int64_t n, const float* xi, const float* xj, const float* ni,
+                                const float* nj, const int* oi, const int* oj, int* out, unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        allowStack(detail::occludedKernel<D>);
+        detail::occludedKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, xi, xj, ni, nj, oi, oj, out, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t sample(const BoundaryView& b, int64_t n, const float* x, const float* r, const float* u, int* found,
+                              float* pt, float* nrm, float* pdf, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        detail::sampleKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, x, r, u, found, pt, nrm, pdf);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace zg

@@ -1,0 +1,4 @@
+// zgpu_walk_3d_wos.cu -- instantiates the 3D Walk on Spheres kernels.
+#include "zgpu_kernels.cuh"
+
+template struct zg::WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>;
