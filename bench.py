@@ -30,6 +30,8 @@ WORKLOADS = {
                           desc="2D mixed Dirichlet/Neumann WoSt, 4096 segments, 256x256 grid, 512 spp, f=-1"),
     "mixed_wost_2d_screened": dict(fn="mixed_wost_2d", kw=dict(n_segments=4096, grid=256, spp=512, sigma=1.0),
                                    desc="2D mixed WoSt, screened Poisson sigma=1, 4096 segments, 256x256 grid, 512 spp"),
+    "mixed_wost_2d_small": dict(fn="mixed_wost_2d", kw=dict(n_segments=4096, grid=128, spp=128, sigma=0.0),
+                                desc="profiling case: 2D mixed WoSt, 4096 segments, 128x128 grid, 128 spp"),
     "laplace_wos_2d": dict(fn="laplace_wos_2d", kw=dict(n_segments=1024, grid=128, spp=256),
                            desc="2D Laplace WoS, 1024 segments, 128x128 grid, 256 spp"),
     "robin_wost_3d": dict(fn="robin_wost_3d", kw=dict(level=6, n_points=1_000_000, spp=128),

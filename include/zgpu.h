@@ -294,6 +294,30 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
                        zgpu_sample_statistics* stats, const zgpu_solve_options* options,
                        zgpu_solve_report* report);
 
+/* ------------------------- allocation-free solve -------------------------- */
+/*
+ * zgpu_solve_static: a variant of zgpu_solve that allocates nothing.  No counterpart in the
+ * reference; it exists for callers that must not allocate device memory, such as a plug-in
+ * whose host application owns the GPU memory budget, or a real-time loop that forbids
+ * cudaMalloc after start-up.  The caller passes inputs and outputs in device memory and the
+ * CUDA stream to run on (cudaStream_t, NULL = legacy default stream), with that stream's
+ * device current.  All scratch (walk prefix, per-point flags and FP64 accumulators,
+ * counters) lives in one file-scope __device__ array of ZGPU_STATIC_SCRATCH_BYTES that every
+ * GPU loading the library holds until process exit.
+ * Limits: points->n <= ZGPU_STATIC_MAX_POINTS; points and statistics in ZGPU_MEM_DEVICE;
+ * no walk splitting (splitting_threshold must be FLT_MAX).  Larger inputs are rejected with
+ * ZGPU_ERR_INVALID_ARG.  The first call on a device looks up the array's device address;
+ * make that first call before any stream capture.  Every call shares the one array and
+ * clears what must start at zero: calls that overlap on the GPU (two streams, two host
+ * threads) race and must be serialised by the caller.  The call returns after the stream
+ * has drained (it reads back the counters for the report and the error word).
+ */
+#define ZGPU_STATIC_MAX_POINTS 65536
+#define ZGPU_STATIC_SCRATCH_BYTES (4u << 20)
+int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_queries* queries, const zgpu_pde* pde,
+                      const zgpu_walk_settings* settings, const zgpu_sample_points* points,
+                      zgpu_sample_statistics* stats, zgpu_solve_report* report);
+
 #ifdef __cplusplus
 }
 #endif

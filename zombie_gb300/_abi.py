@@ -46,6 +46,8 @@ ZGPU_SOLVER_WALK_ON_SPHERES = 0
 ZGPU_SOLVER_WALK_ON_STARS = 1
 
 ZGPU_MAX_TERMS = 8
+ZGPU_STATIC_MAX_POINTS = 65536
+ZGPU_STATIC_SCRATCH_BYTES = 4 << 20
 FLT_MAX = 3.4028234663852886e38
 
 

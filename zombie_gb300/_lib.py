@@ -50,6 +50,7 @@ def lib():
         L.zgpu_query_sample_boundary.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32]
         L.zgpu_solve.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.zgpu_solve_batched.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp]
+        L.zgpu_solve_static.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp]
         if L.zgpu_abi_version() != A.ZGPU_ABI_VERSION:
             raise ZgpuError(A.ZGPU_ERR_INVALID_ARG, "ABI version mismatch between libzgpu.so and zombie_gb300")
         _lib = L

@@ -134,6 +134,16 @@ int checkField(int kind, const char* name) {
 
 }  // namespace
 
+// internal accessors used by the allocation-free entry point (zgpu_static.cu)
+namespace zg {
+void setLastError(const char* msg) { gLastError = msg; }
+bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind) {
+    if (!b) return false;
+    *view = b->view; *dim = b->dim; *kind = b->kind;
+    return true;
+}
+}  // namespace zg
+
 extern "C" {
 
 int zgpu_abi_version(void) { return ZGPU_ABI_VERSION; }

@@ -66,6 +66,10 @@ cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
 int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, int stackEntries);
 size_t scanScratchElems(int64_t n);
 
+// accessors into the C ABI objects (zgpu_api.cu)
+void setLastError(const char* msg);
+bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind);
+
 // batched query kernels
 cudaError_t launchClosest(const BoundaryView& b, int dim, int64_t n, const float* x, int computeSigned,
                           float* pt, float* nrm, float* dist, int* prim, unsigned int* err, cudaStream_t s);
