@@ -80,6 +80,9 @@ struct zgpu_boundary {
     float4* nodes = nullptr;
     float4* cones = nullptr;
     float4* prims = nullptr;
+    float4* silTree = nullptr;
+    float4* silCones = nullptr;
+    float4* silFeat = nullptr;
     float4* sil = nullptr;
     int* primIndex = nullptr;
     std::vector<int> primIndexHost;   // leaf slot -> caller index (for coefficient updates)
@@ -207,8 +210,9 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     if (!buildBoundary(dim, positions, n_vertices, indices, n_prims, kind, min_robin, max_robin,
                        solve_double_sided != 0, silhouette_precision, hb, err))
         return fail(ZGPU_ERR_INVALID_ARG, "boundary build: %s", err.c_str());
-    if (hb.depth > kMaxWideDepth)
-        return fail(ZGPU_ERR_UNSUPPORTED, "boundary BVH depth %d exceeds the traversal stack (max %d)", hb.depth, kMaxWideDepth);
+    if (hb.depth > kMaxWideDepth || hb.silDepth > kMaxWideDepth)
+        return fail(ZGPU_ERR_UNSUPPORTED, "boundary BVH depth %d/%d exceeds the traversal stack (max %d)", hb.depth,
+                    hb.silDepth, kMaxWideDepth);
     ZG_CUDA(cudaSetDevice(ctx->device));
     zgpu_boundary* b = new zgpu_boundary();
     b->ctx = ctx; b->dim = dim; b->kind = kind; b->nPrims = n_prims; b->nNodes = hb.nNodes; b->depth = hb.depth;
@@ -225,6 +229,9 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     if (e == cudaSuccess) e = upload((void**)&b->prims, hb.prims.data(), hb.prims.size() * sizeof(float4));
     if (e == cudaSuccess) e = upload((void**)&b->sil, hb.sil.data(), hb.sil.size() * sizeof(float4));
     if (e == cudaSuccess) e = upload((void**)&b->primIndex, hb.primIndex.data(), hb.primIndex.size() * sizeof(int));
+    if (e == cudaSuccess) e = upload((void**)&b->silTree, hb.silTree.data(), hb.silTree.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->silCones, hb.silCones.data(), hb.silCones.size() * sizeof(float4));
+    if (e == cudaSuccess) e = upload((void**)&b->silFeat, hb.silFeat.data(), hb.silFeat.size() * sizeof(float4));
     if (e != cudaSuccess) {
         zgpu_boundary_destroy(b);
         return fail(e == cudaErrorMemoryAllocation ? ZGPU_ERR_OUT_OF_MEMORY : ZGPU_ERR_CUDA, "boundary upload: %s",
@@ -232,7 +239,10 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     }
     b->view.nodes = b->nodes; b->view.cones = b->cones; b->view.prims = b->prims; b->view.sil = b->sil; b->view.primIndex = b->primIndex;
     b->view.nNodes = b->nNodes; b->view.nPrims = b->nPrims;
-    b->view.stackEntries = stackEntriesForDepth(b->depth);
+    b->view.stackEntries = stackEntriesForDepth(std::max(b->depth, hb.silDepth));
+    b->view.silTree = b->silTree; b->view.silCones = b->silCones; b->view.silFeat = b->silFeat;
+    b->view.silNodes = hb.silNodes;
+    b->view.robin = kind == ZGPU_BOUNDARY_ROBIN;
     *out = b;
     return ZGPU_OK;
 }
@@ -240,6 +250,7 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
 int zgpu_boundary_destroy(zgpu_boundary* b) {
     if (!b) return ZGPU_OK;
     if (b->ctx) cudaSetDevice(b->ctx->device);
+    cudaFree(b->silTree); cudaFree(b->silCones); cudaFree(b->silFeat);
     cudaFree(b->nodes); cudaFree(b->cones); cudaFree(b->prims); cudaFree(b->sil); cudaFree(b->primIndex);
     delete b;
     return ZGPU_OK;

@@ -225,6 +225,69 @@ void coneOf(int D, const std::vector<BNode>& bn, int node, const std::vector<int
     out.halfAngle = (float)std::min(3.14159265, h + 1e-4);
 }
 
+
+// Builds the wide tree over `n` items with the given boxes / centroids / weights; fills
+// `order` (leaf slot -> item) and returns the collapsed nodes (+ per-wide-node binary kids).
+struct WideTree {
+    std::vector<float4> nodes;
+    std::vector<std::array<int, 4>> kids;
+    std::vector<BNode> bnodes;
+    std::vector<int> order;
+    int depth = 0;
+};
+
+void buildWideTree(int D, const std::vector<Box>& boxes, const std::vector<float>& cent, const std::vector<float>& weight,
+                   WideTree& out) {
+    int n = (int)boxes.size();
+    Builder bld;
+    bld.D = D;
+    bld.pbox = boxes;
+    bld.cent = cent;
+    bld.parea = weight;
+    bld.order.resize(n);
+    std::iota(bld.order.begin(), bld.order.end(), 0);
+    bld.nodes.reserve((size_t)2 * n / kLeafMax + 16);
+    bld.build(0, n, 0);
+    out.order = bld.order;
+    out.bnodes = bld.nodes;
+    if (bld.nodes[0].count > 0) {
+        out.nodes.resize(8);
+        for (int i = 0; i < D; i++) {
+            out.nodes[i] = make_float4(bld.nodes[0].box.lo[i], kInf, kInf, kInf);
+            out.nodes[D + i] = make_float4(bld.nodes[0].box.hi[i], -kInf, -kInf, -kInf);
+        }
+        int4 ci = make_int4(makeLeafRef(0, bld.nodes[0].count), kEmpty, kEmpty, kEmpty);
+        std::memcpy(&out.nodes[2 * D], &ci, sizeof(int4));
+        out.nodes[2 * D + 1] = make_float4(bld.nodes[0].area, 0, 0, 0);
+        out.kids.push_back({0, -1, -1, -1});
+        out.depth = 1;
+        return;
+    }
+    Collapser col{D, out.bnodes, out.nodes};
+    col.emit(0, 1);
+    out.kids = col.kidsOf;
+    out.depth = col.maxDepth;
+}
+
+// Normal cone over a set of unit normals (axis = normalised mean, half angle = max deviation).
+void coneOverNormals(int D, const std::vector<const float*>& ns, bool open, float* axis, float& halfAngle) {
+    axis[0] = axis[1] = axis[2] = 0.0f;
+    if (open) { halfAngle = 3.14159265f; return; }
+    if (ns.empty()) { halfAngle = -1.0f; return; }
+    double a[3] = {0, 0, 0};
+    for (const float* n : ns) for (int i = 0; i < D; i++) a[i] += n[i];
+    double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (l < 1e-6) { halfAngle = 3.14159265f; return; }
+    for (int i = 0; i < 3; i++) axis[i] = (float)(a[i] / l);
+    double h = 0.0;
+    for (const float* n : ns) {
+        double c = 0.0;
+        for (int i = 0; i < D; i++) c += axis[i] * n[i];
+        h = std::max(h, std::acos(std::max(-1.0, std::min(1.0, c))));
+    }
+    halfAngle = (float)std::min(3.14159265, h + 1e-4);
+}
+
 }  // namespace
 
 bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
@@ -420,6 +483,92 @@ bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int 
             const float* c = pos + (size_t)idx[i * D + 2] * D;
             vol += (((double)a[1] * b[2] - (double)a[2] * b[1]) * c[0] + ((double)a[2] * b[0] - (double)a[0] * b[2]) * c[1] +
                     ((double)a[0] * b[1] - (double)a[1] * b[0]) * c[2]) / 6.0;
+        }
+    }
+    // ---- silhouette-candidate tree (FCPW computeSilhouettes, fcpw_geometric_queries.h:631):
+    // every non-ignored vertex / edge once (kept by the face with the lower index when it has
+    // two faces), with the normals of its two faces
+    if (reflecting) {
+        struct Feature { float a[3], b[3], nA[3], nB[3]; bool open; };
+        std::vector<Feature> feats;
+        for (int i = 0; i < nP; i++) {
+            for (int j = 0; j < D; j++) {
+                if (flags[i] & (8 << j)) continue;
+                int a = adj[(size_t)i * D + j];
+                if (a >= 0 && a < i) continue;   // the other face holds this feature
+                Feature f{};
+                f.open = a < 0;
+                const float* n0 = &nrm[(size_t)i * D];
+                const float* na = a >= 0 ? &nrm[(size_t)a * D] : n0;
+                if (D == 2) {
+                    const float* v = pos + (size_t)idx[i * 2 + j] * 2;
+                    for (int k = 0; k < 2; k++) { f.a[k] = v[k]; f.b[k] = v[k]; }
+                    // j = 0: the vertex ends the neighbour and starts this segment
+                    const float* nPrev = j == 0 ? na : n0;
+                    const float* nNext = j == 0 ? n0 : na;
+                    for (int k = 0; k < 2; k++) { f.nA[k] = nPrev[k]; f.nB[k] = nNext[k]; }
+                } else {
+                    const float* pa = pos + (size_t)idx[i * 3 + j] * 3;
+                    const float* pb = pos + (size_t)idx[i * 3 + (j + 1) % 3] * 3;
+                    for (int k = 0; k < 3; k++) { f.a[k] = pa[k]; f.b[k] = pb[k]; f.nA[k] = n0[k]; f.nB[k] = na[k]; }
+                }
+                feats.push_back(f);
+            }
+        }
+        hb.silFeatures = (int)feats.size();
+        if (!feats.empty()) {
+            std::vector<Box> fb(feats.size());
+            std::vector<float> fc(feats.size() * D), fw(feats.size(), 1.0f);
+            for (size_t k = 0; k < feats.size(); k++) {
+                fb[k].grow(feats[k].a, D);
+                fb[k].grow(feats[k].b, D);
+                for (int i = 0; i < D; i++) fc[k * D + i] = 0.5f * (feats[k].a[i] + feats[k].b[i]);
+            }
+            WideTree wt;
+            buildWideTree(D, fb, fc, fw, wt);
+            hb.silTree = wt.nodes;
+            hb.silNodes = (int)(wt.nodes.size() / 8);
+            hb.silDepth = wt.depth;
+            hb.silCones.assign(wt.nodes.size(), make_float4(0, 0, 0, -1));
+            for (size_t w = 0; w < wt.kids.size(); w++) {
+                for (int c = 0; c < 4; c++) {
+                    int b = wt.kids[w][c];
+                    if (b < 0) continue;
+                    std::vector<int> stk = {b};
+                    std::vector<const float*> ns;
+                    bool open = false;
+                    while (!stk.empty()) {
+                        const BNode& m = wt.bnodes[stk.back()]; stk.pop_back();
+                        if (m.count == 0) { stk.push_back(m.left); stk.push_back(m.right); continue; }
+                        for (int q = 0; q < m.count; q++) {
+                            const Feature& f = feats[wt.order[m.first + q]];
+                            if (f.open) open = true;
+                            ns.push_back(f.nA);
+                            ns.push_back(f.nB);
+                        }
+                    }
+                    float axis[3], half;
+                    coneOverNormals(D, ns, open, axis, half);
+                    hb.silCones[w * 8 + c] = make_float4(axis[0], axis[1], axis[2], half);
+                }
+            }
+            int per = D == 2 ? 2 : 4;
+            hb.silFeat.resize(feats.size() * per);
+            for (size_t s2 = 0; s2 < feats.size(); s2++) {
+                const Feature& f = feats[wt.order[s2]];
+                float fl;
+                int flg = f.open ? 1 : 0;
+                std::memcpy(&fl, &flg, 4);
+                if (D == 2) {
+                    hb.silFeat[s2 * 2] = make_float4(f.a[0], f.a[1], f.nA[0], f.nA[1]);
+                    hb.silFeat[s2 * 2 + 1] = make_float4(f.nB[0], f.nB[1], fl, 0.0f);
+                } else {
+                    hb.silFeat[s2 * 4] = make_float4(f.a[0], f.a[1], f.a[2], fl);
+                    hb.silFeat[s2 * 4 + 1] = make_float4(f.b[0], f.b[1], f.b[2], 0.0f);
+                    hb.silFeat[s2 * 4 + 2] = make_float4(f.nA[0], f.nA[1], f.nA[2], 0.0f);
+                    hb.silFeat[s2 * 4 + 3] = make_float4(f.nB[0], f.nB[1], f.nB[2], 0.0f);
+                }
+            }
         }
     }
     hb.signedVolume = (float)vol;

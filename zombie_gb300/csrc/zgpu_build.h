@@ -20,6 +20,14 @@ struct HostBoundary {
     std::vector<float4> prims;    // nPrims * (1 | 3)
     std::vector<float4> sil;      // reflecting only: nPrims * (2 | 3)
     std::vector<int> primIndex;   // leaf slot -> caller's primitive index
+    // silhouette-candidate tree (reflecting boundaries): one record per non-ignored vertex
+    // (2D) / edge (3D), deduplicated; 2D record 2 float4, 3D record 4 float4
+    int silNodes = 0;
+    int silDepth = 0;
+    int silFeatures = 0;
+    std::vector<float4> silTree;    // silNodes * 8 (wide nodes, same layout as `nodes`)
+    std::vector<float4> silCones;   // silNodes * 8 (child cones)
+    std::vector<float4> silFeat;    // silFeatures * (2 | 4)
 };
 
 // kind: 0 absorbing, 1 Neumann, 2 Robin (include/zgpu.h).  Returns false with a message.

@@ -85,16 +85,6 @@ struct Walker {
         g.sqrtLambda = sqrtf(fmaxf(P.pde.absorption_coeff, 0.0f));
     }
 
-    ZG_D int findPoint(long long id) const {
-        // largest i with walkStart[i] <= id
-        int64_t lo = 0, hi = P.nPoints;   // walkStart[nPoints] = total > id
-        while (hi - lo > 1) {
-            int64_t mid = (lo + hi) >> 1;
-            if (__ldg(P.walkStart + mid) <= id) lo = mid; else hi = mid;
-        }
-        return (int)lo;
-    }
-
     ZG_D void closestQuery() {
         if (P.hasAbs) {
             ClosestHit<D> h = closestPoint<D>(P.absorbing, pt, S, err);
@@ -113,8 +103,8 @@ struct Walker {
         g.yukawa = P.pde.absorption_coeff > 0.0f && P.ws.steps_before_applying_tikhonov == 0;
     }
 
-    ZG_D void start(long long id) {
-        point = findPoint(id);
+    ZG_D void start(long long id, int pointIndex) {
+        point = pointIndex;
         long long w = id - __ldg(P.walkStart + point);
         rng.seed(__ldg(P.seed + point), (uint64_t)w + (uint64_t)__ldg(P.nPrev + point));
         pt = vload<D>(P.pt + (size_t)point * D);
@@ -377,6 +367,25 @@ struct Walker {
 
 constexpr int kWalkThreads = 128;
 
+// Warp-cooperative search: the largest i in [0, nPoints) with walkStart[i] <= id (all 32
+// lanes take part; 32-ary narrowing with one coalesced probe per lane per round).
+ZG_D int warpFindPoint(const SolveParams& P, long long id, int lane) {
+    int64_t lo = 0, hi = P.nPoints;   // invariant: walkStart[lo] <= id < walkStart[hi]
+    while (hi - lo > 32) {
+        int64_t stride = (hi - lo + 31) / 32;
+        int64_t probe = lo + (int64_t)lane * stride;
+        bool le = probe < hi && __ldg(P.walkStart + probe) <= id;
+        unsigned b = __ballot_sync(kFull, le);
+        int k = 31 - __clz(b);            // lane 0 always holds lo itself
+        lo = lo + (int64_t)k * stride;
+        hi = lo + stride < hi ? lo + stride : hi;
+    }
+    int64_t probe = lo + lane;
+    bool le = probe < hi && __ldg(P.walkStart + probe) <= id;
+    unsigned b = __ballot_sync(kFull, le);
+    return (int)(lo + 31 - __clz(b));
+}
+
 template <int D, int SOLVER, bool SCREENED>
 __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant__ SolveParams P) {
     extern __shared__ int dynStack[];
@@ -395,10 +404,21 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
             unsigned long long base = 0;
             if (lane == leader) base = atomicAdd(P.counters + kCtrNext, (unsigned long long)__popc(m));
             base = __shfl_sync(kFull, base, leader);
-            if (need) {
-                long long id = (long long)base + __popc(m & ((1u << lane) - 1u));
-                if (id >= total) exhausted = true;
-                else { W.start(id); active = true; }
+            if ((long long)base < total) {
+                int p0 = warpFindPoint(P, (long long)base, lane);
+                if (need) {
+                    long long id = (long long)base + __popc(m & ((1u << lane) - 1u));
+                    if (id >= total) {
+                        exhausted = true;
+                    } else {
+                        int p = p0;
+                        while (__ldg(P.walkStart + p + 1) <= id) p++;   // walks of a point are contiguous
+                        W.start(id, p);
+                        active = true;
+                    }
+                }
+            } else if (need) {
+                exhausted = true;
             }
         }
         if (!__any_sync(kFull, active)) break;

@@ -54,6 +54,12 @@ struct BoundaryView {
     int nNodes = 0;
     int nPrims = 0;
     int stackEntries = 8;   // traversal stack entries this tree needs (from its wide depth)
+    // silhouette-candidate tree of a Neumann boundary (Robin boundaries use the primitives)
+    const float4* silTree = nullptr;
+    const float4* silCones = nullptr;
+    const float4* silFeat = nullptr;
+    int silNodes = 0;
+    int robin = 0;
 };
 
 ZG_HD bool isLeaf(int c) { return c < 0; }
@@ -575,11 +581,85 @@ ZG_D bool coneMayHoldSilhouette(float4 cone, const WideNode<D>& w, int k, V<D> x
 }
 
 // computeStarRadiusForReflectingBoundary: max(sqrt(min(maxR^2, silhouettes, Robin bounds)), minR)
+// one silhouette-candidate record: 2D vertex (v, nPrev, nNext), 3D edge (a, b, nA, nB)
+ZG_D void featureRadius(const BoundaryView& b, int slot, V<2> x, float& r2, bool flip, float prec) {
+    float4 f0 = __ldg(b.silFeat + 2 * (size_t)slot), f1 = __ldg(b.silFeat + 2 * (size_t)slot + 1);
+    V<2> view; view[0] = x[0] - f0.x; view[1] = x[1] - f0.y;
+    float d2 = len2(view);
+    if (d2 >= r2) return;
+    float d = sqrtf(d2);
+    bool sil = __float_as_int(f1.z) != 0;
+    if (!sil) {
+        V<2> nPrev; nPrev[0] = f0.z; nPrev[1] = f0.w;
+        V<2> nNext; nNext[0] = f1.x; nNext[1] = f1.y;
+        sil = silhouetteVertex(nPrev, nNext, view, d, flip, prec);
+    }
+    if (sil) r2 = d2;
+}
+ZG_D void featureRadius(const BoundaryView& b, int slot, V<3> x, float& r2, bool flip, float prec) {
+    const float4* f = b.silFeat + 4 * (size_t)slot;
+    float4 f0 = __ldg(f), f1 = __ldg(f + 1);
+    V<3> pa; pa[0] = f0.x; pa[1] = f0.y; pa[2] = f0.z;
+    V<3> pb; pb[0] = f1.x; pb[1] = f1.y; pb[2] = f1.z;
+    V<3> q;
+    float d = closestOnSegment<3>(pa, pb, x, q);
+    if (d * d >= r2) return;
+    bool sil = __float_as_int(f0.w) != 0;
+    if (!sil) {
+        float4 f2 = __ldg(f + 2), f3 = __ldg(f + 3);
+        V<3> nA; nA[0] = f2.x; nA[1] = f2.y; nA[2] = f2.z;
+        V<3> nB; nB[0] = f3.x; nB[1] = f3.y; nB[2] = f3.z;
+        sil = silhouetteEdge(pa, pb, nA, nB, x - q, d, flip, prec);
+    }
+    if (sil) r2 = d * d;
+}
+
+// closest silhouette point of a Neumann boundary within sqrt(r2) (FCPW findClosestSilhouettePoint,
+// fcpw_geometric_queries.h:1264): traversal of the candidate tree, cone-pruned
+template <int D>
+__device__ __noinline__ float silhouetteRadius2(const BoundaryView& b, V<D> x, float r2, bool flip, float prec,
+                                                TravStack& S, uint32_t& err) {
+    if (b.silNodes == 0) return r2;
+    BoundaryView t = b;
+    t.nodes = b.silTree;
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        WideNode<D> w;
+        loadNode<D>(t, node, w);
+        ChildOrder ord; ord.clear();
+        unsigned leaves = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int c = w.child[k];
+            float d2 = boxDist2<D>(w, k, x);
+            bool ok = c != kEmptyChild && d2 < r2 &&
+                      coneMayHoldSilhouette<D>(__ldg(b.silCones + (size_t)node * 8 + k), w, k, x, prec);
+            if (ok && isLeaf(c)) leaves |= 1u << k;
+            if (ok && !isLeaf(c)) { ord.k[k] = d2; ord.c[k] = c; }
+        }
+        while (leaves) {
+            int k = __ffs(leaves) - 1;
+            leaves &= leaves - 1;
+            int c = pick4(k, w.child[0], w.child[1], w.child[2], w.child[3]);
+            int first = leafFirst(c), count = leafCount(c);
+#pragma unroll 1
+            for (int j = 0; j < count; j++) featureRadius(b, first + j, x, r2, flip, prec);
+        }
+        ord.sort();
+        int next = descendAndPush(ord, r2, S, sp, err);
+        node = next >= 0 ? next : popWithin(r2, S, sp);
+        if (node < 0) break;
+    }
+    return r2;
+}
+
 template <int D>
 __device__ __noinline__ float starRadius(const BoundaryView& b, V<D> x, float minR, float maxR, float prec, bool flip,
                                          TravStack& S, uint32_t& err) {
     if (minR > maxR) return maxR;
     float r2 = maxR < kFltMax ? maxR * maxR : kFltMax;
+    if (!b.robin) return fmaxf(sqrtf(silhouetteRadius2<D>(b, x, r2, flip, prec, S, err)), minR);
     if (b.nNodes > 0) {
         int sp = 0;
         int node = 0;
