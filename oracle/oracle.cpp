@@ -38,6 +38,7 @@ Boundary<D>* makeBoundary(const float* pos, int nV, const int* idx, int nP, int 
     b->useBvh = useBvh != 0;
     b->buildBvh();
     b->buildCones();
+    b->buildFeatureTree();
     return b;
 }
 

@@ -309,6 +309,15 @@ struct Boundary {
     void buildAdjacency(bool solveDoubleSided, float silhouettePrecision);
     void buildBvh();
     void buildCones();
+    // silhouette-candidate tree of a Neumann boundary (FCPW computeSilhouettes + its BVH):
+    // one record per non-ignored vertex (2D) / edge (3D), deduplicated
+    struct Feature { Vec<D> a, b, nA, nB; bool open; };
+    std::vector<Feature> feats;
+    std::vector<Node> fnodes;
+    std::vector<int> forder;
+    void buildFeatureTree();
+    int buildFeatureRecursive(int start, int end, int depth);
+    float featureRadius2(const Vec<D>& x, float r2, bool flip, float precision) const;
     bool coneMayHoldSilhouette(const Node& nd, const Vec<D>& x, float prec) const;
     int buildRecursive(int start, int end, std::vector<Vec<D>>& centroids, int depth);
 
@@ -604,6 +613,146 @@ inline void Boundary<3>::primStarRadius(int i, const Vec<3>& c, float& r2, bool 
     }
 }
 
+
+template <int D>
+int Boundary<D>::buildFeatureRecursive(int start, int end, int depth) {
+    int id = (int)fnodes.size();
+    fnodes.emplace_back();
+    Box<D> box, cbox;
+    for (int i = start; i < end; i++) {
+        const Feature& f = feats[forder[i]];
+        box.expand(f.a); box.expand(f.b);
+        cbox.expand(0.5f * (f.a + f.b));
+    }
+    fnodes[id].box = box;
+    int n = end - start;
+    if (n <= 4 || depth > 60) { fnodes[id].start = start; fnodes[id].count = n; return id; }
+    int ax = 0;
+    for (int i = 1; i < D; i++) if (cbox.hi[i] - cbox.lo[i] > cbox.hi[ax] - cbox.lo[ax]) ax = i;
+    int mid = start + n / 2;
+    std::nth_element(forder.begin() + start, forder.begin() + mid, forder.begin() + end, [&](int p, int q) {
+        return feats[p].a[ax] + feats[p].b[ax] < feats[q].a[ax] + feats[q].b[ax];
+    });
+    int l = buildFeatureRecursive(start, mid, depth + 1);
+    int r = buildFeatureRecursive(mid, end, depth + 1);
+    fnodes[id].left = l; fnodes[id].right = r;
+    return id;
+}
+
+template <int D>
+void Boundary<D>::buildFeatureTree() {
+    feats.clear(); fnodes.clear(); forder.clear();
+    if (kind != ZGPU_BOUNDARY_NEUMANN) return;
+    for (int i = 0; i < nPrims(); i++) {
+        Vec<D> p[D]; prim(i, p);
+        Vec<D> n0 = primNormal(p, true);
+        for (int j = 0; j < D; j++) {
+            if (ignore[i][j]) continue;
+            Feature f;
+            f.open = !hasAdj[i][j];
+            if constexpr (D == 2) {
+                f.a = p[j]; f.b = p[j];
+                f.nA = j == 0 ? adjN[i][0] : n0;   // the segment before the vertex
+                f.nB = j == 0 ? n0 : adjN[i][1];   // the segment after it
+            } else {
+                f.a = p[j]; f.b = p[(j + 1) % 3];
+                f.nA = n0; f.nB = adjN[i][j];
+            }
+            // a feature shared by two faces is kept once (by the first face that lists it)
+            bool dup = false;
+            if (!f.open) {
+                if constexpr (D == 2) dup = j == 1;   // each interior vertex: keep the copy of the segment it starts
+                else dup = false;
+            }
+            if (!dup) feats.push_back(f);
+        }
+    }
+    if constexpr (D == 3) {
+        // dedupe shared edges by their sorted endpoint coordinates
+        std::map<std::array<float, 6>, int> seen;
+        std::vector<Feature> kept;
+        for (auto& f : feats) {
+            std::array<float, 6> k;
+            bool ab = std::lexicographical_compare(f.a.v, f.a.v + 3, f.b.v, f.b.v + 3);
+            for (int i = 0; i < 3; i++) { k[i] = ab ? f.a[i] : f.b[i]; k[3 + i] = ab ? f.b[i] : f.a[i]; }
+            if (f.open || seen.emplace(k, 1).second) kept.push_back(f);
+        }
+        feats.swap(kept);
+    }
+    if (feats.empty()) return;
+    forder.resize(feats.size());
+    for (size_t i = 0; i < feats.size(); i++) forder[i] = (int)i;
+    buildFeatureRecursive(0, (int)feats.size(), 0);
+    // cones over the features' normals
+    for (auto& nd : fnodes) {
+        std::vector<int> stk = {(int)(&nd - &fnodes[0])};
+        std::vector<Vec<D>> ns;
+        bool open = false;
+        while (!stk.empty()) {
+            const Node& m = fnodes[stk.back()]; stk.pop_back();
+            if (m.count == 0) { stk.push_back(m.left); stk.push_back(m.right); continue; }
+            for (int k = 0; k < m.count; k++) {
+                const Feature& f = feats[forder[m.start + k]];
+                open = open || f.open;
+                ns.push_back(f.nA); ns.push_back(f.nB);
+            }
+        }
+        nd.kmax = 0.0f;
+        if (open) { nd.halfAngle = kPi; continue; }
+        double a[3] = {0, 0, 0};
+        for (auto& n : ns) for (int i = 0; i < D; i++) a[i] += n[i];
+        double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        if (l < 1e-6) { nd.halfAngle = kPi; continue; }
+        for (int i = 0; i < 3; i++) nd.axis[i] = (float)(a[i] / l);
+        double h = 0.0;
+        for (auto& n : ns) {
+            double c = 0.0;
+            for (int i = 0; i < D; i++) c += nd.axis[i] * n[i];
+            h = std::max(h, std::acos(std::max(-1.0, std::min(1.0, c))));
+        }
+        nd.halfAngle = (float)std::min((double)kPi, h + 1e-4);
+    }
+}
+
+// closest silhouette point within sqrt(r2) (FCPW findClosestSilhouettePoint, fcpw_geometric_queries.h:1264)
+template <int D>
+float Boundary<D>::featureRadius2(const Vec<D>& x, float r2, bool flip, float precision) const {
+    if (fnodes.empty()) return r2;
+    Counters& C = counters();
+    int stack[128]; int sp = 0; stack[sp++] = 0;
+    while (sp > 0) {
+        const Node& nd = fnodes[stack[--sp]];
+        C.nodes[3]++;
+        if (nd.box.dist2(x) > r2) continue;
+        if (!coneMayHoldSilhouette(nd, x, precision)) continue;
+        if (nd.count > 0) {
+            for (int k = 0; k < nd.count; k++) {
+                const Feature& f = feats[forder[nd.start + k]];
+                C.prims[3]++;
+                bool sil = f.open;
+                float d;
+                if constexpr (D == 2) {
+                    Vec<2> view = x - f.a;
+                    d = norm(view);
+                    if (d * d >= r2) continue;
+                    if (!sil) sil = isSilhouetteVertex(f.nA, f.nB, view, d, flip, precision);
+                } else {
+                    Vec<3> q;
+                    d = closestPointSegment3(f.a, f.b, x, q);
+                    if (d * d >= r2) continue;
+                    if (!sil) sil = isSilhouetteEdge(f.a, f.b, f.nA, f.nB, x - q, d, flip, precision);
+                }
+                if (sil) r2 = d * d;
+            }
+            continue;
+        }
+        float dl = fnodes[nd.left].box.dist2(x), dr = fnodes[nd.right].box.dist2(x);
+        if (dl <= dr) { stack[sp++] = nd.right; stack[sp++] = nd.left; }
+        else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
+    }
+    return r2;
+}
+
 // computeStarRadiusForReflectingBoundary: Neumann (fcpw_geometric_queries.h:1254-1268) and
 // Robin (:1277-1289, ReflectanceBvh::computeSquaredStarRadius bvh.h:414-506) in one rule:
 // with kappa = 0 the reflectance primitives reduce to the closest-silhouette distance.
@@ -613,6 +762,7 @@ float Boundary<D>::starRadius(const Vec<D>& x, float minR, float maxR, float pre
     float r2 = maxR < kMaxFloat ? maxR * maxR : kMaxFloat;
     Counters& C = counters();
     C.calls[3]++;
+    if (useBvh && kind == ZGPU_BOUNDARY_NEUMANN) return std::max(std::sqrt(featureRadius2(x, r2, flip, precision)), minR);
     if (!useBvh || nodes.empty()) {
         for (int i = 0; i < nPrims(); i++) primStarRadius(i, x, r2, flip, precision);
         C.prims[3] += nPrims();
