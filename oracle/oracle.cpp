@@ -17,6 +17,15 @@ struct Handle {
 
 std::atomic<uint64_t> gCounters[15];
 
+// moves this thread's traversal counters into the global totals
+void flushCounters() {
+    Counters& c = counters();
+    for (int k = 0; k < 5; k++) {
+        gCounters[k] += c.calls[k]; gCounters[5 + k] += c.nodes[k]; gCounters[10 + k] += c.prims[k];
+        c.calls[k] = c.nodes[k] = c.prims[k] = 0;
+    }
+}
+
 template <int D>
 Boundary<D>* makeBoundary(const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
                           const float* kmax, int doubleSided, float silPrec, int useBvh) {
@@ -92,11 +101,7 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
             }
         }
         steps += localSteps;
-        Counters& c = counters();
-        for (int k = 0; k < 5; k++) {
-            gCounters[k] += c.calls[k]; gCounters[5 + k] += c.nodes[k]; gCounters[10 + k] += c.prims[k];
-            c.calls[k] = c.nodes[k] = c.prims[k] = 0;
-        }
+        flushCounters();
     };
     if (nThreads <= 1) {
         work();
@@ -111,7 +116,8 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
 }  // namespace
 
 
-// traversal counters accumulated by orc_solve: calls[5], nodes[5], prims[5]; reset after read
+// traversal counters accumulated by orc_solve and the batched queries: calls[5], nodes[5],
+// prims[5]; reset after read
 extern "C" void orc_counters(uint64_t* out) {
     for (int k = 0; k < 15; k++) out[k] = gCounters[k].exchange(0);
 }
@@ -153,7 +159,8 @@ extern "C" double orc_signed_volume(void* hp) {
 
 #define ORC_DISPATCH(h, body2, body3) \
     if ((h)->dim == 2) { auto* b = (Boundary<2>*)(h)->b; constexpr int D = 2; (void)b; (void)D; body2; } \
-    else { auto* b = (Boundary<3>*)(h)->b; constexpr int D = 3; (void)b; (void)D; body3; }
+    else { auto* b = (Boundary<3>*)(h)->b; constexpr int D = 3; (void)b; (void)D; body3; } \
+    flushCounters();
 
 template <int D>
 static void closestImpl(const Boundary<D>* b, int64_t n, const float* x, float* pt, float* nrm, float* d, int* prim) {

@@ -266,6 +266,11 @@ struct Box {
         for (int i = 0; i < D; i++) { float d = std::max(std::max(lo[i] - x[i], 0.0f), x[i] - hi[i]); s += d * d; }
         return s;
     }
+    float maxDist2(const Vec<D>& x) const {
+        float s = 0.0f;
+        for (int i = 0; i < D; i++) { float d = std::max(std::fabs(x[i] - lo[i]), std::fabs(x[i] - hi[i])); s += d * d; }
+        return s;
+    }
     float surface() const {
         Vec<D> e = hi - lo;
         if (D == 2) return 2.0f * (e[0] + e[1]);
@@ -294,7 +299,8 @@ struct Boundary {
     // binary SAH BVH
     struct Node {
         Box<D> box; int left = -1, right = -1, start = 0, count = 0; float area = 0.0f;
-        float axis[3] = {0, 0, 0}; float halfAngle = 3.14159265f; float kmax = 0.0f;   // silhouette cone
+        float axis[3] = {0, 0, 0}; float halfAngle = 3.14159265f;   // normal cone
+        float kmin = 0.0f, kmax = 0.0f;                                  // Robin coefficient range
     };
     std::vector<Node> nodes;
     std::vector<int> order;
@@ -319,6 +325,7 @@ struct Boundary {
     int buildFeatureRecursive(int start, int end, int depth);
     float featureRadius2(const Vec<D>& x, float r2, bool flip, float precision) const;
     bool coneMayHoldSilhouette(const Node& nd, const Vec<D>& x, float prec) const;
+    bool robinVisit(const Node& nd, const Vec<D>& x, float r2, float& r2Min, float& r2Max) const;
     int buildRecursive(int start, int end, std::vector<Vec<D>>& centroids, int depth);
 
     // queries
@@ -767,25 +774,89 @@ float Boundary<D>::starRadius(const Vec<D>& x, float minR, float maxR, float pre
         for (int i = 0; i < nPrims(); i++) primStarRadius(i, x, r2, flip, precision);
         C.prims[3] += nPrims();
     } else {
-        int stack[128]; int sp = 0; stack[sp++] = 0;
+        // ReflectanceBvh::computeSquaredStarRadius (bvh.h:414-506): a node is entered with the
+        // lower bound of its radius as key; a node without silhouettes also caps the radius
+        int stack[128]; float key[128]; int sp = 0;
+        float lo, hi;
+        C.nodes[3]++;
+        if (robinVisit(nodes[0], x, r2, lo, hi)) { stack[sp] = 0; key[sp] = lo; sp++; }
         while (sp > 0) {
-            int ni = stack[--sp];
+            sp--;
+            int ni = stack[sp];
+            if (key[sp] > r2) continue;
             const Node& nd = nodes[ni];
-            C.nodes[3]++;
-            if (nd.box.dist2(x) > r2) continue;
-            // subtrees without Robin reflectance only matter through their silhouettes
-            if (nd.kmax <= kFcpwEpsilon && !coneMayHoldSilhouette(nd, x, precision)) continue;
             if (nd.count > 0) {
                 for (int k = 0; k < nd.count; k++) primStarRadius(order[nd.start + k], x, r2, flip, precision);
                 C.prims[3] += nd.count;
                 continue;
             }
-            float dl = nodes[nd.left].box.dist2(x), dr = nodes[nd.right].box.dist2(x);
-            if (dl <= dr) { stack[sp++] = nd.right; stack[sp++] = nd.left; }
-            else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
+            float l0, h0, l1, h1;
+            C.nodes[3] += 2;
+            bool hit0 = robinVisit(nodes[nd.left], x, r2, l0, h0);
+            if (hit0) r2 = std::min(r2, h0);
+            bool hit1 = robinVisit(nodes[nd.right], x, r2, l1, h1);
+            if (hit1) r2 = std::min(r2, h1);
+            // farther child first, the closer one on top
+            if (hit0 && hit1 && l1 < l0) { stack[sp] = nd.left; key[sp] = l0; sp++; stack[sp] = nd.right; key[sp] = l1; sp++; }
+            else {
+                if (hit1) { stack[sp] = nd.right; key[sp] = l1; sp++; }
+                if (hit0) { stack[sp] = nd.left; key[sp] = l0; sp++; }
+            }
         }
     }
     return std::max(std::sqrt(r2), minR);
+}
+
+// ReflectanceBvh::visitNode (bvh.h:369-412) with RobinBvhNodeBound (robin_bounds.h:110-154):
+// false when the node cannot lower the radius; otherwise r2Min is the key it is entered with
+// and r2Max a radius every primitive below it allows
+template <int D>
+bool Boundary<D>::robinVisit(const Node& nd, const Vec<D>& x, float r2, float& r2Min, float& r2Max) const {
+    r2Min = nd.box.dist2(x);
+    r2Max = nd.box.maxDist2(x);
+    if (r2Min > r2) return false;
+    if (nd.kmin >= kMaxFloat - kFcpwEpsilon) return true;          // perfectly absorbing subtree
+    // angular range of the normals as seen from x (the view cone of the box's bounding sphere)
+    bool silhouette = nd.halfAngle >= 0.5f * kPi;
+    float lo = 0.0f, hi = 0.5f * kPi;
+    if (!silhouette) {
+        Vec<D> v;
+        float rb2 = 0.0f;
+        for (int i = 0; i < D; i++) {
+            float h = 0.5f * (nd.box.hi[i] - nd.box.lo[i]);
+            rb2 += h * h;
+            v[i] = x[i] - 0.5f * (nd.box.lo[i] + nd.box.hi[i]);
+        }
+        float dv = norm(v);
+        if (dv * dv <= rb2) silhouette = true;
+        else {
+            Vec<D> a;
+            for (int i = 0; i < D; i++) a[i] = nd.axis[i];
+            float theta = std::acos(std::min(std::max(dot(a, v) / dv, -1.0f), 1.0f));
+            float spread = nd.halfAngle + std::asin(std::min(std::sqrt(rb2) / dv, 1.0f));
+            lo = theta - spread;
+            hi = theta + spread;
+            silhouette = spread >= 0.5f * kPi || (lo <= 0.5f * kPi && 0.5f * kPi <= hi);
+        }
+    }
+    if (silhouette) { r2Max = kMaxFloat; return true; }
+    if (nd.kmax <= kFcpwEpsilon) return false;                       // perfectly reflecting, no silhouette
+    float rMin = std::sqrt(r2Min), rMax = std::sqrt(r2Max);
+    float minCos = std::min(std::fabs(std::cos(lo)), std::fabs(std::cos(hi)));
+    if constexpr (D == 2) {
+        float a = rMin * std::exp(minCos / (nd.kmax * rMax));
+        float b = rMax * std::exp(1.0f / (nd.kmin * rMin));
+        r2Min = a * a;
+        r2Max = b * b;
+    } else {
+        if (rMax < minCos / nd.kmax) r2Min = kMaxFloat;
+        else { float a = rMin / (1.0f - minCos / (nd.kmax * rMax)); r2Min = a * a; }
+        if (rMin < 1.0f / nd.kmin) r2Max = kMaxFloat;
+        else { float b = rMax / (1.0f - 1.0f / (nd.kmin * rMin)); r2Max = b * b; }
+    }
+    if (!(r2Min == r2Min)) r2Min = 0.0f;
+    if (!(r2Max == r2Max)) r2Max = kMaxFloat;
+    return true;
 }
 
 // weighted pick: returns index i with probability w[i]/sum(w), rescales u to [0,1) for reuse
@@ -864,8 +935,10 @@ bool Boundary<D>::sample(const Vec<D>& x, float radius, const float* uIn, Vec<D>
 }
 
 // normal cone per node over the faces adjacent to its non-ignored silhouette features
-// (halfAngle < 0: no candidate; pi: an open feature or a degenerate axis) and the max
-// Robin coefficient of the subtree
+// (halfAngle < 0: no candidate; pi: an open feature or a degenerate axis) and the Robin
+// coefficient range of the subtree.  On a Robin boundary the cone covers every face of the
+// subtree and its neighbours, as computeBoundingConeForPrimitives does
+// (reflectance_boundary_bvh/bvh.h:210-262): the node bounds need the range of all normals.
 template <int D>
 void Boundary<D>::buildCones() {
     if (nodes.empty() || kind == ZGPU_BOUNDARY_ABSORBING) return;
@@ -873,16 +946,18 @@ void Boundary<D>::buildCones() {
         std::vector<int> stk = {(int)(&nd - &nodes[0])};
         std::vector<Vec<D>> ns;
         bool open = false;
-        float km = 0.0f;
+        const bool all = kind == ZGPU_BOUNDARY_ROBIN;
+        float km = 0.0f, kn = all ? kMaxFloat : 0.0f;
         while (!stk.empty()) {
             const Node& m = nodes[stk.back()]; stk.pop_back();
             if (m.count == 0) { stk.push_back(m.left); stk.push_back(m.right); continue; }
             for (int k = 0; k < m.count; k++) {
                 int i = order[m.start + k];
                 km = std::max(km, kmax[i]);
-                bool any = false;
+                if (all) kn = std::min(kn, kmin[i]);
+                bool any = all;
                 for (int j = 0; j < D; j++) {
-                    if (ignore[i][j]) continue;
+                    if (!all && ignore[i][j]) continue;
                     if (!hasAdj[i][j]) { open = true; continue; }
                     ns.push_back(adjN[i][j]);
                     any = true;
@@ -891,6 +966,7 @@ void Boundary<D>::buildCones() {
             }
         }
         nd.kmax = km;
+        nd.kmin = kn;
         if (open) { nd.halfAngle = kPi; continue; }
         if (ns.empty()) { nd.halfAngle = -1.0f; continue; }
         double a[3] = {0, 0, 0};

@@ -103,6 +103,49 @@ def test_star_radius_parity(zgpu, oracle, dim, kind, kappa):
     assert np.all(gr <= np.maximum(mx, mn) * (1 + 1e-6))
 
 
+def _mixed_robin(n, seed):
+    rng = np.random.default_rng(seed)
+    kmax = rng.uniform(0.5, 6.0, n).astype(np.float32)
+    kmin = (kmax * rng.uniform(0.3, 1.0, n)).astype(np.float32)
+    absorbing, reflecting = rng.random(n) < 0.05, rng.random(n) < 0.1
+    kmin[absorbing] = kmax[absorbing] = A.FLT_MAX
+    kmin[reflecting] = kmax[reflecting] = 0.0
+    return kmin, kmax
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_robin_node_bounds_after_coefficient_update(zgpu, oracle, dim):
+    """Per-face Robin coefficients (perfectly absorbing and purely reflecting faces mixed in),
+    set by updateCoefficientValues on a boundary built with other values: the refitted node
+    ranges give the radii of a boundary built with the new values and of the oracle."""
+    from zombie_gb300 import api
+    pos, idx = _scene(dim, level=4)
+    n = idx.shape[0]
+    kmin, kmax = _mixed_robin(n, 11)
+    ones = np.ones(n, np.float32)
+    updated = api.GpuRobinBoundaryHandler(dim)
+    updated.build_acceleration_structure(pos, idx, api.IgnoreCandidateSilhouette(False, 0.0), ones, ones)
+    updated.update_coefficient_values(kmin, kmax)
+    fresh = api.GpuRobinBoundaryHandler(dim)
+    fresh.build_acceleration_structure(pos, idx, api.IgnoreCandidateSilhouette(False, 0.0), kmin, kmax)
+    rng = np.random.default_rng(12)
+    m = 6000
+    x = rng.uniform(-0.6, 0.6, (m, dim)).astype(np.float32)
+    mn = np.full(m, 1e-3, np.float32)
+    mx = np.where(rng.random(m) < 0.5, A.FLT_MAX, rng.uniform(0.05, 3.0, m)).astype(np.float32)
+    fl = np.zeros(m, np.int32)
+    ru = updated.star_radius(x, mn, mx, 1e-3, fl)
+    rf = fresh.star_radius(x, mn, mx, 1e-3, fl)
+    assert np.array_equal(ru, rf)
+    ob = oracle.Boundary(dim, pos, idx, kind=A.ZGPU_BOUNDARY_ROBIN, kmin=kmin, kmax=kmax, silhouette_precision=0.0,
+                         use_bvh=False)
+    orr = ob.star_radius(x, mn, mx, 1e-3, fl)
+    rel = np.abs(ru - orr) / np.maximum(orr, 1e-30)
+    assert np.median(rel) <= 1e-6
+    assert np.quantile(rel, 0.99) <= 2e-3
+    assert np.mean(rel <= 1e-5) > 0.95
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_line_of_sight_parity(zgpu, oracle, dim):
     pos, idx = _scene(dim)

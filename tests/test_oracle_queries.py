@@ -69,6 +69,39 @@ def test_star_radius_bvh_matches_brute_force(oracle, dim):
         assert np.all(r1 <= np.maximum(maxr, minr)) and np.all(r1 >= minr)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_robin_node_bounds_keep_the_brute_force_radius(oracle, dim):
+    """Robin coefficients that vary per face, with perfectly absorbing (FLT_MAX) and purely
+    reflecting (0) faces mixed in: the node-level bounds of the BVH traversal prune work
+    but give the radius of the all-primitive loop."""
+    if dim == 2:
+        pos, idx = P.star_polygon(2048)
+    else:
+        pos, idx, _ = P.displaced_icosphere(4, seed=5)
+    rng = np.random.default_rng(7)
+    n = idx.shape[0]
+    kmax = rng.uniform(0.5, 6.0, n).astype(np.float32)
+    kmin = (kmax * rng.uniform(0.3, 1.0, n)).astype(np.float32)
+    absorbing = rng.random(n) < 0.05
+    reflecting = rng.random(n) < 0.1
+    kmin[absorbing] = kmax[absorbing] = A.FLT_MAX
+    kmin[reflecting] = kmax[reflecting] = 0.0
+    m = 1500
+    x = rng.uniform(-0.6, 0.6, (m, dim)).astype(np.float32)
+    minr = np.full(m, 1e-3, np.float32)
+    maxr = np.where(rng.random(m) < 0.5, A.FLT_MAX, rng.uniform(0.05, 3.0, m)).astype(np.float32)
+    flip = np.zeros(m, np.int32)
+    b = oracle.Boundary(dim, pos, idx, kind=A.ZGPU_BOUNDARY_ROBIN, kmin=kmin, kmax=kmax, silhouette_precision=0.0)
+    f = oracle.Boundary(dim, pos, idx, kind=A.ZGPU_BOUNDARY_ROBIN, kmin=kmin, kmax=kmax, silhouette_precision=0.0,
+                        use_bvh=False)
+    oracle.counters()
+    r1 = b.star_radius(x, minr, maxr, 1e-3, flip)
+    visited = oracle.counters()["star_radius"]["prims"]
+    r2 = f.star_radius(x, minr, maxr, 1e-3, flip)
+    assert np.array_equal(r1, r2)
+    assert visited < 0.25 * m * n
+
+
 def test_silhouette_flags_convex_and_concave(oracle):
     # a convex square: every vertex is convex -> ignored for single-sided problems
     sq = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)

@@ -3,6 +3,7 @@
 // Host-memory arrays are staged through device scratch owned by the context (the
 // end-to-end path); device-memory arrays are used in place.  Every kernel of a context
 // runs on its stream; entry points return after the stream has drained.
+#include <cfloat>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -269,6 +270,38 @@ int zgpu_boundary_update_robin_coefficients(zgpu_boundary* b, const float* min_r
         else { sil[(size_t)s * 3 + 1].w = min_robin[i]; sil[(size_t)s * 3 + 2].w = max_robin[i]; }
     }
     ZG_CUDA(cudaMemcpy(b->sil, sil.data(), sil.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    // refit the per-child coefficient ranges of the wide nodes (rows 4 and 5 of each node's
+    // cone block), as updateCoefficientValues refits its nodes (reflectance_boundary_bvh/bvh.h:345-367)
+    std::vector<float4> nodes((size_t)b->nNodes * 8), cones((size_t)b->nNodes * 8);
+    ZG_CUDA(cudaMemcpy(nodes.data(), b->nodes, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    ZG_CUDA(cudaMemcpy(cones.data(), b->cones, cones.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    const int D = b->dim;
+    auto range = [&](auto&& self, int c, float& lo, float& hi) -> void {
+        lo = FLT_MAX; hi = 0.0f;
+        if (c == kEmptyChild) return;
+        if (isLeaf(c)) {
+            for (int j = 0; j < leafCount(c); j++) {
+                int i = b->primIndexHost[leafFirst(c) + j];
+                lo = std::min(lo, min_robin[i]);
+                hi = std::max(hi, max_robin[i]);
+            }
+            return;
+        }
+        int4 kids;
+        std::memcpy(&kids, &nodes[(size_t)c * 8 + 2 * D], sizeof(int4));
+        const int k4[4] = {kids.x, kids.y, kids.z, kids.w};
+        float l4[4], h4[4];
+        for (int k = 0; k < 4; k++) {
+            self(self, k4[k], l4[k], h4[k]);
+            lo = std::min(lo, l4[k]);
+            hi = std::max(hi, h4[k]);
+        }
+        cones[(size_t)c * 8 + 4] = make_float4(h4[0], h4[1], h4[2], h4[3]);
+        cones[(size_t)c * 8 + 5] = make_float4(l4[0], l4[1], l4[2], l4[3]);
+    };
+    float lo, hi;
+    range(range, 0, lo, hi);
+    ZG_CUDA(cudaMemcpy(b->cones, cones.data(), cones.size() * sizeof(float4), cudaMemcpyHostToDevice));
     return ZGPU_OK;
 }
 

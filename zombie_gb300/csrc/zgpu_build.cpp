@@ -182,24 +182,29 @@ inline void normal3(const float* a, const float* b, const float* c, float* n) {
 // Normal cone over the silhouette candidates of a binary subtree: every normal of a face
 // adjacent to a non-ignored feature lies within halfAngle of axis.  halfAngle < 0: no
 // candidate in the subtree; halfAngle = pi: a feature with a single face (always a
-// silhouette) or a degenerate axis.
-struct Cone { float axis[3] = {0, 0, 0}; float halfAngle = -1.0f; float kmax = 0.0f; };
+// silhouette) or a degenerate axis.  With allNormals (Robin boundaries) the cone covers
+// every face of the subtree and its neighbours, ignored features included, as the Robin
+// star-radius bounds need the angular range of all normals
+// (reflectance_boundary_bvh/bvh.h:210-262).
+struct Cone { float axis[3] = {0, 0, 0}; float halfAngle = -1.0f; float kmax = 0.0f; float kmin = 0.0f; };
 
 void coneOf(int D, const std::vector<BNode>& bn, int node, const std::vector<int>& order, const std::vector<float>& nrm,
-            const std::vector<int>& adj, const std::vector<int>& flags, const float* kmaxArr, Cone& out) {
+            const std::vector<int>& adj, const std::vector<int>& flags, const float* kmaxArr, const float* kminArr,
+            bool allNormals, Cone& out) {
     std::vector<int> stack = {node};
     std::vector<const float*> normals;
     bool open = false;
-    float kmax = 0.0f;
+    float kmax = 0.0f, kmin = kmaxArr ? kInf : 0.0f;
     while (!stack.empty()) {
         int b = stack.back(); stack.pop_back();
         if (bn[b].count == 0) { stack.push_back(bn[b].left); stack.push_back(bn[b].right); continue; }
         for (int k = 0; k < bn[b].count; k++) {
             int i = order[bn[b].first + k];
             if (kmaxArr) kmax = std::max(kmax, kmaxArr[i]);
-            bool any = false;
+            if (kminArr) kmin = std::min(kmin, kminArr[i]);
+            bool any = allNormals;
             for (int j = 0; j < D; j++) {
-                if (flags[i] & (8 << j)) continue;          // ignored feature
+                if (!allNormals && (flags[i] & (8 << j))) continue;   // ignored feature
                 if (!(flags[i] & (1 << j))) { open = true; continue; }
                 normals.push_back(&nrm[(size_t)adj[(size_t)i * D + j] * D]);
                 any = true;
@@ -209,6 +214,7 @@ void coneOf(int D, const std::vector<BNode>& bn, int node, const std::vector<int
     }
     out = Cone();
     out.kmax = kmax;
+    out.kmin = kmin;
     if (open) { out.halfAngle = 3.14159265f; return; }
     if (normals.empty()) { out.halfAngle = -1.0f; return; }
     double a[3] = {0, 0, 0};
@@ -413,16 +419,19 @@ bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int 
         if (kind != 0) {
             hb.cones.assign(hb.nodes.size(), make_float4(0, 0, 0, -1));
             for (size_t w = 0; w < col.kidsOf.size(); w++) {
-                float km[4] = {0, 0, 0, 0};
+                float km[4] = {0, 0, 0, 0}, kn[4] = {0, 0, 0, 0};
                 for (int c = 0; c < 4; c++) {
                     int b = col.kidsOf[w][c];
                     if (b < 0) continue;
                     Cone cone;
-                    coneOf(D, bld.nodes, b, bld.order, nrm, adj, flags, kind == 2 ? kmax : nullptr, cone);
+                    coneOf(D, bld.nodes, b, bld.order, nrm, adj, flags, kind == 2 ? kmax : nullptr,
+                           kind == 2 ? kmin : nullptr, kind == 2, cone);
                     hb.cones[w * 8 + c] = make_float4(cone.axis[0], cone.axis[1], cone.axis[2], cone.halfAngle);
                     km[c] = cone.kmax;
+                    kn[c] = cone.kmin;
                 }
                 hb.cones[w * 8 + 4] = make_float4(km[0], km[1], km[2], km[3]);
+                hb.cones[w * 8 + 5] = make_float4(kn[0], kn[1], kn[2], kn[3]);
             }
         }
     }
@@ -430,9 +439,10 @@ bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int 
     if (kind != 0 && hb.cones.empty()) {
         // single-leaf scene: an always-visit cone
         hb.cones.assign(8, make_float4(0, 0, 0, 3.14159265f));
-        float km = 0.0f;
-        if (kind == 2 && kmax) for (int i = 0; i < nP; i++) km = std::max(km, kmax[i]);
+        float km = 0.0f, kn = kind == 2 ? kInf : 0.0f;
+        if (kind == 2 && kmax) for (int i = 0; i < nP; i++) { km = std::max(km, kmax[i]); kn = std::min(kn, kmin[i]); }
         hb.cones[4] = make_float4(km, 0, 0, 0);
+        hb.cones[5] = make_float4(kn, 0, 0, 0);
     }
 
     // ---- primitives and silhouette data in leaf order

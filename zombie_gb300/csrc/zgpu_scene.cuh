@@ -580,6 +580,69 @@ ZG_D bool coneMayHoldSilhouette(float4 cone, const WideNode<D>& w, int k, V<D> x
     return !(cosT > sinSpread || cosT < -sinSpread);   // all front-facing or all back-facing
 }
 
+// Angular range of the normals of child k's faces as seen from x: returns false when the
+// range straddles pi/2 (a silhouette is possible); otherwise minAbsCos = |cos| of the range
+// end nearest to pi/2 (reflectance_boundary_bvh/bvh.h:382-392 with FCPW's cone overlap).
+template <int D>
+ZG_D bool coneAngleRange(float4 cone, const WideNode<D>& w, int k, V<D> x, float& minAbsCos) {
+    if (cone.w < 0.0f) { minAbsCos = 1.0f; return true; }      // no silhouette candidate at all
+    if (cone.w >= 1.5707963f) return false;
+    V<D> v;
+    float rb2 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float h = 0.5f * (w.hi[i][k] - w.lo[i][k]);
+        rb2 += h * h;
+        v[i] = x[i] - 0.5f * (w.lo[i][k] + w.hi[i][k]);
+    }
+    float dv2 = len2(v);
+    if (dv2 <= rb2) return false;
+    float inv = rsqrtf(dv2);
+    V<D> a;
+    a[0] = cone.x; a[1] = cone.y;
+    if (D == 3) a[D - 1] = cone.z;
+    float cosT = fminf(fmaxf(dot(a, v) * inv, -1.0f), 1.0f), sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
+    float sB = fminf(sqrtf(rb2) * inv, 1.0f), cB = sqrtf(fmaxf(0.0f, 1.0f - sB * sB));
+    float sA, cA;
+    __sincosf(cone.w, &sA, &cA);
+    float cS = cB * cA - sB * sA, sS = sB * cA + cB * sA;   // cos / sin of spread = beta + halfAngle
+    if (cS <= 0.0f) return false;
+    float cHi = cosT * cS - sinT * sS;                      // cos(theta + spread)
+    float cLo = cosT * cS + sinT * sS;                      // cos(theta - spread)
+    if (cHi > 0.0f) { minAbsCos = cHi; return true; }       // every face front-facing
+    if (cLo < 0.0f) { minAbsCos = -cLo; return true; }      // every face back-facing
+    return false;
+}
+
+// node bounds on the squared star radius of every primitive below a node without
+// silhouettes (reflectance_boundary_bvh/robin_bounds.h:110-154), maxAbsCos = 1
+ZG_D void robinNodeBounds(int D, float rMin, float rMax, float kmin, float kmax, float minCos, float& r2Min, float& r2Max) {
+    if (D == 2) {
+        float lo = rMin * expf(minCos / (kmax * rMax));
+        float hi = rMax * expf(1.0f / (kmin * rMin));
+        r2Min = lo * lo;
+        r2Max = hi * hi;
+    } else {
+        if (rMax < minCos / kmax) r2Min = kFltMax;
+        else { float lo = rMin / (1.0f - minCos / (kmax * rMax)); r2Min = lo * lo; }
+        if (rMin < 1.0f / kmin) r2Max = kFltMax;
+        else { float hi = rMax / (1.0f - 1.0f / (kmin * rMin)); r2Max = hi * hi; }
+    }
+    if (!(r2Min == r2Min)) r2Min = 0.0f;     // NaN -> no pruning
+    if (!(r2Max == r2Max)) r2Max = kFltMax;
+}
+
+template <int D>
+ZG_D float boxMaxDist2(const WideNode<D>& w, int k, V<D> x) {
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float d = fmaxf(fabsf(x[i] - w.lo[i][k]), fabsf(x[i] - w.hi[i][k]));
+        s += d * d;
+    }
+    return s;
+}
+
 // computeStarRadiusForReflectingBoundary: max(sqrt(min(maxR^2, silhouettes, Robin bounds)), minR)
 // one silhouette-candidate record: 2D vertex (v, nPrev, nNext), 3D edge (a, b, nA, nB)
 ZG_D void featureRadius(const BoundaryView& b, int slot, V<2> x, float& r2, bool flip, float prec) {
@@ -667,19 +730,38 @@ __device__ __noinline__ float starRadius(const BoundaryView& b, V<D> x, float mi
             WideNode<D> w;
             loadNode<D>(b, node, w);
             float4 km = b.cones ? __ldg(b.cones + (size_t)node * 8 + 4) : make_float4(kFltMax, kFltMax, kFltMax, kFltMax);
+            float4 kn = b.cones ? __ldg(b.cones + (size_t)node * 8 + 5) : make_float4(0, 0, 0, 0);
             const float kmaxChild[4] = {km.x, km.y, km.z, km.w};
+            const float kminChild[4] = {kn.x, kn.y, kn.z, kn.w};
             ChildOrder ord; ord.clear();
             unsigned leaves = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 int c = w.child[k];
                 float d2 = boxDist2<D>(w, k, x);
+                float key = d2;
                 bool ok = c != kEmptyChild && d2 <= r2;
-                // subtrees without Robin reflectance only matter through their silhouettes
-                if (ok && kmaxChild[k] <= kReflEps)
-                    ok = coneMayHoldSilhouette<D>(__ldg(b.cones + (size_t)node * 8 + k), w, k, x, prec);
+                if (ok && kminChild[k] >= kFltMax - kReflEps) {
+                    // perfectly absorbing subtree: the farthest box point bounds the radius
+                    r2 = fminf(r2, boxMaxDist2<D>(w, k, x));
+                } else if (ok) {
+                    float minCos;
+                    if (coneAngleRange<D>(__ldg(b.cones + (size_t)node * 8 + k), w, k, x, minCos)) {
+                        // no silhouette below: pure reflection contributes nothing, reflectance is bounded
+                        if (kmaxChild[k] <= kReflEps) {
+                            ok = false;
+                        } else {
+                            float r2Min, r2Max;
+                            robinNodeBounds(D, sqrtf(d2), sqrtf(boxMaxDist2<D>(w, k, x)), kminChild[k], kmaxChild[k],
+                                            minCos, r2Min, r2Max);
+                            key = fmaxf(d2, r2Min);
+                            ok = key <= r2;
+                            if (ok) r2 = fminf(r2, r2Max);
+                        }
+                    }
+                }
                 if (ok && isLeaf(c)) leaves |= 1u << k;
-                if (ok && !isLeaf(c)) { ord.k[k] = d2; ord.c[k] = c; }
+                if (ok && !isLeaf(c)) { ord.k[k] = key; ord.c[k] = c; }
             }
             while (leaves) {
                 int k = __ffs(leaves) - 1;
