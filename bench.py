@@ -36,6 +36,12 @@ WORKLOADS = {
                            desc="2D Laplace WoS, 1024 segments, 128x128 grid, 256 spp"),
     "robin_wost_3d": dict(fn="robin_wost_3d", kw=dict(level=6, n_points=1_000_000, spp=128),
                           desc="3D Robin WoSt, icosphere L6 (81,920 tris), 1M points, 128 spp, kappa=2"),
+    "robin_wost_3d_small": dict(fn="robin_wost_3d", kw=dict(level=6, n_points=4096, spp=16),
+                                desc="profiling case: 3D Robin WoSt, icosphere L6, 4096 points, 16 spp, kappa=2"),
+    "screened_wos_3d": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=4_000_000, spp=64),
+                            desc="3D screened Poisson WoS sigma=4, icosphere L8 (1,310,720 tris), 4M points, 64 spp"),
+    "screened_wos_3d_small": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=16384, spp=4),
+                                  desc="profiling case: 3D screened WoS sigma=4, icosphere L8, 16384 points, 4 spp"),
 }
 
 # algorithmic bytes per traversal unit under the oracle's binary SAH BVH (leaf 4):

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define ZGPU_ABI_VERSION 1
+#define ZGPU_ABI_VERSION 2
 
 /* ------------------------------------------------------------------------- */
 /* status codes                                                               */
@@ -184,6 +184,7 @@ typedef struct zgpu_solve_report {
     float kernel_ms;           /* CUDA-event time of the walk kernel */
     float total_ms;            /* CUDA-event time of prepare + walk + finalize */
     uint32_t error_word;       /* nonzero: device-side internal error (stack overflow, budget) */
+    uint64_t cache_terminated; /* walks ended through the neural cache (zgpu_solve_cached) */
 } zgpu_solve_report;
 
 typedef struct zgpu_context zgpu_context;
@@ -317,6 +318,68 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
 int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_queries* queries, const zgpu_pde* pde,
                       const zgpu_walk_settings* settings, const zgpu_sample_points* points,
                       zgpu_sample_statistics* stats, zgpu_solve_report* report);
+
+/* ------------------------------ neural cache ------------------------------ */
+/*
+ * A learned cache of the solution: a multiresolution hash-grid encoding (n_levels levels of
+ * 2 FP16 features, 2^log2_table_size entries per level, resolutions growing geometrically
+ * from base_resolution to max_resolution over the domain box) feeding a 32-64-64-1 ReLU MLP
+ * with BF16 weights evaluated on the tensor cores (FP32 accumulation).  No counterpart in
+ * the reference.  It is trained online on walk estimates (zgpu_cache_train, Adam on the
+ * mean squared error), and zgpu_solve_cached ends a walk at its first position after the
+ * first step that lies at least min_distance from the boundary, paying
+ * throughput * cache(x) there.  The plain walk (zgpu_solve) stays the fallback.
+ */
+typedef struct zgpu_cache zgpu_cache;
+
+typedef struct zgpu_cache_config {
+    int32_t dim;                 /* 2 or 3 */
+    int32_t n_levels;            /* 1..16 (encoding width 32; unused levels encode 0) */
+    int32_t log2_table_size;     /* 8..24 */
+    float base_resolution;       /* coarsest grid resolution (>= 1) */
+    float max_resolution;        /* finest grid resolution */
+    float domain_min[3];         /* box mapped to [0,1]^dim before encoding */
+    float domain_max[3];
+    float learning_rate_grid;    /* Adam step of the table */
+    float learning_rate_mlp;     /* Adam step of the network */
+    float beta1, beta2, epsilon; /* Adam moments */
+    uint64_t seed;               /* initialisation */
+} zgpu_cache_config;
+
+int zgpu_cache_create(zgpu_context* ctx, const zgpu_cache_config* config, zgpu_cache** out);
+int zgpu_cache_destroy(zgpu_cache* cache);
+/* offsets[8] into the flat FP32 parameter vector: table [levels][T][2], W1 [64][32], b1 [64],
+ * W2 [64][64], b2 [64], w3 [64], b3, total */
+int zgpu_cache_layout(const zgpu_cache* cache, int64_t* offsets);
+/* the integer resolution of each level (n_levels floats) */
+int zgpu_cache_resolutions(const zgpu_cache* cache, float* res);
+int zgpu_cache_get_parameters(zgpu_cache* cache, float* out_params);
+int zgpu_cache_set_parameters(zgpu_cache* cache, const float* params);
+/* `steps` Adam steps on batches of batch_size consecutive (wrapping) points of the training
+ * set (pass it in random order); mean_loss (may be NULL) = mean squared error over them */
+int zgpu_cache_train(zgpu_cache* cache, int64_t n, const float* x, const float* target, int memory,
+                     int32_t steps, int32_t batch_size, float* mean_loss);
+/* gradient of the mean squared error over all n points (no update); grads laid out as the
+ * parameters */
+int zgpu_cache_gradients(zgpu_cache* cache, int64_t n, const float* x, const float* target, int memory,
+                         float* grads, double* loss);
+int zgpu_cache_evaluate(zgpu_cache* cache, int64_t n, const float* x, float* y, int memory);
+/* the FP32 hash-grid encoding of each point, enc [n][32] (for inspection and tests) */
+int zgpu_cache_encode(zgpu_cache* cache, int64_t n, const float* x, float* enc, int memory);
+
+/*
+ * zgpu_solve with early walk termination through the cache: once a walk has taken a step and
+ * its position lies at least min_distance from the absorbing boundary (and, for Walk on
+ * Stars, from the reflecting boundary, off it), the walk ends and its estimate is the
+ * contributions gathered so far plus throughput * cache(x).  Walk splitting is not supported
+ * (splitting_threshold must be FLT_MAX).  report->rr_terminated etc. count as in zgpu_solve;
+ * cache-terminated walks are reported in report->total_walks like the others.
+ */
+int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries,
+                      const zgpu_pde* pde, const zgpu_walk_settings* settings,
+                      const zgpu_sample_points* points, zgpu_sample_statistics* stats,
+                      const zgpu_solve_options* options, zgpu_cache* cache, float min_distance,
+                      zgpu_solve_report* report);
 
 #ifdef __cplusplus
 }

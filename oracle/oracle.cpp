@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cstdio>
 #include "oracle_walk.h"
+#include "oracle_cache.h"
 
 using namespace orc;
 
@@ -321,3 +322,71 @@ extern "C" int orc_solve(int solver, const zgpu_geometric_queries* q, const zgpu
     return 0;
 }
 
+
+// ---------------------------------------------------------------- neural cache oracle
+// Parameters arrive as float arrays (the GPU's FP16 table and BF16 weights widened to FP32);
+// res = per-level resolutions, lo / inv = domain normalisation.
+static CacheModel makeCacheModel(int dim, int levels, int log2T, const float* res, const float* lo, const float* inv,
+                                 const float* table, const float* W1, const float* b1, const float* W2,
+                                 const float* b2, const float* w3, float b3) {
+    CacheModel m;
+    m.dim = dim; m.levels = levels; m.log2T = log2T;
+    m.res.assign(res, res + levels);
+    for (int i = 0; i < dim; i++) { m.lo[i] = lo[i]; m.inv[i] = inv[i]; }
+    const size_t T = (size_t)1 << log2T, I = (size_t)2 * levels, H = kCacheHidden;
+    m.table.assign(table, table + (size_t)levels * T * 2);
+    m.W1.assign(W1, W1 + H * I); m.b1.assign(b1, b1 + H);
+    m.W2.assign(W2, W2 + H * H); m.b2.assign(b2, b2 + H);
+    m.w3.assign(w3, w3 + H); m.b3 = b3;
+    return m;
+}
+
+extern "C" void orc_cache_forward(int dim, int levels, int log2T, const float* res, const float* lo, const float* inv,
+                                  const float* table, const float* W1, const float* b1, const float* W2,
+                                  const float* b2, const float* w3, float b3, int64_t n, const float* x,
+                                  double* y, double* enc) {
+    CacheModel m = makeCacheModel(dim, levels, log2T, res, lo, inv, table, W1, b1, W2, b2, w3, b3);
+    CacheActivations a;
+    for (int64_t i = 0; i < n; i++) {
+        y[i] = cacheForward(m, x + i * dim, a);
+        if (enc) for (int k = 0; k < 2 * levels; k++) enc[i * 2 * levels + k] = a.e[k];
+    }
+}
+
+// corner indices of every level for each point: out[n][levels][2^dim]
+extern "C" void orc_cache_corners(int dim, int levels, int log2T, const float* res, const float* lo, const float* inv,
+                                  int64_t n, const float* x, uint32_t* idx, double* w) {
+    CacheModel m;
+    m.dim = dim; m.levels = levels; m.log2T = log2T;
+    m.res.assign(res, res + levels);
+    for (int i = 0; i < dim; i++) { m.lo[i] = lo[i]; m.inv[i] = inv[i]; }
+    CacheCorner cs[8];
+    const int C = 1 << dim;
+    for (int64_t i = 0; i < n; i++)
+        for (int l = 0; l < levels; l++) {
+            cacheCorners(m, l, x + i * dim, cs);
+            for (int k = 0; k < C; k++) {
+                idx[(i * levels + l) * C + k] = cs[k].index;
+                if (w) w[(i * levels + l) * C + k] = cs[k].weight;
+            }
+        }
+}
+
+// mean squared error and its gradient; outputs laid out like the parameters (double)
+extern "C" double orc_cache_grads(int dim, int levels, int log2T, const float* res, const float* lo, const float* inv,
+                                  const float* table, const float* W1, const float* b1, const float* W2,
+                                  const float* b2, const float* w3, float b3, int n, const float* x,
+                                  const float* target, double* gTable, double* gW1, double* gb1, double* gW2,
+                                  double* gb2, double* gw3, double* gb3) {
+    CacheModel m = makeCacheModel(dim, levels, log2T, res, lo, inv, table, W1, b1, W2, b2, w3, b3);
+    CacheGrads g;
+    double loss = cacheLossAndGrads(m, n, x, target, g);
+    std::copy(g.table.begin(), g.table.end(), gTable);
+    std::copy(g.W1.begin(), g.W1.end(), gW1);
+    std::copy(g.b1.begin(), g.b1.end(), gb1);
+    std::copy(g.W2.begin(), g.W2.end(), gW2);
+    std::copy(g.b2.begin(), g.b2.end(), gb2);
+    std::copy(g.w3.begin(), g.w3.end(), gw3);
+    *gb3 = g.b3;
+    return loss;
+}

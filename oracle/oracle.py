@@ -16,7 +16,7 @@ from zombie_gb300 import _abi as A
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = ["oracle.cpp", "oracle_core.h", "oracle_geometry.h", "oracle_walk.h"]
+SOURCES = ["oracle.cpp", "oracle_core.h", "oracle_geometry.h", "oracle_walk.h", "oracle_cache.h"]
 
 
 def build(force=False):
@@ -69,6 +69,11 @@ def lib():
         L.orc_solve.argtypes = [i32, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_uint64)]
         L.orc_hardware_threads.restype = i32
         L.orc_counters.argtypes = [vp]
+        L.orc_cache_forward.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, f32, i64, vp, vp, vp]
+        L.orc_cache_corners.argtypes = [i32, i32, i32, vp, vp, vp, i64, vp, vp, vp]
+        L.orc_cache_grads.restype = C.c_double
+        L.orc_cache_grads.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, f32, i32, vp, vp,
+                                      vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -218,3 +223,49 @@ def solve(solver, dim, absorbing, reflecting, domain_min, domain_max, pde, setti
     lib().orc_solve(solver, C.byref(q), C.byref(pde), C.byref(settings), C.byref(sp), C.byref(st),
                     int(n_threads), C.byref(steps))
     return int(steps.value)
+
+
+class CacheModel:
+    """The neural cache's definition (oracle_cache.h) with parameters given as numpy arrays:
+    table [levels, T, 2], W1 [64, 2L], b1 [64], W2 [64, 64], b2 [64], w3 [64], b3 scalar."""
+
+    def __init__(self, dim, res, lo, inv, table, W1, b1, W2, b2, w3, b3):
+        self.dim = dim
+        self.res = _f32(res)
+        self.levels = len(self.res)
+        self.table = _f32(table).reshape(self.levels, -1, 2)
+        self.log2T = int(np.log2(self.table.shape[1]))
+        self.lo = _f32(np.resize(lo, 3))
+        self.inv = _f32(np.resize(inv, 3))
+        self.W1, self.b1, self.W2, self.b2, self.w3 = (_f32(a) for a in (W1, b1, W2, b2, w3))
+        self.b3 = float(b3)
+
+    def _args(self):
+        return (self.dim, self.levels, self.log2T, A.ptr(self.res), A.ptr(self.lo), A.ptr(self.inv),
+                A.ptr(self.table), A.ptr(self.W1), A.ptr(self.b1), A.ptr(self.W2), A.ptr(self.b2),
+                A.ptr(self.w3), self.b3)
+
+    def forward(self, x, with_encoding=False):
+        x = _f32(x).reshape(-1, self.dim)
+        y = np.zeros(x.shape[0])
+        enc = np.zeros((x.shape[0], 2 * self.levels)) if with_encoding else None
+        lib().orc_cache_forward(*self._args(), x.shape[0], A.ptr(x), A.ptr(y), A.ptr(enc))
+        return (y, enc) if with_encoding else y
+
+    def corners(self, x):
+        x = _f32(x).reshape(-1, self.dim)
+        C_ = 1 << self.dim
+        idx = np.zeros((x.shape[0], self.levels, C_), np.uint32)
+        w = np.zeros((x.shape[0], self.levels, C_))
+        lib().orc_cache_corners(self.dim, self.levels, self.log2T, A.ptr(self.res), A.ptr(self.lo), A.ptr(self.inv),
+                                x.shape[0], A.ptr(x), A.ptr(idx), A.ptr(w))
+        return idx, w
+
+    def loss_and_grads(self, x, target):
+        x = _f32(x).reshape(-1, self.dim)
+        t = _f32(target)
+        g = dict(table=np.zeros(self.table.shape), W1=np.zeros(self.W1.shape), b1=np.zeros(64),
+                 W2=np.zeros(self.W2.shape), b2=np.zeros(64), w3=np.zeros(64), b3=np.zeros(1))
+        loss = lib().orc_cache_grads(*self._args(), x.shape[0], A.ptr(x), A.ptr(t), A.ptr(g["table"]), A.ptr(g["W1"]),
+                                     A.ptr(g["b1"]), A.ptr(g["W2"]), A.ptr(g["b2"]), A.ptr(g["w3"]), A.ptr(g["b3"]))
+        return loss, g

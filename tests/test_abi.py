@@ -15,7 +15,7 @@ STRUCTS = {
     "zgpu_analytic": A.Analytic, "zgpu_grid": A.Grid, "zgpu_pde": A.Pde, "zgpu_walk_settings": A.WalkSettingsC,
     "zgpu_sample_points": A.SamplePointsC, "zgpu_sample_statistics": A.SampleStatisticsC,
     "zgpu_solve_options": A.SolveOptions, "zgpu_solve_report": A.SolveReport,
-    "zgpu_geometric_queries": A.GeometricQueriesC,
+    "zgpu_geometric_queries": A.GeometricQueriesC, "zgpu_cache_config": A.CacheConfig,
 }
 
 

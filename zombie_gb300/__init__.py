@@ -10,7 +10,7 @@ import types as _types
 from . import _abi
 from .api import (BranchTraversalWeight, Context, EstimationQuantity, Field, GeometricQueries,
                   GpuDirichletBoundaryHandler, GpuNeumannBoundaryHandler, GpuRobinBoundaryHandler,
-                  IgnoreCandidateSilhouette, PDE, SampleArrays, SamplePoint, SampleStatistics, SampleType,
+                  IgnoreCandidateSilhouette, NeuralCache, PDE, SampleArrays, SamplePoint, SampleStatistics, SampleType,
                   WalkCompletionCode, WalkOnSpheres, WalkOnStars, WalkSettings, create_sample_statistics_list,
                   default_context, populate_geometric_queries_for_dirichlet_boundary,
                   populate_geometric_queries_for_neumann_boundary, populate_geometric_queries_for_robin_boundary)
@@ -59,6 +59,7 @@ Solvers = _types.SimpleNamespace(
     create_sample_statistics_list=lambda size, dim=None, channels=1: create_sample_statistics_list(size),
     WalkOnSpheres=_solver_factory(WalkOnSpheres),
     WalkOnStars=_solver_factory(WalkOnStars),
+    NeuralCache=NeuralCache,
 )
 
 Utils = _types.SimpleNamespace(

@@ -5,7 +5,7 @@ offsets against the compiled library.
 """
 import ctypes as C
 
-ZGPU_ABI_VERSION = 1
+ZGPU_ABI_VERSION = 2
 
 ZGPU_OK = 0
 ZGPU_ERR_INVALID_ARG = 1
@@ -164,6 +164,7 @@ class SolveReport(C.Structure):
         ("kernel_ms", C.c_float),
         ("total_ms", C.c_float),
         ("error_word", C.c_uint32),
+        ("cache_terminated", C.c_uint64),
     ]
 
 
@@ -185,3 +186,21 @@ def ptr(a):
     if hasattr(a, "data_ptr"):
         return a.data_ptr()
     return a.ctypes.data
+
+
+class CacheConfig(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("n_levels", C.c_int32),
+        ("log2_table_size", C.c_int32),
+        ("base_resolution", C.c_float),
+        ("max_resolution", C.c_float),
+        ("domain_min", C.c_float * 3),
+        ("domain_max", C.c_float * 3),
+        ("learning_rate_grid", C.c_float),
+        ("learning_rate_mlp", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("epsilon", C.c_float),
+        ("seed", C.c_uint64),
+    ]

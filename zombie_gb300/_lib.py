@@ -51,6 +51,17 @@ def lib():
         L.zgpu_solve.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.zgpu_solve_batched.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp]
         L.zgpu_solve_static.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp]
+        L.zgpu_cache_create.argtypes = [vp, vp, pp]
+        L.zgpu_cache_destroy.argtypes = [vp]
+        L.zgpu_cache_layout.argtypes = [vp, vp]
+        L.zgpu_cache_resolutions.argtypes = [vp, vp]
+        L.zgpu_cache_get_parameters.argtypes = [vp, vp]
+        L.zgpu_cache_set_parameters.argtypes = [vp, vp]
+        L.zgpu_cache_train.argtypes = [vp, i64, vp, vp, i32, i32, i32, C.POINTER(C.c_float)]
+        L.zgpu_cache_gradients.argtypes = [vp, i64, vp, vp, i32, vp, C.POINTER(C.c_double)]
+        L.zgpu_cache_evaluate.argtypes = [vp, i64, vp, vp, i32]
+        L.zgpu_cache_encode.argtypes = [vp, i64, vp, vp, i32]
+        L.zgpu_solve_cached.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp]
         if L.zgpu_abi_version() != A.ZGPU_ABI_VERSION:
             raise ZgpuError(A.ZGPU_ERR_INVALID_ARG, "ABI version mismatch between libzgpu.so and zombie_gb300")
         _lib = L

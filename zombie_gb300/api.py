@@ -591,6 +591,7 @@ class SolveReport:
         self.kernel_ms = r.kernel_ms
         self.total_ms = r.total_ms
         self.error_word = r.error_word
+        self.cache_terminated = r.cache_terminated
 
 
 class _Solver:
@@ -608,16 +609,23 @@ class _Solver:
         self.options = options
         self.last_report = None
 
-    def solve_arrays(self, pde, walk_settings, arrays, options=None):
-        """Fast path: structure-of-arrays points/statistics (host numpy or CUDA tensors)."""
+    def solve_arrays(self, pde, walk_settings, arrays, options=None, cache=None, cache_min_distance=0.05):
+        """Fast path: structure-of-arrays points/statistics (host numpy or CUDA tensors).
+        With `cache` (a NeuralCache) walks end early through it (zgpu_solve_cached)."""
         q = self.queries.to_c()
         p = pde.to_c() if isinstance(pde, PDE) else pde
         ws = walk_settings.to_c() if isinstance(walk_settings, WalkSettings) else walk_settings
         sp, st = arrays.to_c()
         opt = options or self.options
         rep = A.SolveReport()
-        check(lib().zgpu_solve(self.ctx.h, self.solver_id, C.byref(q), C.byref(p), C.byref(ws), C.byref(sp),
-                               C.byref(st), C.byref(opt) if opt is not None else None, C.byref(rep)))
+        optp = C.byref(opt) if opt is not None else None
+        if cache is None:
+            check(lib().zgpu_solve(self.ctx.h, self.solver_id, C.byref(q), C.byref(p), C.byref(ws), C.byref(sp),
+                                   C.byref(st), optp, C.byref(rep)))
+        else:
+            check(lib().zgpu_solve_cached(self.ctx.h, self.solver_id, C.byref(q), C.byref(p), C.byref(ws),
+                                          C.byref(sp), C.byref(st), optp, cache.h, float(cache_min_distance),
+                                          C.byref(rep)))
         self.last_report = SolveReport(rep)
         return self.last_report
 
@@ -678,3 +686,124 @@ class WalkOnSpheres(_Solver):
 class WalkOnStars(_Solver):
     """WalkOnStars<T,DIM> (point_estimation/walk_on_stars.h:22-... )."""
     solver_id = A.ZGPU_SOLVER_WALK_ON_STARS
+
+
+# ----------------------------------------------------------------- neural cache
+class NeuralCache:
+    """Hash-grid + MLP cache of the solution, trained on the GPU (zgpu_cache_*).  No
+    counterpart in the reference.  Parameters live on the device; x / targets may be numpy
+    arrays (host) or CUDA tensors (device)."""
+
+    PARAM_NAMES = ("table", "W1", "b1", "W2", "b2", "w3", "b3")
+
+    def __init__(self, dim, domain_min, domain_max, n_levels=16, log2_table_size=19, base_resolution=4.0,
+                 max_resolution=None, learning_rate_grid=1e-2, learning_rate_mlp=1e-3, beta1=0.9, beta2=0.99,
+                 epsilon=1e-15, seed=0, padding=0.02, context=None):
+        _validate(dim)
+        self.ctx = context or default_context()
+        self.dim = dim
+        lo = np.asarray(domain_min, np.float64)[:dim]
+        hi = np.asarray(domain_max, np.float64)[:dim]
+        pad = padding * (hi - lo)
+        cfg = A.CacheConfig()
+        cfg.dim = dim
+        cfg.n_levels = n_levels
+        cfg.log2_table_size = log2_table_size
+        cfg.base_resolution = base_resolution
+        # the solution of an elliptic problem is smooth: a coarse finest level keeps many
+        # training estimates per cell, which averages their noise instead of memorising it
+        cfg.max_resolution = max_resolution if max_resolution is not None else (64.0 if dim == 3 else 128.0)
+        for i in range(dim):
+            cfg.domain_min[i] = lo[i] - pad[i]
+            cfg.domain_max[i] = hi[i] + pad[i]
+        cfg.learning_rate_grid = learning_rate_grid
+        cfg.learning_rate_mlp = learning_rate_mlp
+        cfg.beta1, cfg.beta2, cfg.epsilon = beta1, beta2, epsilon
+        cfg.seed = seed
+        self.config = cfg
+        h = C.c_void_p()
+        check(lib().zgpu_cache_create(self.ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        off = np.zeros(8, np.int64)
+        check(lib().zgpu_cache_layout(self.h, A.ptr(off)))
+        self.offsets = off
+        res = np.zeros(n_levels, np.float32)
+        check(lib().zgpu_cache_resolutions(self.h, A.ptr(res)))
+        self.resolutions = res
+
+    @property
+    def n_parameters(self):
+        return int(self.offsets[7])
+
+    def _mem(self, a):
+        return A.ZGPU_MEM_DEVICE if hasattr(a, "is_cuda") and a.is_cuda else A.ZGPU_MEM_HOST
+
+    def _prep(self, a, dtype=np.float32):
+        if hasattr(a, "is_cuda") and a.is_cuda:
+            return a.contiguous()
+        return np.ascontiguousarray(a, dtype)
+
+    def train(self, x, target, steps, batch_size=1 << 16):
+        """`steps` Adam steps on consecutive batches of the training set (random order expected);
+        returns the mean squared error over those batches."""
+        x, t = self._prep(x), self._prep(target)
+        loss = C.c_float()
+        check(lib().zgpu_cache_train(self.h, int(t.shape[0]), A.ptr(x), A.ptr(t), self._mem(x), int(steps),
+                                     int(batch_size), C.byref(loss)))
+        return loss.value
+
+    def evaluate(self, x):
+        x = self._prep(x)
+        n = int(x.shape[0])
+        if self._mem(x) == A.ZGPU_MEM_DEVICE:
+            import torch
+            y = torch.empty(n, dtype=torch.float32, device=x.device)
+        else:
+            y = np.zeros(n, np.float32)
+        check(lib().zgpu_cache_evaluate(self.h, n, A.ptr(x), A.ptr(y), self._mem(x)))
+        return y
+
+    def encode(self, x):
+        """FP32 hash-grid encoding [n, 32] (host arrays)."""
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.dim)
+        enc = np.zeros((x.shape[0], 32), np.float32)
+        check(lib().zgpu_cache_encode(self.h, x.shape[0], A.ptr(x), A.ptr(enc), A.ZGPU_MEM_HOST))
+        return enc
+
+    def gradients(self, x, target):
+        """Gradient of the mean squared error over all points (no update): (loss, flat grads)."""
+        x, t = self._prep(x), self._prep(target)
+        g = np.zeros(self.n_parameters, np.float32)
+        loss = C.c_double()
+        check(lib().zgpu_cache_gradients(self.h, int(t.shape[0]), A.ptr(x), A.ptr(t), self._mem(x), A.ptr(g),
+                                         C.byref(loss)))
+        return loss.value, g
+
+    def get_parameters(self):
+        p = np.zeros(self.n_parameters, np.float32)
+        check(lib().zgpu_cache_get_parameters(self.h, A.ptr(p)))
+        return p
+
+    def set_parameters(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.shape[0] == self.n_parameters
+        check(lib().zgpu_cache_set_parameters(self.h, A.ptr(p)))
+
+    def split(self, flat):
+        """Views of a flat parameter (or gradient) vector by name."""
+        o = self.offsets
+        L = self.config.n_levels
+        return dict(table=flat[o[0]:o[1]].reshape(L, -1, 2), W1=flat[o[1]:o[2]].reshape(64, 32),
+                    b1=flat[o[2]:o[3]], W2=flat[o[3]:o[4]].reshape(64, 64), b2=flat[o[4]:o[5]],
+                    w3=flat[o[5]:o[6]], b3=flat[o[6]:o[7]])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().zgpu_cache_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -65,7 +65,7 @@ struct zgpu_context {
     // scratch (indexed by role)
     enum { kPt, kNormal, kType, kEq, kDist, kNWalks, kSeed, kFsr, kAligned, kMean, kM2, kN, kLen, kSplits,
            kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
-           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kNumBufs };
+           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
 };
@@ -138,9 +138,10 @@ int checkField(int kind, const char* name) {
 
 }  // namespace
 
-// internal accessors used by the allocation-free entry point (zgpu_static.cu)
+// internal accessors used by the allocation-free entry point (zgpu_static.cu) and the cache
 namespace zg {
 void setLastError(const char* msg) { gLastError = msg; }
+int contextDevice(const zgpu_context* ctx) { return ctx->device; }
 bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind) {
     if (!b) return false;
     *view = b->view; *dim = b->dim; *kind = b->kind;
@@ -474,9 +475,14 @@ int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, cons
 }
 
 // -------------------------------------------------------------------------- solve
-int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
-               const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
-               const zgpu_solve_options* opt, zgpu_solve_report* report) {
+}  // extern "C"
+
+namespace {
+
+// zgpu_solve and zgpu_solve_cached: cache == NULL runs the plain walk
+int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+              const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
+              const zgpu_solve_options* opt, zgpu_cache* cache, float cacheMinDist, zgpu_solve_report* report) {
     if (!ctx || !q || !pde || !ws || !pts || !stats) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
     if (solver != ZGPU_SOLVER_WALK_ON_SPHERES && solver != ZGPU_SOLVER_WALK_ON_STARS)
         return fail(ZGPU_ERR_INVALID_ARG, "unknown solver %d", solver);
@@ -571,8 +577,20 @@ int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, c
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
     ZG_CUDA(launchPrepare(P, D, s));
     ZG_CUDA(launchScan(P.walkStart, n, blockSums, s));
+    if (cache) {
+        // one record per walk at most (no splitting): size the buffer by the walk count
+        long long totalWalks = 0;
+        ZG_CUDA(cudaMemcpyAsync(&totalWalks, P.walkStart + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        ZG_CUDA(cudaStreamSynchronize(s));
+        P.cacheCap = std::max(1LL, totalWalks);
+        ZG_TRY(scratch<float4>(ctx, C::kCacheRec, (size_t)P.cacheCap * 2, &P.cacheRec));
+        P.cacheMinDist = cacheMinDist;
+    }
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (n > 0) ZG_CUDA(launchWalk(P, D, blocks, threads, s));
+    if (cache && n > 0)
+        ZG_CUDA(launchCacheAccumulate(cache, P.cacheRec, P.counters + kCtrCache, P.cacheCap, P.accSum, P.accSq,
+                                      P.accN, P.accLen, s));
     ZG_CUDA(cudaEventRecord(ctx->ev[2], s));
     ZG_CUDA(launchFinalize(P, D, s));
     ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
@@ -594,12 +612,38 @@ int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, c
         report->rr_terminated = ctx->hostCounters[kCtrRR];
         report->total_walks = ctx->hostCounters[12];
         report->error_word = errWord;
+        report->cache_terminated = cache ? std::min<unsigned long long>(ctx->hostCounters[kCtrCache], P.cacheCap) : 0;
         cudaEventElapsedTime(&report->kernel_ms, ctx->ev[1], ctx->ev[2]);
         cudaEventElapsedTime(&report->total_ms, ctx->ev[0], ctx->ev[3]);
     }
     if (errWord)
-        return fail(ZGPU_ERR_DEVICE_STATE, "device error word 0x%x (1: traversal stack, 2: split stack overflow)", errWord);
+        return fail(ZGPU_ERR_DEVICE_STATE,
+                    "device error word 0x%x (1: traversal stack, 2: split stack, 16: cache record overflow)", errWord);
     return ZGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+               const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
+               const zgpu_solve_options* opt, zgpu_solve_report* report) {
+    return solveImpl(ctx, solver, q, pde, ws, pts, stats, opt, nullptr, 0.0f, report);
+}
+
+int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+                      const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
+                      const zgpu_solve_options* opt, zgpu_cache* cache, float min_distance, zgpu_solve_report* report) {
+    if (!cache) return fail(ZGPU_ERR_INVALID_ARG, "cache is NULL (use zgpu_solve for the plain walk)");
+    if (!ctx || !q || !ws) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (cacheDim(cache) != q->dim) return fail(ZGPU_ERR_INVALID_ARG, "cache dim %d does not match queries dim %d",
+                                              cacheDim(cache), q->dim);
+    if (!(min_distance > 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "min_distance must be > 0");
+    if (ws->splitting_threshold < FLT_MAX)
+        return fail(ZGPU_ERR_UNSUPPORTED, "walk splitting is not supported with the cache (splitting_threshold must be FLT_MAX)");
+    if (cacheStream(cache) != ctx->stream) return fail(ZGPU_ERR_INVALID_ARG, "cache belongs to another context");
+    return solveImpl(ctx, solver, q, pde, ws, pts, stats, opt, cache, min_distance, report);
 }
 
 int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_geometric_queries* queries,

@@ -11,7 +11,8 @@ namespace zg {
 enum : int { kReached = 0, kRussianRoulette = 1, kExceeded = 2, kEscaped = 3 };
 
 // counters[] slots
-enum : int { kCtrNext = 0, kCtrSteps = 1, kCtrEscaped = 2, kCtrExceeded = 3, kCtrRR = 4, kCtrWalks = 5, kCtrCount = 8 };
+enum : int { kCtrNext = 0, kCtrSteps = 1, kCtrEscaped = 2, kCtrExceeded = 3, kCtrRR = 4, kCtrWalks = 5, kCtrCache = 6,
+             kCtrCount = 8 };
 
 // per-point flags written by the prepare kernel
 enum : int { kPointBoundaryValue = 1, kPointFlip = 2 };
@@ -54,6 +55,12 @@ struct SolveParams {
     unsigned int* errorWord;
     float4* splitStack;         // walk threads x kSplitStack x 3 float4
     int stackEntries;           // shared-memory traversal stack entries per thread
+    // neural cache: walks end at their first position after a step that lies at least
+    // cacheMinDist from the boundary (0 = off) and leave a record (2 float4: position and
+    // throughput; partial estimate, point, walk length) for the cache pass
+    float cacheMinDist;
+    float4* cacheRec;
+    long long cacheCap;
 };
 
 constexpr int kSplitStack = 8;
@@ -64,6 +71,13 @@ cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStr
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
 int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, int stackEntries);
+// neural cache pass over the walk records (zgpu_cache.cu)
+cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
+                                  int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,
+                                  cudaStream_t s);
+int cacheDim(const zgpu_cache* c);
+cudaStream_t cacheStream(const zgpu_cache* c);
+int contextDevice(const zgpu_context* ctx);
 size_t scanScratchElems(int64_t n);
 
 // accessors into the C ABI objects (zgpu_api.cu)

@@ -205,10 +205,23 @@ struct Walker {
         return false;
     }
 
+    // Ends the walk through the neural cache: records the position, the throughput and the
+    // contributions gathered so far; the cache pass adds throughput * cache(x) and merges the
+    // walk into its point.  False (keep walking) when the record buffer is full.
+    __device__ __noinline__ bool cacheTerminate() {
+        unsigned long long slot = atomicAdd(P.counters + kCtrCache, 1ull);
+        if ((long long)slot >= P.cacheCap) { err |= kErrCacheOverflow; return false; }
+        float4* r = P.cacheRec + 2 * slot;
+        r[0] = make_float4(pt[0], pt[1], D == 3 ? pt[D - 1] : 0.0f, thr);
+        r[1] = make_float4(walkTotal + totRefl + totSrc, __int_as_float(point), __int_as_float((int)(lenSum + wlen)), 0.0f);
+        return true;
+    }
+
     // --------------------------------------------------------------- Walk on Spheres step
     ZG_D bool stepWoS() {
         const zgpu_walk_settings& ws = P.ws;
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        if (P.cacheMinDist > 0.0f && wlen > 0 && distAbs >= P.cacheMinDist && cacheTerminate()) return false;
         steps++;
         g.update(pt, distAbs);
         if (!ws.ignore_source_contribution) {
@@ -239,6 +252,10 @@ struct Walker {
     ZG_D bool stepWoSt() {
         const zgpu_walk_settings& ws = P.ws;
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        if (P.cacheMinDist > 0.0f && wlen > 0 && !onRefl && distAbs >= P.cacheMinDist) {
+            bool far = !P.hasRefl || closestPoint<D>(P.reflecting, pt, S, err).d >= P.cacheMinDist;
+            if (far && cacheTerminate()) return false;
+        }
         steps++;
         float R;
         if (firstStep && fsr > 0.0f) {

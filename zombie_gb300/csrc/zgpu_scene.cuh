@@ -44,6 +44,7 @@ constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrSplitOverflow = 2u;
 constexpr uint32_t kErrBudget = 4u;
 constexpr uint32_t kErrBadInput = 8u;
+constexpr uint32_t kErrCacheOverflow = 16u;
 
 struct BoundaryView {
     const float4* nodes = nullptr;

@@ -1,0 +1,112 @@
+"""Neural-cache solving around the plain walk: online training on the solver's own walk
+estimates, a held-out error gate, early walk termination through the cache, and the plain
+walk as fallback and judge of the cache's bias.  No counterpart in the reference.
+
+The compute (walks, training, inference) runs in libzgpu.so; this module is the policy:
+
+1. training estimates: walks at `train_spp` from random interior points (plain walks in the
+   first round; cached walks in later rounds, whose estimates are less noisy);
+2. `cache.train`: Adam on the mean squared error against those estimates;
+3. gate: on held-out points with plain-walk estimates, the cache's error corrected for the
+   estimates' own noise, sqrt(max(0, mean (c(x) - y)^2 - mean se^2)), must stay below
+   `error_bound`; otherwise solves fall back to the plain walk;
+4. solve: zgpu_solve_cached when the gate passed, zgpu_solve otherwise.
+"""
+import time
+
+import numpy as np
+
+from . import problems as P
+from .api import NeuralCache, SampleArrays
+
+
+class NeuralCacheSolver:
+    def __init__(self, solver, pde, walk_settings, cache, min_distance=0.05, error_bound=1e-2):
+        self.solver = solver                # WalkOnSpheres / WalkOnStars over the problem's queries
+        self.pde = pde
+        self.settings = walk_settings
+        self.cache = cache
+        self.min_distance = float(min_distance)
+        self.error_bound = float(error_bound)
+        self.enabled = False
+        self.gate_report = None
+        self.history = []
+
+    @property
+    def queries(self):
+        return self.solver.queries
+
+    def sample_interior(self, n, rng, margin=1e-3):
+        """n uniform points of the domain box that lie inside the domain, at least `margin`
+        from the absorbing boundary, with their distances."""
+        q = self.queries
+        lo = np.asarray(q.domain_min, np.float64)[:q.dim]
+        hi = np.asarray(q.domain_max, np.float64)[:q.dim]
+        pts, dist = [], []
+        have = 0
+        while have < n:
+            x = rng.uniform(lo, hi, (max(2 * (n - have), 1024), q.dim)).astype(np.float32)
+            x = x[q.inside_domain(x)]
+            d = q.compute_dist_to_absorbing_boundary(x)
+            keep = d > margin
+            pts.append(x[keep]); dist.append(d[keep])
+            have += int(keep.sum())
+        return np.concatenate(pts)[:n], np.concatenate(dist)[:n]
+
+    def _arrays(self, x, dist, spp, seed_base):
+        n = x.shape[0]
+        seeds = P.seeds_for(n, base=seed_base)
+        return SampleArrays.host(x, dist, np.full(n, spp, np.int32), seeds)
+
+    def estimate(self, x, dist, spp, seed_base, use_cache):
+        arr = self._arrays(x, dist, spp, seed_base)
+        rep = self.solver.solve_arrays(self.pde, self.settings, arr, cache=self.cache if use_cache else None,
+                                       cache_min_distance=self.min_distance)
+        n = arr["n_solution_estimates"].astype(np.float64)
+        mean = arr["solution_mean"]
+        var = arr["solution_m2"] / np.maximum(n - 1, 1)
+        return mean, np.sqrt(var / np.maximum(n, 1)), rep
+
+    def train(self, x, dist, spp, steps, batch_size=1 << 16, rounds=1, seed_base=1 << 40):
+        """`rounds` of (estimate on x at spp, then `steps` Adam steps); rounds after the first
+        use cached walks when the gate is open."""
+        for r in range(rounds):
+            t0 = time.perf_counter()
+            y, se, rep = self.estimate(x, dist, spp, seed_base + r * (1 << 32), use_cache=self.enabled and r > 0)
+            t1 = time.perf_counter()
+            loss = self.cache.train(x, y.astype(np.float32), steps, batch_size)
+            t2 = time.perf_counter()
+            self.history.append(dict(round=r, estimate_s=t1 - t0, train_s=t2 - t1, loss=loss,
+                                     target_se=float(np.sqrt(np.mean(se ** 2))), steps=rep.total_steps))
+        return self.history[-1]
+
+    def gate(self, x, dist, spp, seed_base=1 << 50):
+        """Held-out check: plain-walk estimates at x decide whether the cache may end walks."""
+        y, se, _ = self.estimate(x, dist, spp, seed_base, use_cache=False)
+        c = self.cache.evaluate(x).astype(np.float64)
+        mse = float(np.mean((c - y) ** 2))
+        noise = float(np.mean(se ** 2))
+        err = float(np.sqrt(max(0.0, mse - noise)))
+        self.enabled = err <= self.error_bound
+        self.gate_report = dict(cache_error=err, raw_rmse=float(np.sqrt(mse)), estimate_se=float(np.sqrt(noise)),
+                                bound=self.error_bound, enabled=self.enabled)
+        return self.gate_report
+
+    def solve_arrays(self, arrays):
+        return self.solver.solve_arrays(self.pde, self.settings, arrays, cache=self.cache if self.enabled else None,
+                                        cache_min_distance=self.min_distance)
+
+    def judge_bias(self, x, dist, spp, seed_base=1 << 52):
+        """Plain against cached estimates at the same points: the mean difference and its
+        standard error (z = mean / se; |z| large means the cache biases the solve)."""
+        yp, sp, _ = self.estimate(x, dist, spp, seed_base, use_cache=False)
+        yc, sc, _ = self.estimate(x, dist, spp, seed_base + 1, use_cache=True)
+        d = yc - yp
+        se = float(np.sqrt(np.mean(sp ** 2 + sc ** 2) / len(d)))
+        return dict(mean_difference=float(np.mean(d)), se=se, z=float(np.mean(d) / max(se, 1e-300)),
+                    rms_difference=float(np.sqrt(np.mean(d ** 2))))
+
+
+def make_cache(queries, dim, **kw):
+    """A NeuralCache over the queries' domain box."""
+    return NeuralCache(dim, np.asarray(queries.domain_min)[:dim], np.asarray(queries.domain_max)[:dim], **kw)

@@ -54,8 +54,9 @@ class GpuProblem:
             dev[k] = t.to("cuda:%d" % self.ctx.device)
         return SampleArrays(**dev)
 
-    def solve(self, arrays, options=None):
-        return self.solver.solve_arrays(self.pde, self.problem.settings, arrays, options)
+    def solve(self, arrays, options=None, cache=None, cache_min_distance=0.05):
+        return self.solver.solve_arrays(self.pde, self.problem.settings, arrays, options, cache=cache,
+                                        cache_min_distance=cache_min_distance)
 
     def exact(self):
         return self.problem.exact()
