@@ -354,11 +354,89 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
+        if args.ttr_points > 0 and not dist:
+            try:
+                line["time_to_rmse"] = time_to_rmse(ctx, args.ttr_points, budget_s=args.ttr_budget)
+            except Exception as e:          # the walk-steps/s line stands on its own
+                line["time_to_rmse"] = {"error": f"{type(e).__name__}: {e}"}
         print(json.dumps(line), flush=True)
     if dist:
         tdist.barrier()
         tdist.destroy_process_group()
     return line
+
+
+def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2), budget_s=150.0, level=8):
+    """Time to reach RMSE targets against the analytic solution on the 3D screened Poisson
+    problem (sigma = 4, icosphere L8, u = exp(0.5x) cos y + z^2): plain Walk on Spheres with
+    progressively doubled walk counts, against the neural cache (online training on the
+    solver's own estimates, held-out gate, then cached walks, doubled the same way).  Wall
+    time on the GPU-resident problem; the cache's time includes all of its training."""
+    import torch
+    from zombie_gb300 import problems as P
+    from zombie_gb300.neural import NeuralCacheSolver, make_cache
+    from zombie_gb300.runner import GpuProblem
+    pr = P.screened_wos_3d(level=level, n_points=n_points, spp=16)
+    gp = GpuProblem(pr, context=ctx)
+    ex = pr.exact()
+    goal = min(targets)
+
+    def rmse(arr):
+        return float(np.sqrt(np.mean((arr["solution_mean"].cpu().numpy() - ex) ** 2)))
+
+    def progressive(arr, t0, cache=None, first_spp=16, deadline=None):
+        hist, total, spp = [], 0, first_spp
+        while True:
+            arr["n_walks"].fill_(spp)
+            rep = gp.solve(arr, cache=cache, cache_min_distance=0.05)
+            torch.cuda.synchronize()
+            total += spp
+            r = rmse(arr)
+            hist.append(dict(t=time.perf_counter() - t0, spp=total, rmse=r, steps_per_walk=rep.total_steps / max(1, rep.total_walks)))
+            log("time-to-rmse", "cache" if cache is not None else "plain", hist[-1])
+            if r <= goal or time.perf_counter() > deadline:
+                return hist
+            spp = total
+
+    def first(hist, tgt):
+        for h in hist:
+            if h["rmse"] <= tgt:
+                return h
+        return None
+
+    start = time.perf_counter()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain = progressive(gp.device_arrays(n_walks=16), t0, deadline=t0 + budget_s / 2)
+    # neural cache: train, gate, then cached walks
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cache = make_cache(gp.queries, 3, log2_table_size=19, max_resolution=64.0, learning_rate_grid=1e-2,
+                       learning_rate_mlp=5e-3, context=ctx)
+    ncs = NeuralCacheSolver(gp.solver, gp.pde, pr.settings, cache, min_distance=0.05, error_bound=5e-3)
+    rng = np.random.default_rng(1234)
+    xt, dt = ncs.sample_interior(1 << 20, rng)
+    ncs.train(xt, dt, spp=16, steps=2000, batch_size=1 << 16)
+    for r in range(4):
+        # self-training on cached walks with a decaying step
+        cache.set_learning_rates(1e-2 * 0.5 ** r, 5e-3 * 0.5 ** r)
+        xt, dt = ncs.sample_interior(1 << 20, rng)
+        ncs.train(xt, dt, spp=16, steps=1000, batch_size=1 << 16, seed_base=(r + 2) << 44, cached=True)
+    xh, dh = ncs.sample_interior(4096, np.random.default_rng(99))
+    gate = ncs.gate(xh, dh, spp=512)
+    train_s = time.perf_counter() - t0
+    log("time-to-rmse cache training", round(train_s, 2), "s; gate", gate, "; rounds", ncs.history)
+    cached = progressive(gp.device_arrays(n_walks=16), t0, cache=cache if gate["enabled"] else None,
+                         deadline=time.perf_counter() + budget_s / 2)
+    out = {"problem": f"3D screened Poisson sigma=4, icosphere L{level}, {n_points} evaluation points",
+           "cache_train_s": train_s, "gate": gate,
+           "plain": plain, "cached": cached, "targets": {}}
+    for tgt in targets:
+        a, b = first(plain, tgt), first(cached, tgt)
+        out["targets"][str(tgt)] = {"plain_s": a["t"] if a else None, "cache_s": b["t"] if b else None,
+                                    "speedup": (a["t"] / b["t"]) if (a and b) else None}
+    out["wall_s"] = time.perf_counter() - start
+    return out
 
 
 def main():
@@ -370,6 +448,9 @@ def main():
     ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ttr-points", type=int, default=1 << 19,
+                    help="evaluation points of the neural-cache time-to-RMSE comparison (0 = skip)")
+    ap.add_argument("--ttr-budget", type=float, default=300.0, help="seconds allowed for that comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -171,6 +171,8 @@ typedef struct zgpu_solve_options {
     int32_t block_size;        /* 0 -> autotuned / default */
     int32_t blocks_per_sm;     /* 0 -> occupancy-derived */
     int32_t use_graph;         /* capture prepare+walk+finalize in a CUDA graph and replay */
+    int32_t query_mode;        /* closest-point queries of Walk on Spheres: 0 auto, 1 one lane per
+                                  query, 2 the whole warp per query (large scenes) */
     int64_t step_budget;       /* per-walk-state hard cap on device loop iterations (0 -> max_walk_length+1) */
 } zgpu_solve_options;
 
@@ -353,6 +355,8 @@ int zgpu_cache_destroy(zgpu_cache* cache);
 int zgpu_cache_layout(const zgpu_cache* cache, int64_t* offsets);
 /* the integer resolution of each level (n_levels floats) */
 int zgpu_cache_resolutions(const zgpu_cache* cache, float* res);
+/* changes the Adam step sizes of later zgpu_cache_train calls (a decay schedule) */
+int zgpu_cache_set_learning_rates(zgpu_cache* cache, float learning_rate_grid, float learning_rate_mlp);
 int zgpu_cache_get_parameters(zgpu_cache* cache, float* out_params);
 int zgpu_cache_set_parameters(zgpu_cache* cache, const float* params);
 /* `steps` Adam steps on batches of batch_size consecutive (wrapping) points of the training

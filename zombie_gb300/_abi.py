@@ -150,6 +150,7 @@ class SolveOptions(C.Structure):
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("use_graph", C.c_int32),
+        ("query_mode", C.c_int32),
         ("step_budget", C.c_int64),
     ]
 

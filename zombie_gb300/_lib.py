@@ -56,6 +56,7 @@ def lib():
         L.zgpu_cache_layout.argtypes = [vp, vp]
         L.zgpu_cache_resolutions.argtypes = [vp, vp]
         L.zgpu_cache_get_parameters.argtypes = [vp, vp]
+        L.zgpu_cache_set_learning_rates.argtypes = [vp, f32, f32]
         L.zgpu_cache_set_parameters.argtypes = [vp, vp]
         L.zgpu_cache_train.argtypes = [vp, i64, vp, vp, i32, i32, i32, C.POINTER(C.c_float)]
         L.zgpu_cache_gradients.argtypes = [vp, i64, vp, vp, i32, vp, C.POINTER(C.c_double)]

@@ -13,7 +13,9 @@ Utils.*BoundaryHandler / populate_geometric_queries_for_*_boundary, all with the
   * walk w of a point draws from pcg32(seed, w + previous estimate count).
 """
 import ctypes as C
+import atexit
 import enum
+import weakref
 
 import numpy as np
 
@@ -61,6 +63,7 @@ class Context:
 
 
 _default_ctx = None
+_live_caches = weakref.WeakSet()
 
 
 def default_context():
@@ -68,6 +71,18 @@ def default_context():
     if _default_ctx is None:
         _default_ctx = Context(0)
     return _default_ctx
+
+
+@atexit.register
+def _shutdown():
+    """Release caches before the contexts whose streams they run on, while the CUDA runtime
+    is still up (interpreter teardown would finalise them in arbitrary order)."""
+    global _default_ctx
+    for c in list(_live_caches):
+        c.close()
+    if _default_ctx is not None:
+        _default_ctx.close()
+        _default_ctx = None
 
 
 # ----------------------------------------------------------------------------- enums
@@ -724,6 +739,7 @@ class NeuralCache:
         h = C.c_void_p()
         check(lib().zgpu_cache_create(self.ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h
+        _live_caches.add(self)
         off = np.zeros(8, np.int64)
         check(lib().zgpu_cache_layout(self.h, A.ptr(off)))
         self.offsets = off
@@ -778,6 +794,9 @@ class NeuralCache:
         check(lib().zgpu_cache_gradients(self.h, int(t.shape[0]), A.ptr(x), A.ptr(t), self._mem(x), A.ptr(g),
                                          C.byref(loss)))
         return loss.value, g
+
+    def set_learning_rates(self, grid, mlp):
+        check(lib().zgpu_cache_set_learning_rates(self.h, float(grid), float(mlp)))
 
     def get_parameters(self):
         p = np.zeros(self.n_parameters, np.float32)

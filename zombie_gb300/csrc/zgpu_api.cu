@@ -569,8 +569,18 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
     P.stackEntries = 8;
     if (P.hasAbs) P.stackEntries = std::max(P.stackEntries, P.absorbing.stackEntries);
     if (P.hasRefl) P.stackEntries = std::max(P.stackEntries, P.reflecting.stackEntries);
+    // Walk on Spheres on a large scene: each closest-point query is answered by a whole warp
+    // (per-query work varies by orders of magnitude between walks, which idles the lanes of
+    // a one-lane-per-query traversal); the walk kernel then needs no per-thread stack
+    const int queryMode = opt ? opt->query_mode : 0;
+    if (queryMode < 0 || queryMode > 2) return fail(ZGPU_ERR_INVALID_ARG, "query_mode must be 0, 1 or 2");
+    const int walkStackEntries = P.stackEntries;
+    if (solver == ZGPU_SOLVER_WALK_ON_SPHERES && P.hasAbs)
+        P.coop = queryMode == 2 || (queryMode == 0 && D == 3 && q->absorbing->nPrims >= kCoopMinPrims);
+    if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
-                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f, threads, P.stackEntries);
+                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f, threads, P);
+    P.stackEntries = walkStackEntries;
     int blocks = ctx->numSMs * perSM;
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
 
@@ -587,6 +597,7 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
         P.cacheMinDist = cacheMinDist;
     }
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
+    if (P.coop) P.stackEntries = 0;     // the prepare kernel above used the per-thread stacks
     if (n > 0) ZG_CUDA(launchWalk(P, D, blocks, threads, s));
     if (cache && n > 0)
         ZG_CUDA(launchCacheAccumulate(cache, P.cacheRec, P.counters + kCtrCache, P.cacheCap, P.accSum, P.accSq,

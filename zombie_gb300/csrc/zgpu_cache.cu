@@ -20,8 +20,8 @@ namespace {
 // shared-memory carve-up of the training kernel (byte offsets, 16-byte aligned)
 constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 constexpr size_t kOffW = 0;
-constexpr size_t kOffE = align16(kOffW + sizeof(SharedWeights));                        // 4 x [16][kS32]
-constexpr size_t kOffET = align16(kOffE + sizeof(__nv_bfloat16) * kWarps * kRows * kS32);   // [32][kS64]
+constexpr size_t kOffE = align16(kOffW + sizeof(SharedWeights));                        // 4 x 2 x [16][kS32]
+constexpr size_t kOffET = align16(kOffE + sizeof(__nv_bfloat16) * kWarps * 2 * kRows * kS32);   // [32][kS64]
 constexpr size_t kOffH1T = align16(kOffET + sizeof(__nv_bfloat16) * kInputs * kS64);    // [64][kS64]
 constexpr size_t kOffDZ2T = align16(kOffH1T + sizeof(__nv_bfloat16) * kHidden * kS64);
 constexpr size_t kOffDZ1T = align16(kOffDZ2T + sizeof(__nv_bfloat16) * kHidden * kS64);
@@ -30,7 +30,7 @@ constexpr size_t kOffX = align16(kOffDE + sizeof(float) * kWarps * kRows * 33); 
 constexpr size_t kTrainSmem = align16(kOffX + sizeof(float) * kWarps * kRows * 3);
 // inference kernel: weights + per-warp encoding tiles + positions
 constexpr size_t kEvalOffE = align16(sizeof(SharedWeights));
-constexpr size_t kEvalOffX = align16(kEvalOffE + sizeof(__nv_bfloat16) * kWarps * kRows * kS32);
+constexpr size_t kEvalOffX = align16(kEvalOffE + sizeof(__nv_bfloat16) * kWarps * 2 * kRows * kS32);
 constexpr size_t kEvalSmem = align16(kEvalOffX + sizeof(float) * kWarps * kRows * 3);
 
 ZG_D __nv_bfloat16 bf(float v) { return __float2bfloat16_rn(v); }
@@ -45,7 +45,7 @@ trainKernel(const Net N, const Grads G, const float* __restrict__ x, const float
     SharedWeights& S = *reinterpret_cast<SharedWeights*>(smem + kOffW);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* E = reinterpret_cast<__nv_bfloat16*>(smem + kOffE) + warp * kRows * kS32;
+    __nv_bfloat16* E = reinterpret_cast<__nv_bfloat16*>(smem + kOffE) + warp * 2 * kRows * kS32;
     __nv_bfloat16* eT = reinterpret_cast<__nv_bfloat16*>(smem + kOffET);
     __nv_bfloat16* h1T = reinterpret_cast<__nv_bfloat16*>(smem + kOffH1T);
     __nv_bfloat16* dz2T = reinterpret_cast<__nv_bfloat16*>(smem + kOffDZ2T);
@@ -262,7 +262,7 @@ evalKernel(const Net N, const float* __restrict__ x, float* __restrict__ y, int6
     SharedWeights& S = *reinterpret_cast<SharedWeights*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* E = reinterpret_cast<__nv_bfloat16*>(smem + kEvalOffE) + warp * kRows * kS32;
+    __nv_bfloat16* E = reinterpret_cast<__nv_bfloat16*>(smem + kEvalOffE) + warp * 2 * kRows * kS32;
     float (*xs)[3] = reinterpret_cast<float (*)[3]>(smem + kEvalOffX) + warp * kRows;
     loadWeights(N, S, false);
     __syncthreads();
@@ -330,7 +330,8 @@ __global__ void encodeKernel(const Net N, const float* __restrict__ x, float* __
 __global__ void adamKernel(float* __restrict__ p, float* __restrict__ gr, float* __restrict__ m, float* __restrict__ v,
                            int64_t nTotal, int64_t nTable, int64_t oW1, int64_t oW2, float lrGrid, float lrMlp,
                            float beta1, float beta2, float eps, float c1, float c2, __half* tableHalf,
-                           __nv_bfloat16* W1b, __nv_bfloat16* W2b, int apply) {
+                           __nv_bfloat16* W1b, __nv_bfloat16* W2b, __nv_bfloat16* W1lo, __nv_bfloat16* W2lo,
+                           int apply) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nTotal; i += (int64_t)gridDim.x * blockDim.x) {
         float w = p[i];
         if (apply) {
@@ -344,9 +345,17 @@ __global__ void adamKernel(float* __restrict__ p, float* __restrict__ gr, float*
             p[i] = w;
             gr[i] = 0.0f;
         }
-        if (i < nTable) tableHalf[i] = __float2half_rn(w);
-        else if (i >= oW1 && i < oW1 + kHidden * kInputs) W1b[i - oW1] = __float2bfloat16_rn(w);
-        else if (i >= oW2 && i < oW2 + kHidden * kHidden) W2b[i - oW2] = __float2bfloat16_rn(w);
+        if (i < nTable) {
+            tableHalf[i] = __float2half_rn(w);
+        } else if (i >= oW1 && i < oW1 + kHidden * kInputs) {
+            __nv_bfloat16 hi = __float2bfloat16_rn(w);
+            W1b[i - oW1] = hi;
+            W1lo[i - oW1] = __float2bfloat16_rn(w - __bfloat162float(hi));
+        } else if (i >= oW2 && i < oW2 + kHidden * kHidden) {
+            __nv_bfloat16 hi = __float2bfloat16_rn(w);
+            W2b[i - oW2] = hi;
+            W2lo[i - oW2] = __float2bfloat16_rn(w - __bfloat162float(hi));
+        }
     }
 }
 
@@ -367,6 +376,8 @@ struct zgpu_cache {
     __half* tableHalf = nullptr;
     __nv_bfloat16* W1b = nullptr;
     __nv_bfloat16* W2b = nullptr;
+    __nv_bfloat16* W1lo = nullptr;
+    __nv_bfloat16* W2lo = nullptr;
     double* loss = nullptr;
     float* stageX = nullptr;
     float* stageT = nullptr;
@@ -445,7 +456,7 @@ cudaError_t launchAdam(zgpu_cache* c, int apply) {
     int blocks = c->numSMs * 8;
     adamKernel<<<blocks, 256, 0, c->stream>>>(c->master, c->grad, c->m, c->v, c->total, c->oW1, c->oW1, c->oW2,
                                                k.learning_rate_grid, k.learning_rate_mlp, k.beta1, k.beta2, k.epsilon,
-                                               c1, c2, c->tableHalf, c->W1b, c->W2b, apply);
+                                               c1, c2, c->tableHalf, c->W1b, c->W2b, c->W1lo, c->W2lo, apply);
     return cudaGetLastError();
 }
 
@@ -541,10 +552,12 @@ int zgpu_cache_create(zgpu_context* ctx, const zgpu_cache_config* cfg, zgpu_cach
         cudaMalloc(&c->tableHalf, (size_t)c->oW1 * sizeof(__half)) != cudaSuccess ||
         cudaMalloc(&c->W1b, kHidden * kInputs * sizeof(__nv_bfloat16)) != cudaSuccess ||
         cudaMalloc(&c->W2b, kHidden * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&c->W1lo, kHidden * kInputs * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&c->W2lo, kHidden * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
         cudaMalloc(&c->loss, sizeof(double)) != cudaSuccess)
         return cleanup(cfail(ZGPU_ERR_OUT_OF_MEMORY, "cannot allocate the cache parameters (%zu bytes each)", bytes));
     N.table = reinterpret_cast<const __half2*>(c->tableHalf);
-    N.W1 = c->W1b; N.W2 = c->W2b;
+    N.W1 = c->W1b; N.W2 = c->W2b; N.W1lo = c->W1lo; N.W2lo = c->W2lo;
     N.b1 = c->master + c->oB1; N.b2 = c->master + c->oB2; N.w3 = c->master + c->oW3; N.b3 = c->master + c->oB3;
     // initialisation: table U(-1e-4, 1e-4), weights Glorot-uniform, biases 0
     std::vector<float> h((size_t)c->total, 0.0f);
@@ -568,9 +581,11 @@ int zgpu_cache_create(zgpu_context* ctx, const zgpu_cache_config* cfg, zgpu_cach
 
 int zgpu_cache_destroy(zgpu_cache* c) {
     if (!c) return ZGPU_OK;
-    if (c->stream) cudaStreamSynchronize(c->stream);
+    // the context's stream may already be gone: wait on the whole device instead
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
     for (void* p : {(void*)c->master, (void*)c->grad, (void*)c->m, (void*)c->v, (void*)c->tableHalf, (void*)c->W1b,
-                    (void*)c->W2b, (void*)c->loss, (void*)c->stageX, (void*)c->stageT})
+                    (void*)c->W2b, (void*)c->W1lo, (void*)c->W2lo, (void*)c->loss, (void*)c->stageX, (void*)c->stageT})
         if (p) cudaFree(p);
     delete c;
     return ZGPU_OK;
@@ -586,6 +601,14 @@ int zgpu_cache_layout(const zgpu_cache* c, int64_t* offsets) {
 int zgpu_cache_resolutions(const zgpu_cache* c, float* res) {
     if (!c || !res) return cfail(ZGPU_ERR_INVALID_ARG, "NULL argument");
     for (int l = 0; l < c->cfg.n_levels; l++) res[l] = c->net.res[l];
+    return ZGPU_OK;
+}
+
+int zgpu_cache_set_learning_rates(zgpu_cache* c, float grid, float mlp) {
+    if (!c) return cfail(ZGPU_ERR_INVALID_ARG, "NULL argument");
+    if (!(grid >= 0.0f) || !(mlp >= 0.0f)) return cfail(ZGPU_ERR_INVALID_ARG, "learning rates must be >= 0");
+    c->cfg.learning_rate_grid = grid;
+    c->cfg.learning_rate_mlp = mlp;
     return ZGPU_OK;
 }
 

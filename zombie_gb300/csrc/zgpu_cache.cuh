@@ -40,8 +40,10 @@ struct Net {
     float res[kMaxLevels];
     float lo[3], inv[3];
     const __half2* table = nullptr;            // [levels][T] (2 features per entry)
-    const __nv_bfloat16* W1 = nullptr;         // [64][32]
+    const __nv_bfloat16* W1 = nullptr;         // [64][32] BF16 of the FP32 master
     const __nv_bfloat16* W2 = nullptr;         // [64][64]
+    const __nv_bfloat16* W1lo = nullptr;       // BF16 of the rounding remainders (W = W1 + W1lo)
+    const __nv_bfloat16* W2lo = nullptr;
     const float* b1 = nullptr;                 // FP32 master copies
     const float* b2 = nullptr;
     const float* w3 = nullptr;
@@ -114,8 +116,10 @@ ZG_D float2 encodeLevel(const Net& N, int l, const float* x) {
     return f;
 }
 
-// Encodes the warp's 16 points into E (row-major [16][kS32] BF16).  Lane j handles point
-// j & 15 for levels (j >> 4) + 2s, s = 0..7; rows >= nValid and levels >= N.levels are 0.
+// Encodes the warp's 16 points into two row-major [16][kS32] BF16 tiles: E holds the
+// rounded features, E + kRows * kS32 the rounding remainders (hi + lo carries ~16 mantissa
+// bits into the tensor cores).  Lane j handles point j & 15 for levels (j >> 4) + 2s,
+// s = 0..7; rows >= nValid and levels >= N.levels are 0.
 template <int D>
 ZG_D void encodeTile(const Net& N, const float (*x)[3], int nValid, __nv_bfloat16* E, int lane) {
     const int p = lane & 15;
@@ -124,7 +128,10 @@ ZG_D void encodeTile(const Net& N, const float (*x)[3], int nValid, __nv_bfloat1
         int l = (lane >> 4) + 2 * s;
         float2 f = make_float2(0.0f, 0.0f);
         if (p < nValid && l < N.levels) f = encodeLevel<D>(N, l, x[p]);
-        *reinterpret_cast<__nv_bfloat162*>(E + p * kS32 + 2 * l) = __floats2bfloat162_rn(f.x, f.y);
+        __nv_bfloat162 hi = __floats2bfloat162_rn(f.x, f.y);
+        float2 h = __bfloat1622float2(hi);
+        *reinterpret_cast<__nv_bfloat162*>(E + p * kS32 + 2 * l) = hi;
+        *reinterpret_cast<__nv_bfloat162*>(E + kRows * kS32 + p * kS32 + 2 * l) = __floats2bfloat162_rn(f.x - h.x, f.y - h.y);
     }
 }
 
@@ -133,6 +140,13 @@ ZG_D uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint
 ZG_D uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
+}
+// BF16 pair of (a, b) and the pair of their rounding remainders
+ZG_D void pack2split(float a, float b, uint32_t& hi, uint32_t& lo) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    float2 f = __bfloat1622float2(v);
+    hi = *reinterpret_cast<uint32_t*>(&v);
+    lo = pack2(a - f.x, b - f.y);
 }
 // D = A(16x16, row) * B(16x8, col) + C, BF16 in, FP32 accumulate
 ZG_D void mma16816(float c[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1) {
@@ -147,6 +161,8 @@ ZG_D void mma16816(float c[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a
 struct SharedWeights {
     __nv_bfloat16 W1[kHidden * kS32];    // [out][in]
     __nv_bfloat16 W2[kHidden * kS64];
+    __nv_bfloat16 W1lo[kHidden * kS32];  // remainders of the BF16 rounding
+    __nv_bfloat16 W2lo[kHidden * kS64];
     __nv_bfloat16 W1T[kInputs * kS64];   // [in][out] (backward)
     __nv_bfloat16 W2T[kHidden * kS64];
     float b1[kHidden], b2[kHidden], w3[kHidden];
@@ -158,12 +174,14 @@ ZG_D void loadWeights(const Net& N, SharedWeights& S, bool transposed) {
         int o = i / kInputs, k = i % kInputs;
         __nv_bfloat16 v = N.W1[i];
         S.W1[o * kS32 + k] = v;
+        S.W1lo[o * kS32 + k] = N.W1lo[i];
         if (transposed) S.W1T[k * kS64 + o] = v;
     }
     for (int i = threadIdx.x; i < kHidden * kHidden; i += blockDim.x) {
         int o = i / kHidden, k = i % kHidden;
         __nv_bfloat16 v = N.W2[i];
         S.W2[o * kS64 + k] = v;
+        S.W2lo[o * kS64 + k] = N.W2lo[i];
         if (transposed) S.W2T[k * kS64 + o] = v;
     }
     for (int i = threadIdx.x; i < kHidden; i += blockDim.x) {
@@ -174,7 +192,10 @@ ZG_D void loadWeights(const Net& N, SharedWeights& S, bool transposed) {
 
 // Forward pass of one warp tile.  h1/h2 hold the post-ReLU activations in accumulator layout
 // (n-tile nt, element e: row g + 8 (e >> 1), column 8 nt + 2 t + (e & 1)); returns the output
-// for rows g (y.x) and g + 8 (y.y), identical in the 4 lanes of a quad.
+// for rows g (y.x) and g + 8 (y.y), identical in the 4 lanes of a quad.  Activations and
+// weights enter each layer as BF16 hi + lo pairs and every product takes three MMAs
+// (hi*hi + lo*hi + hi*lo), so the output keeps FP32-class precision instead of BF16's 0.4%
+// relative rounding, which would otherwise floor the cache's accuracy.
 ZG_D float2 forwardTile(const SharedWeights& S, const __nv_bfloat16* E, float h1[8][4], float h2[8][4], int lane) {
     const int g = lane >> 2, t = lane & 3;
 #pragma unroll
@@ -184,12 +205,17 @@ ZG_D float2 forwardTile(const SharedWeights& S, const __nv_bfloat16* E, float h1
     }
 #pragma unroll
     for (int kt = 0; kt < 2; kt++) {
-        uint32_t a0 = ld32(E + g * kS32 + 16 * kt + 2 * t), a1 = ld32(E + (g + 8) * kS32 + 16 * kt + 2 * t);
-        uint32_t a2 = ld32(E + g * kS32 + 16 * kt + 8 + 2 * t), a3 = ld32(E + (g + 8) * kS32 + 16 * kt + 8 + 2 * t);
+        const __nv_bfloat16* El = E + kRows * kS32;
+        const int o0 = g * kS32 + 16 * kt + 2 * t, o1 = (g + 8) * kS32 + 16 * kt + 2 * t;
+        uint32_t a0 = ld32(E + o0), a1 = ld32(E + o1), a2 = ld32(E + o0 + 8), a3 = ld32(E + o1 + 8);
+        uint32_t l0 = ld32(El + o0), l1 = ld32(El + o1), l2 = ld32(El + o0 + 8), l3 = ld32(El + o1 + 8);
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
-            const __nv_bfloat16* w = S.W1 + (8 * nt + g) * kS32 + 16 * kt + 2 * t;
-            mma16816(h1[nt], a0, a1, a2, a3, ld32(w), ld32(w + 8));
+            const int wo = (8 * nt + g) * kS32 + 16 * kt + 2 * t;
+            const uint32_t b0 = ld32(S.W1 + wo), b1 = ld32(S.W1 + wo + 8);
+            mma16816(h1[nt], a0, a1, a2, a3, b0, b1);
+            mma16816(h1[nt], l0, l1, l2, l3, b0, b1);
+            mma16816(h1[nt], a0, a1, a2, a3, ld32(S.W1lo + wo), ld32(S.W1lo + wo + 8));
         }
     }
 #pragma unroll
@@ -203,12 +229,18 @@ ZG_D float2 forwardTile(const SharedWeights& S, const __nv_bfloat16* E, float h1
     }
 #pragma unroll
     for (int kt = 0; kt < 4; kt++) {
-        uint32_t a0 = pack2(h1[2 * kt][0], h1[2 * kt][1]), a1 = pack2(h1[2 * kt][2], h1[2 * kt][3]);
-        uint32_t a2 = pack2(h1[2 * kt + 1][0], h1[2 * kt + 1][1]), a3 = pack2(h1[2 * kt + 1][2], h1[2 * kt + 1][3]);
+        uint32_t a0, a1, a2, a3, l0, l1, l2, l3;
+        pack2split(h1[2 * kt][0], h1[2 * kt][1], a0, l0);
+        pack2split(h1[2 * kt][2], h1[2 * kt][3], a1, l1);
+        pack2split(h1[2 * kt + 1][0], h1[2 * kt + 1][1], a2, l2);
+        pack2split(h1[2 * kt + 1][2], h1[2 * kt + 1][3], a3, l3);
 #pragma unroll
         for (int nt = 0; nt < 8; nt++) {
-            const __nv_bfloat16* w = S.W2 + (8 * nt + g) * kS64 + 16 * kt + 2 * t;
-            mma16816(h2[nt], a0, a1, a2, a3, ld32(w), ld32(w + 8));
+            const int wo = (8 * nt + g) * kS64 + 16 * kt + 2 * t;
+            const uint32_t b0 = ld32(S.W2 + wo), b1 = ld32(S.W2 + wo + 8);
+            mma16816(h2[nt], a0, a1, a2, a3, b0, b1);
+            mma16816(h2[nt], l0, l1, l2, l3, b0, b1);
+            mma16816(h2[nt], a0, a1, a2, a3, ld32(S.W2lo + wo), ld32(S.W2lo + wo + 8));
         }
     }
     float y0 = 0.0f, y1 = 0.0f;

@@ -61,16 +61,22 @@ struct SolveParams {
     float cacheMinDist;
     float4* cacheRec;
     long long cacheCap;
+    // Walk on Spheres: closest-point queries answered by the whole warp (CoopWork per warp in
+    // shared memory after the per-thread stacks)
+    int coop;
 };
 
 constexpr int kSplitStack = 8;
+// Walk on Spheres in 3D answers closest-point queries with a whole warp from this many
+// absorbing primitives on (query_mode 0)
+constexpr int kCoopMinPrims = 20000;
 
 // kernels / launchers (zgpu_walk.cu)
 cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);
 cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStream_t s);
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
-int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, int stackEntries);
+int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, const SolveParams& p);
 // neural cache pass over the walk records (zgpu_cache.cu)
 cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
                                   int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,

@@ -69,6 +69,8 @@ struct Walker {
     // loop state
     float distAbs, fsr;
     bool firstStep, cpValid;
+    bool queryPending;      // cooperative mode: the closest-point query of this state is due
+    int pendingCode;        // cooperative mode: terminate(code) once the query is answered (-1: none)
     V<D> cpPt, cpN;
     Greens<D, SCREENED> g;
     float4* splitSlots;   // this thread's kSplitStack slots of 3 float4
@@ -86,6 +88,7 @@ struct Walker {
     }
 
     ZG_D void closestQuery() {
+        if (P.coop && P.hasAbs) { queryPending = true; cpValid = false; return; }
         if (P.hasAbs) {
             ClosestHit<D> h = closestPoint<D>(P.absorbing, pt, S, err);
             distAbs = h.d;
@@ -127,7 +130,24 @@ struct Walker {
         fsr = P.fsr[point];
         firstStep = true;
         cpValid = false;
+        queryPending = false;
+        pendingCode = -1;
         resetGreens();
+    }
+
+    // answer of a cooperative closest-point query
+    ZG_D void setClosest(float d, int slot) {
+        distAbs = d;
+        cpPt = pt;
+        if (slot >= 0) {
+            Prim<D> t = loadPrim<D>(P.absorbing, slot);
+            V<D> q;
+            closestOnPrim(t, pt, q);
+            cpPt = q;
+            cpN = primNormal<D>(t);
+        }
+        cpValid = true;
+        queryPending = false;
     }
 
     __device__ __noinline__ void pushSplit() {
@@ -182,7 +202,7 @@ struct Walker {
             if (payTerminal && !P.ws.ignore_absorbing_boundary_contribution) {
                 // projectToAbsorbingBoundary then pde.dirichlet (walk_on_spheres.h:294-318, walk_on_stars.h:493-516)
                 if (P.hasAbs) {
-                    if (!cpValid) closestQuery();
+                    if (!cpValid && !P.coop) closestQuery();
                     bool aligned = false;
                     if (P.ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
                     term = pde.dirichlet(cpPt, aligned);
@@ -220,7 +240,11 @@ struct Walker {
     // --------------------------------------------------------------- Walk on Spheres step
     ZG_D bool stepWoS() {
         const zgpu_walk_settings& ws = P.ws;
-        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) {
+            // the terminal value needs the projection: in cooperative mode the warp answers first
+            if (P.coop && P.hasAbs && !cpValid) { pendingCode = kReached; closestQuery(); return true; }
+            return terminate(kReached);
+        }
         if (P.cacheMinDist > 0.0f && wlen > 0 && distAbs >= P.cacheMinDist && cacheTerminate()) return false;
         steps++;
         g.update(pt, distAbs);
@@ -242,7 +266,11 @@ struct Walker {
         if (outsideBox(P, pt.v, D)) return terminate(kEscaped);
         if (weightWindow()) return terminate(kRussianRoulette);
         wlen++;
-        if (wlen >= ws.max_walk_length) return terminate(kExceeded);
+        if (wlen >= ws.max_walk_length) {
+            // WoS pays the terminal value of the projected point: query first when cooperative
+            if (P.coop && P.hasAbs) { pendingCode = kExceeded; closestQuery(); return true; }
+            return terminate(kExceeded);
+        }
         if (P.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
         closestQuery();
         return true;
@@ -379,7 +407,13 @@ struct Walker {
         return true;
     }
 
-    ZG_D bool step() { return SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES ? stepWoS() : stepWoSt(); }
+    ZG_D bool step() {
+        if (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES) {
+            if (pendingCode >= 0) { const int code = pendingCode; pendingCode = -1; return terminate(code); }
+            return stepWoS();
+        }
+        return stepWoSt();
+    }
 };
 
 constexpr int kWalkThreads = 128;
@@ -408,6 +442,7 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
     extern __shared__ int dynStack[];
     TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
                 (int)blockDim.x, P.stackEntries};
+    CoopWork* coopWork = reinterpret_cast<CoopWork*>(dynStack + 2 * P.stackEntries * blockDim.x) + (threadIdx.x >> 5);
     Walker<D, SOLVER, SCREENED> W(P, S);
     W.splitSlots = P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack;
     const int lane = threadIdx.x & 31;
@@ -440,6 +475,21 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
         }
         if (!__any_sync(kFull, active)) break;
         if (active) active = W.step();
+        if (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && P.coop) {
+            // closest-point queries of this round, one at a time with the whole warp
+            unsigned qm = __ballot_sync(kFull, active && W.queryPending);
+            while (qm) {
+                const int src = __ffs(qm) - 1;
+                qm &= qm - 1;
+                V<D> x;
+#pragma unroll
+                for (int i = 0; i < D; i++) x[i] = __shfl_sync(kFull, W.pt[i], src);
+                float d;
+                int slot;
+                coopClosest<D>(P.absorbing, x, *coopWork, lane, d, slot, W.err);
+                if (lane == src) W.setClosest(d, slot);
+            }
+        }
     }
     // warp-reduce the counters, one atomic per warp
     unsigned long long v[4] = {W.steps, W.escaped, W.exceeded, W.rr};
@@ -673,25 +723,28 @@ inline unsigned gridFor(int64_t n, int t) { return (unsigned)((n + t - 1) / t); 
 
 
 inline size_t smemBytes(int stackEntries, int threads) { return (size_t)stackEntries * threads * 8; }
+// walk kernel: per-thread stacks, then one CoopWork per warp in cooperative mode
+inline size_t walkSmemBytes(const SolveParams& p, int threads) {
+    return smemBytes(p.stackEntries, threads) + (p.coop ? sizeof(CoopWork) * (size_t)(threads / 32) : 0);
+}
 
 // walk kernel launchers, explicitly instantiated per (dimension, solver) in zgpu_walk_<D>d_<solver>.cu
 template <int D, int SOLVER>
 struct WalkLaunch {
     static cudaError_t walk(const SolveParams& p, int blocks, int threads, cudaStream_t s) {
-        size_t smem = smemBytes(p.stackEntries, threads);
+        size_t smem = walkSmemBytes(p, threads);
         cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (p.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true><<<blocks, threads, smemBytes(p.stackEntries, threads), s>>>(p);
-        else detail::walkKernel<D, SOLVER, false><<<blocks, threads, smemBytes(p.stackEntries, threads), s>>>(p);
+        if (p.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true><<<blocks, threads, smem, s>>>(p);
+        else detail::walkKernel<D, SOLVER, false><<<blocks, threads, smem, s>>>(p);
         return cudaGetLastError();
     }
-    static int maxBlocksPerSM(bool screened, int threads, int stackEntries) {
+    static int maxBlocksPerSM(bool screened, int threads, size_t smem) {
         int n = 0;
-        size_t smem = smemBytes(stackEntries, threads);
         cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         const void* f = screened ? (const void*)detail::walkKernel<D, SOLVER, true> : (const void*)detail::walkKernel<D, SOLVER, false>;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smemBytes(stackEntries, threads)) != cudaSuccess) return 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess) return 1;
         return n > 0 ? n : 1;
     }
 };

@@ -312,6 +312,137 @@ __device__ __noinline__ ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x
     return best;
 }
 
+// ---------------------------------------------------------------- warp-cooperative closest point
+// All 32 lanes of a warp answer one query together (the caller loops over the lanes that
+// need one).  A greedy descent to the nearest leaf gives the first bound; then each round
+// takes up to 8 stack entries and tests their 4 children in parallel (lane = 4 * entry +
+// child), pushes internal children within the bound and gathers the primitives of leaf
+// children, which are tested 32 at a time.  The bound only shrinks and every comparison is
+// inclusive, so the answer -- the primitive of least (distance, index) -- is the one the
+// per-thread traversal returns.  The per-warp stack holds kCoopStack entries; on overflow the
+// query stops and kErrStackOverflow is raised.
+constexpr int kCoopStack = 480;
+constexpr int kCoopPrims = 256;       // 8 entries x 4 leaf children x up to 8 primitives
+struct CoopWork {
+    int node[kCoopStack];
+    float key[kCoopStack];
+    int prim[kCoopPrims];
+};
+
+// component c of a float4 (c uniform within a quad of lanes, varying across the warp)
+ZG_D float comp4(float4 v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+ZG_D int comp4i(int4 v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+
+template <int D>
+ZG_D float childBoxDist2(const BoundaryView& b, int node, int c, V<D> x, int& child) {
+    const float4* p = b.nodes + (size_t)node * 8;
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float lo = comp4(__ldg(p + i), c), hi = comp4(__ldg(p + D + i), c);
+        float d = fmaxf(fmaxf(lo - x[i], 0.0f), x[i] - hi);
+        s += d * d;
+    }
+    child = comp4i(__ldg(reinterpret_cast<const int4*>(p + 2 * D)), c);
+    return s;
+}
+
+// folds the lanes' (d, idx, slot) candidates into the warp's best (uniform result)
+ZG_D void warpBest(float d, int idx, int slot, float& bestD, int& bestIdx, int& bestSlot) {
+    unsigned dm = __reduce_min_sync(0xffffffffu, __float_as_uint(d));   // d >= 0: bits order as values
+    float dmin = __uint_as_float(dm);
+    int im = __reduce_min_sync(0xffffffffu, (unsigned)(d == dmin ? idx : 0x7fffffff));
+    unsigned owner = __ballot_sync(0xffffffffu, d == dmin && idx == im);
+    int smin = __shfl_sync(0xffffffffu, slot, __ffs(owner) - 1);
+    if (dmin < bestD || (dmin == bestD && im < bestIdx)) { bestD = dmin; bestIdx = im; bestSlot = smin; }
+}
+
+template <int D>
+__device__ __noinline__ void coopClosest(const BoundaryView& b, V<D> x, CoopWork& W, int lane, float& outD,
+                                         int& outSlot, uint32_t& err) {
+    float bestD = kFltMax, best2 = kFltMax;
+    int bestIdx = 0x7fffffff, bestSlot = -1;
+    outD = kFltMax; outSlot = -1;
+    if (b.nNodes == 0) return;
+    const int c = lane & 3;
+    // greedy descent: follow the nearest child to a leaf and test its primitives
+    {
+        int node = 0;
+        for (int guard = 0; guard < kMaxWideDepth + 2; guard++) {
+            int child;
+            float d2 = childBoxDist2<D>(b, node, c, x, child);
+            if (child == kEmptyChild) d2 = kFltMax;
+            unsigned m = __reduce_min_sync(0xffffffffu, __float_as_uint(d2));
+            int k = __ffs(__ballot_sync(0xffffffffu, __float_as_uint(d2) == m)) - 1;
+            int pick = __shfl_sync(0xffffffffu, child, k);
+            if (pick == kEmptyChild) break;
+            if (!isLeaf(pick)) { node = pick; continue; }
+            float d = kFltMax; int idx = 0x7fffffff, slot = -1;
+            if (lane < leafCount(pick)) {
+                slot = leafFirst(pick) + lane;
+                V<D> q;
+                d = closestOnPrim(loadPrim<D>(b, slot), x, q);
+                idx = __ldg(b.primIndex + slot);
+            }
+            warpBest(d, idx, slot, bestD, bestIdx, bestSlot);
+            best2 = bestD * bestD;
+            break;
+        }
+    }
+    if (lane == 0) { W.node[0] = 0; W.key[0] = 0.0f; }
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int take = min(8, sp);
+        sp -= take;
+        const int e = lane >> 2;
+        int node = -1;
+        float key = kFltMax;
+        if (e < take) { node = W.node[sp + e]; key = W.key[sp + e]; }
+        __syncwarp();
+        int child = kEmptyChild;
+        float d2 = kFltMax;
+        if (node >= 0 && key <= best2) d2 = childBoxDist2<D>(b, node, c, x, child);
+        const bool ok = child != kEmptyChild && d2 <= best2;
+        const bool inner = ok && !isLeaf(child), leaf = ok && isLeaf(child);
+        // push the internal children
+        const unsigned im = __ballot_sync(0xffffffffu, inner);
+        const int nIn = __popc(im);
+        if (sp + nIn > kCoopStack) { err |= kErrStackOverflow; break; }
+        if (inner) {
+            int pos = sp + __popc(im & ((1u << lane) - 1u));
+            W.node[pos] = child;
+            W.key[pos] = d2;
+        }
+        sp += nIn;
+        // gather the leaf primitives: exclusive scan of the leaf sizes
+        int cnt = leaf ? leafCount(child) : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int j = 0; j < cnt; j++) W.prim[incl - cnt + j] = leafFirst(child) + j;
+        __syncwarp();
+        for (int base = 0; base < total; base += 32) {
+            float d = kFltMax; int idx = 0x7fffffff, slot = -1;
+            if (base + lane < total) {
+                slot = W.prim[base + lane];
+                V<D> q;
+                d = closestOnPrim(loadPrim<D>(b, slot), x, q);
+                idx = __ldg(b.primIndex + slot);
+            }
+            warpBest(d, idx, slot, bestD, bestIdx, bestSlot);
+            best2 = bestD * bestD;
+        }
+        __syncwarp();
+    }
+    outD = bestD;
+    outSlot = bestSlot;
+}
+
 // ---------------------------------------------------------------- first ray hit
 template <int D>
 struct RayHit {
