@@ -417,13 +417,15 @@ def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2), budget_s=150.0, level=8):
     rng = np.random.default_rng(1234)
     xt, dt = ncs.sample_interior(1 << 20, rng)
     ncs.train(xt, dt, spp=16, steps=2000, batch_size=1 << 16)
-    for r in range(4):
-        # self-training on cached walks with a decaying step
-        cache.set_learning_rates(1e-2 * 0.5 ** r, 5e-3 * 0.5 ** r)
+    for r in range(6):
+        # self-training on cached walks
         xt, dt = ncs.sample_interior(1 << 20, rng)
         ncs.train(xt, dt, spp=16, steps=1000, batch_size=1 << 16, seed_base=(r + 2) << 44, cached=True)
+    xc, dc = ncs.sample_interior(8192, np.random.default_rng(98))
+    offset, tau = ncs.calibrate(xc, dc, spp=256)
     xh, dh = ncs.sample_interior(4096, np.random.default_rng(99))
     gate = ncs.gate(xh, dh, spp=512)
+    gate["calibrated_offset"], gate["termination_throughput"] = offset, tau
     train_s = time.perf_counter() - t0
     log("time-to-rmse cache training", round(train_s, 2), "s; gate", gate, "; rounds", ncs.history)
     cached = progressive(gp.device_arrays(n_walks=16), t0, cache=cache if gate["enabled"] else None,

@@ -356,3 +356,39 @@ def test_cooperative_queries_reproduce_per_lane_queries(zgpu, make):
     # query mode changes: the moments agree to the last few bits
     for k in ("solution_mean", "solution_m2"):
         assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-15), k
+
+
+def test_batched_solve_equals_individual_solves(zgpu):
+    """Independent 2D problems in one launch (scene table + per-point scene id) run the walks
+    each problem runs alone: identical counts and walk lengths, moments to the last bits."""
+    from zombie_gb300.runner import GpuBatch, GpuProblem
+    scenes = P.batched_scenes(n_scenes=5, seed=3, point_scale=0.004, segments=(256, 4096))
+    batch = GpuBatch(scenes)
+    arr = batch.device_arrays()
+    rep = batch.solve(arr)
+    assert rep.error_word == 0
+    for k, g in enumerate(batch.problems):
+        d = g.device_arrays()
+        g.solve(d)
+        lo, hi = batch.offsets[k], batch.offsets[k + 1]
+        for key in ("n_solution_estimates", "total_walk_length"):
+            assert np.array_equal(d[key].cpu().numpy(), arr[key][lo:hi].cpu().numpy()), (k, key)
+        for key in ("solution_mean", "solution_m2"):
+            assert np.allclose(d[key].cpu().numpy(), arr[key][lo:hi].cpu().numpy(), rtol=1e-12, atol=1e-15), (k, key)
+    # and the batch solves its problems: within a few standard errors of the exact solutions
+    n = arr["n_solution_estimates"].cpu().numpy().astype(np.float64)
+    err = arr["solution_mean"].cpu().numpy() - batch.exact()
+    se = np.sqrt(arr["solution_m2"].cpu().numpy() / np.maximum(n - 1, 1) / n)
+    assert np.mean(np.abs(err) <= 4 * se + 1e-6) > 0.99
+
+
+def test_batched_solve_rejects_scene_ids_outside_the_table(zgpu):
+    import ctypes as C
+    from zombie_gb300 import _lib
+    from zombie_gb300.runner import GpuBatch
+    batch = GpuBatch(P.batched_scenes(n_scenes=2, seed=4, point_scale=0.002, segments=(256, 512)))
+    arr = batch.device_arrays()
+    arr["scene_id"][3] = 7
+    with pytest.raises(_lib.ZgpuError) as e:
+        batch.solve(arr)
+    assert e.value.status == A.ZGPU_ERR_DEVICE_STATE

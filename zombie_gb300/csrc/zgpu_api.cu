@@ -65,7 +65,7 @@ struct zgpu_context {
     // scratch (indexed by role)
     enum { kPt, kNormal, kType, kEq, kDist, kNWalks, kSeed, kFsr, kAligned, kMean, kM2, kN, kLen, kSplits,
            kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
-           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kNumBufs };
+           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
 };
@@ -480,28 +480,15 @@ int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, cons
 namespace {
 
 // zgpu_solve and zgpu_solve_cached: cache == NULL runs the plain walk
-int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
-              const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
-              const zgpu_solve_options* opt, zgpu_cache* cache, float cacheMinDist, zgpu_solve_report* report) {
-    if (!ctx || !q || !pde || !ws || !pts || !stats) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
-    if (solver != ZGPU_SOLVER_WALK_ON_SPHERES && solver != ZGPU_SOLVER_WALK_ON_STARS)
-        return fail(ZGPU_ERR_INVALID_ARG, "unknown solver %d", solver);
-    const int D = q->dim;
-    if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3, got %d", D);
+// checks one scene (queries, PDE, settings) of a solve
+int checkScene(const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_walk_settings* ws, int D) {
+    if (q->dim != D) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be %d, got %d", D, q->dim);
     ZG_TRY(checkBoundary(q->absorbing, D, "absorbing"));
     ZG_TRY(checkBoundary(q->reflecting, D, "reflecting"));
     if (q->reflecting && q->reflecting->kind == ZGPU_BOUNDARY_ABSORBING)
         return fail(ZGPU_ERR_INVALID_ARG, "reflecting slot holds an absorbing boundary");
     if (q->absorbing && q->absorbing->kind != ZGPU_BOUNDARY_ABSORBING)
         return fail(ZGPU_ERR_INVALID_ARG, "absorbing slot holds a reflecting boundary");
-    if (pts->n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative point count");
-    if (pts->memory != stats->memory) return fail(ZGPU_ERR_INVALID_ARG, "points and statistics must share a memory space");
-    if (pts->memory != ZGPU_MEM_HOST && pts->memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
-    if (pts->n > 0 && (!pts->pt || !pts->dist_to_absorbing || !pts->n_walks || !pts->seed))
-        return fail(ZGPU_ERR_INVALID_ARG, "pt, dist_to_absorbing, n_walks and seed are required");
-    if (!stats->solution_mean || !stats->solution_m2 || !stats->n_solution_estimates || !stats->total_walk_length ||
-        !stats->total_splits)
-        return fail(ZGPU_ERR_INVALID_ARG, "statistics arrays are required");
     if (ws->max_walk_length <= 0) return fail(ZGPU_ERR_INVALID_ARG, "max_walk_length must be positive");
     if (!(ws->epsilon_shell_for_absorbing_boundary >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "epsilon shell must be >= 0");
     if (!(ws->splitting_threshold > 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "splitting threshold must be > 0");
@@ -513,6 +500,46 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
     if (pde->robin_coeff_kind == ZGPU_FIELD_ANALYTIC) return fail(ZGPU_ERR_UNSUPPORTED, "robin_coeff must be ZERO or CONSTANT");
     if (pde->solution.n_terms < 0 || pde->solution.n_terms > ZGPU_MAX_TERMS)
         return fail(ZGPU_ERR_INVALID_ARG, "analytic solution has %d terms (max %d)", pde->solution.n_terms, ZGPU_MAX_TERMS);
+    return ZGPU_OK;
+}
+
+SceneDesc sceneOf(const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_walk_settings* ws) {
+    SceneDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.hasAbs = q->absorbing && q->absorbing->nPrims > 0;
+    d.hasRefl = q->reflecting && q->reflecting->nPrims > 0;
+    if (d.hasAbs) d.absorbing = q->absorbing->view;
+    if (d.hasRefl) d.reflecting = q->reflecting->view;
+    for (int i = 0; i < 3; i++) { d.domainMin[i] = q->domain_min[i]; d.domainMax[i] = q->domain_max[i]; }
+    d.ws = *ws;
+    d.pde = *pde;
+    return d;
+}
+
+// zgpu_solve, zgpu_solve_cached and zgpu_solve_batched.  nScenes > 1: points->scene_id
+// selects each point's row of q / pde / ws.
+int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+              const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
+              const zgpu_solve_options* opt, zgpu_cache* cache, float cacheMinDist, zgpu_solve_report* report) {
+    if (!ctx || !q || !pde || !ws || !pts || !stats) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (solver != ZGPU_SOLVER_WALK_ON_SPHERES && solver != ZGPU_SOLVER_WALK_ON_STARS)
+        return fail(ZGPU_ERR_INVALID_ARG, "unknown solver %d", solver);
+    const int D = q->dim;
+    if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3, got %d", D);
+    if (nScenes < 1) return fail(ZGPU_ERR_INVALID_ARG, "n_scenes must be >= 1");
+    const bool batched = nScenes > 1 || (pts->scene_id != nullptr);
+    if (batched && D != 2) return fail(ZGPU_ERR_UNSUPPORTED, "batched many-solve is built for 2D scenes");
+    if (batched && cache) return fail(ZGPU_ERR_UNSUPPORTED, "the neural cache serves single-scene solves");
+    if (batched && pts->n > 0 && !pts->scene_id) return fail(ZGPU_ERR_INVALID_ARG, "scene_id is required with n_scenes > 1");
+    for (int k = 0; k < nScenes; k++) ZG_TRY(checkScene(q + k, pde + k, ws + k, D));
+    if (pts->n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative point count");
+    if (pts->memory != stats->memory) return fail(ZGPU_ERR_INVALID_ARG, "points and statistics must share a memory space");
+    if (pts->memory != ZGPU_MEM_HOST && pts->memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    if (pts->n > 0 && (!pts->pt || !pts->dist_to_absorbing || !pts->n_walks || !pts->seed))
+        return fail(ZGPU_ERR_INVALID_ARG, "pt, dist_to_absorbing, n_walks and seed are required");
+    if (!stats->solution_mean || !stats->solution_m2 || !stats->n_solution_estimates || !stats->total_walk_length ||
+        !stats->total_splits)
+        return fail(ZGPU_ERR_INVALID_ARG, "statistics arrays are required");
 
     ZG_CUDA(cudaSetDevice(ctx->device));
     const int64_t n = pts->n;
@@ -521,15 +548,26 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
     SolveParams P;
     std::memset(&P, 0, sizeof(P));
     P.solver = solver;
-    P.hasAbs = q->absorbing && q->absorbing->nPrims > 0;
-    P.hasRefl = q->reflecting && q->reflecting->nPrims > 0;
-    if (P.hasAbs) P.absorbing = q->absorbing->view;
-    if (P.hasRefl) P.reflecting = q->reflecting->view;
-    for (int i = 0; i < 3; i++) { P.domainMin[i] = q->domain_min[i]; P.domainMax[i] = q->domain_max[i]; }
-    P.ws = *ws;
-    P.pde = *pde;
+    P.sc = sceneOf(q, pde, ws);
     P.nPoints = n;
     using C = zgpu_context;
+    int sceneStack = 8;
+    if (batched) {
+        // the scene table and each point's row in it
+        std::vector<SceneDesc> table(nScenes);
+        for (int k = 0; k < nScenes; k++) {
+            table[k] = sceneOf(q + k, pde + k, ws + k);
+            if (table[k].hasAbs) sceneStack = std::max(sceneStack, table[k].absorbing.stackEntries);
+            if (table[k].hasRefl) sceneStack = std::max(sceneStack, table[k].reflecting.stackEntries);
+            P.batchScreened |= pde[k].absorption_coeff > 0.0f;
+        }
+        SceneDesc* dTable = nullptr;
+        ZG_TRY(scratch<SceneDesc>(ctx, C::kSceneTable, (size_t)nScenes, &dTable));
+        ZG_CUDA(cudaMemcpyAsync(dTable, table.data(), sizeof(SceneDesc) * nScenes, cudaMemcpyHostToDevice, s));
+        P.scenes = dTable;
+        P.nScenes = nScenes;
+        ZG_TRY(stageIn<int>(ctx, C::kSceneId, pts->scene_id, (size_t)n, mem, &P.sceneId));
+    }
     ZG_TRY(stageIn<float>(ctx, C::kPt, pts->pt, (size_t)n * D, mem, &P.pt));
     ZG_TRY(stageIn<float>(ctx, C::kNormal, pts->normal, (size_t)n * D, mem, &P.normal));
     ZG_TRY(stageIn<int>(ctx, C::kType, pts->type, (size_t)n, mem, &P.type));
@@ -566,20 +604,21 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
 
     int threads = opt && opt->block_size > 0 ? opt->block_size : 128;
     if (threads % 32 != 0 || threads > 128) return fail(ZGPU_ERR_INVALID_ARG, "block_size must be a multiple of 32 and <= 128");
-    P.stackEntries = 8;
-    if (P.hasAbs) P.stackEntries = std::max(P.stackEntries, P.absorbing.stackEntries);
-    if (P.hasRefl) P.stackEntries = std::max(P.stackEntries, P.reflecting.stackEntries);
+    P.stackEntries = sceneStack;
+    if (P.sc.hasAbs) P.stackEntries = std::max(P.stackEntries, P.sc.absorbing.stackEntries);
+    if (P.sc.hasRefl) P.stackEntries = std::max(P.stackEntries, P.sc.reflecting.stackEntries);
     // Walk on Spheres on a large scene: each closest-point query is answered by a whole warp
     // (per-query work varies by orders of magnitude between walks, which idles the lanes of
     // a one-lane-per-query traversal); the walk kernel then needs no per-thread stack
     const int queryMode = opt ? opt->query_mode : 0;
     if (queryMode < 0 || queryMode > 2) return fail(ZGPU_ERR_INVALID_ARG, "query_mode must be 0, 1 or 2");
     const int walkStackEntries = P.stackEntries;
-    if (solver == ZGPU_SOLVER_WALK_ON_SPHERES && P.hasAbs)
+    if (solver == ZGPU_SOLVER_WALK_ON_SPHERES && P.sc.hasAbs && !batched)
         P.coop = queryMode == 2 || (queryMode == 0 && D == 3 && q->absorbing->nPrims >= kCoopMinPrims);
     if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
-                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f, threads, P);
+                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f || P.batchScreened,
+                                                                         threads, P);
     P.stackEntries = walkStackEntries;
     int blocks = ctx->numSMs * perSM;
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
@@ -629,7 +668,8 @@ int solveImpl(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, co
     }
     if (errWord)
         return fail(ZGPU_ERR_DEVICE_STATE,
-                    "device error word 0x%x (1: traversal stack, 2: split stack, 16: cache record overflow)", errWord);
+                    "device error word 0x%x (1: traversal stack, 2: split stack, 8: scene id outside the table, "
+                    "16: cache record overflow)", errWord);
     return ZGPU_OK;
 }
 
@@ -640,7 +680,7 @@ extern "C" {
 int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
                const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
                const zgpu_solve_options* opt, zgpu_solve_report* report) {
-    return solveImpl(ctx, solver, q, pde, ws, pts, stats, opt, nullptr, 0.0f, report);
+    return solveImpl(ctx, solver, 1, q, pde, ws, pts, stats, opt, nullptr, 0.0f, report);
 }
 
 int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
@@ -654,7 +694,7 @@ int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_querie
     if (ws->splitting_threshold < FLT_MAX)
         return fail(ZGPU_ERR_UNSUPPORTED, "walk splitting is not supported with the cache (splitting_threshold must be FLT_MAX)");
     if (cacheStream(cache) != ctx->stream) return fail(ZGPU_ERR_INVALID_ARG, "cache belongs to another context");
-    return solveImpl(ctx, solver, q, pde, ws, pts, stats, opt, cache, min_distance, report);
+    return solveImpl(ctx, solver, 1, q, pde, ws, pts, stats, opt, cache, min_distance, report);
 }
 
 int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_geometric_queries* queries,
@@ -662,7 +702,7 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_g
                        zgpu_sample_statistics* stats, const zgpu_solve_options* options, zgpu_solve_report* report) {
     if (n_scenes == 1 && (!points || !points->scene_id))
         return zgpu_solve(ctx, solver, queries, pdes, settings, points, stats, options, report);
-    return fail(ZGPU_ERR_UNSUPPORTED, "batched many-solve is not available in this build");
+    return solveImpl(ctx, solver, n_scenes, queries, pdes, settings, points, stats, options, nullptr, 0.0f, report);
 }
 
 }  // extern "C"

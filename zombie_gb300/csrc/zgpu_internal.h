@@ -17,13 +17,22 @@ enum : int { kCtrNext = 0, kCtrSteps = 1, kCtrEscaped = 2, kCtrExceeded = 3, kCt
 // per-point flags written by the prepare kernel
 enum : int { kPointBoundaryValue = 1, kPointFlip = 2 };
 
-struct SolveParams {
-    int solver;
+// what a walk needs of its problem: boundaries, domain box, settings and PDE
+struct SceneDesc {
     int hasAbs, hasRefl;
     BoundaryView absorbing, reflecting;
     float domainMin[3], domainMax[3];
     zgpu_walk_settings ws;
     zgpu_pde pde;
+};
+
+struct SolveParams {
+    int solver;
+    SceneDesc sc;               // the problem of a single-scene solve
+    const SceneDesc* scenes;    // batched solve: the scene table (device memory) ...
+    const int* sceneId;         // ... and each point's row in it (NULL: single scene)
+    int nScenes;
+    int batchScreened;          // some scene of the table has an absorption coefficient > 0
     int64_t nPoints;
     // sample points (device)
     const float* pt;

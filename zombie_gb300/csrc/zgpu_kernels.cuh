@@ -21,18 +21,28 @@ namespace detail {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-ZG_D bool outsideBox(const SolveParams& P, const float* x, int D) {
+// the scene of point i (batched solves read the point's row of the scene table; a row
+// outside the table is reported and the point is skipped)
+ZG_D const SceneDesc& sceneOfPoint(const SolveParams& P, int64_t i, bool& bad) {
+    bad = false;
+    if (!P.sceneId) return P.sc;
+    const int sid = P.sceneId[i];
+    if (sid < 0 || sid >= P.nScenes) { bad = true; return P.sc; }
+    return P.scenes[sid];
+}
+
+ZG_D bool outsideBox(const SceneDesc& S, const float* x, int D) {
     for (int i = 0; i < D; i++)
-        if (x[i] < P.domainMin[i] || x[i] > P.domainMax[i]) return true;
+        if (x[i] < S.domainMin[i] || x[i] > S.domainMax[i]) return true;
     return false;
 }
 
 template <int D>
-ZG_D float bboxDistance(const SolveParams& P, V<D> x) {
+ZG_D float bboxDistance(const SceneDesc& S, V<D> x) {
     // default computeDistToAbsorbingBoundary (core/geometric_queries.h:212-217)
     V<D> m;
 #pragma unroll
-    for (int i = 0; i < D; i++) m[i] = fminf(P.domainMin[i] - x[i], x[i] - P.domainMax[i]);
+    for (int i = 0; i < D; i++) m[i] = fminf(S.domainMin[i] - x[i], x[i] - S.domainMax[i]);
     return len(m);
 }
 
@@ -48,9 +58,10 @@ ZG_D void storeSplit(float4* slot, V<D> pt, V<D> nrm, V<D> prevDir, float prevDi
     slot[2] = make_float4(v[8], v[9], v[10], v[11]);
 }
 
-template <int D, int SOLVER, bool SCREENED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED>
 struct Walker {
     const SolveParams& P;
+    const SceneDesc* sc;   // the walk's problem: P.sc, or its row of the scene table
     DevicePde<D> pde;
     // walk identity
     int point;
@@ -81,33 +92,39 @@ struct Walker {
     TravStack S;
 
     ZG_D Walker(const SolveParams& p, TravStack s) : P(p), S(s) {
-        pde.p = &P.pde;
+        sc = &P.sc;
+        pde.p = &sc->pde;
         steps = escaped = exceeded = rr = 0;
         err = 0;
-        g.sqrtLambda = sqrtf(fmaxf(P.pde.absorption_coeff, 0.0f));
+        g.sqrtLambda = sqrtf(fmaxf(sc->pde.absorption_coeff, 0.0f));
     }
 
     ZG_D void closestQuery() {
-        if (P.coop && P.hasAbs) { queryPending = true; cpValid = false; return; }
-        if (P.hasAbs) {
-            ClosestHit<D> h = closestPoint<D>(P.absorbing, pt, S, err);
+        if (P.coop && sc->hasAbs) { queryPending = true; cpValid = false; return; }
+        if (sc->hasAbs) {
+            ClosestHit<D> h = closestPoint<D>(sc->absorbing, pt, S, err);
             distAbs = h.d;
             cpPt = h.pt;
-            if (h.slot >= 0) cpN = primNormal<D>(loadPrim<D>(P.absorbing, h.slot));
+            if (h.slot >= 0) cpN = primNormal<D>(loadPrim<D>(sc->absorbing, h.slot));
             cpValid = true;
         } else {
-            distAbs = bboxDistance<D>(P, pt);
+            distAbs = bboxDistance<D>(*sc, pt);
             cpValid = false;
         }
     }
 
     ZG_D void resetGreens() {
         // a new GreensFnBall for every dequeued state (walk_on_spheres.h:376-383, walk_on_stars.h:618-625)
-        g.yukawa = P.pde.absorption_coeff > 0.0f && P.ws.steps_before_applying_tikhonov == 0;
+        g.yukawa = sc->pde.absorption_coeff > 0.0f && sc->ws.steps_before_applying_tikhonov == 0;
     }
 
     ZG_D void start(long long id, int pointIndex) {
         point = pointIndex;
+        if (BATCHED) {
+            sc = P.scenes + __ldg(P.sceneId + point);
+            pde.p = &sc->pde;
+            g.sqrtLambda = sqrtf(fmaxf(sc->pde.absorption_coeff, 0.0f));
+        }
         long long w = id - __ldg(P.walkStart + point);
         rng.seed(__ldg(P.seed + point), (uint64_t)w + (uint64_t)__ldg(P.nPrev + point));
         pt = vload<D>(P.pt + (size_t)point * D);
@@ -140,7 +157,7 @@ struct Walker {
         distAbs = d;
         cpPt = pt;
         if (slot >= 0) {
-            Prim<D> t = loadPrim<D>(P.absorbing, slot);
+            Prim<D> t = loadPrim<D>(sc->absorbing, slot);
             V<D> q;
             closestOnPrim(t, pt, q);
             cpPt = q;
@@ -173,7 +190,7 @@ struct Walker {
 
     // weight window (walk_on_spheres.h:193-226, walk_on_stars.h:309-343); true -> terminated
     ZG_D bool weightWindow() {
-        const float sT = P.ws.splitting_threshold, rT = P.ws.russian_roulette_threshold;
+        const float sT = sc->ws.splitting_threshold, rT = sc->ws.russian_roulette_threshold;
         if (thr > sT) {
             float left = thr - sT;
             thr = sT;
@@ -199,12 +216,12 @@ struct Walker {
             if (code == kRussianRoulette) rr++;
             float term = 0.0f;
             bool payTerminal = code == kReached || (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && code == kExceeded);
-            if (payTerminal && !P.ws.ignore_absorbing_boundary_contribution) {
+            if (payTerminal && !sc->ws.ignore_absorbing_boundary_contribution) {
                 // projectToAbsorbingBoundary then pde.dirichlet (walk_on_spheres.h:294-318, walk_on_stars.h:493-516)
-                if (P.hasAbs) {
+                if (sc->hasAbs) {
                     if (!cpValid && !P.coop) closestQuery();
                     bool aligned = false;
-                    if (P.ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
+                    if (sc->ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
                     term = pde.dirichlet(cpPt, aligned);
                 } else {
                     term = pde.dirichlet(pt, false);
@@ -239,10 +256,10 @@ struct Walker {
 
     // --------------------------------------------------------------- Walk on Spheres step
     ZG_D bool stepWoS() {
-        const zgpu_walk_settings& ws = P.ws;
+        const zgpu_walk_settings& ws = sc->ws;
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) {
             // the terminal value needs the projection: in cooperative mode the warp answers first
-            if (P.coop && P.hasAbs && !cpValid) { pendingCode = kReached; closestQuery(); return true; }
+            if (P.coop && sc->hasAbs && !cpValid) { pendingCode = kReached; closestQuery(); return true; }
             return terminate(kReached);
         }
         if (P.cacheMinDist > 0.0f && wlen > 0 && distAbs >= P.cacheMinDist && cacheTerminate()) return false;
@@ -250,7 +267,7 @@ struct Walker {
         g.update(pt, distAbs);
         if (!ws.ignore_source_contribution) {
             float src;
-            if (P.pde.is_source_constant) {
+            if (sc->pde.is_source_constant) {
                 src = g.norm() * pde.source(pt);
             } else {
                 V<D> d = sampleSphere<D>(rng);
@@ -263,25 +280,25 @@ struct Walker {
         pt = pt + distAbs * dir;
         cpValid = false;
         thr *= g.directionSampledPoissonKernel(pt);
-        if (outsideBox(P, pt.v, D)) return terminate(kEscaped);
+        if (outsideBox(*sc, pt.v, D)) return terminate(kEscaped);
         if (weightWindow()) return terminate(kRussianRoulette);
         wlen++;
         if (wlen >= ws.max_walk_length) {
             // WoS pays the terminal value of the projected point: query first when cooperative
-            if (P.coop && P.hasAbs) { pendingCode = kExceeded; closestQuery(); return true; }
+            if (P.coop && sc->hasAbs) { pendingCode = kExceeded; closestQuery(); return true; }
             return terminate(kExceeded);
         }
-        if (P.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        if (sc->pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
         closestQuery();
         return true;
     }
 
     // --------------------------------------------------------------- Walk on Stars step
     ZG_D bool stepWoSt() {
-        const zgpu_walk_settings& ws = P.ws;
+        const zgpu_walk_settings& ws = sc->ws;
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
         if (P.cacheMinDist > 0.0f && wlen > 0 && !onRefl && distAbs >= P.cacheMinDist) {
-            bool far = !P.hasRefl || closestPoint<D>(P.reflecting, pt, S, err).d >= P.cacheMinDist;
+            bool far = !sc->hasRefl || closestPoint<D>(sc->reflecting, pt, S, err).d >= P.cacheMinDist;
             if (far && cacheTerminate()) return false;
         }
         steps++;
@@ -299,10 +316,10 @@ struct Walker {
             } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
                 R = ws.epsilon_shell_for_reflecting_boundary;
             } else {
-                R = P.hasRefl ? starRadius<D>(P.reflecting, pt, ws.epsilon_shell_for_reflecting_boundary, distAbs,
+                R = sc->hasRefl ? starRadius<D>(sc->reflecting, pt, ws.epsilon_shell_for_reflecting_boundary, distAbs,
                                               ws.silhouette_precision, flip, S, err)
                               : distAbs;
-                if (P.hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
+                if (sc->hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
                     R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
             }
         }
@@ -313,13 +330,13 @@ struct Walker {
         V<D> hitPt, hitN;
         float hitDist;
         bool hit = false;
-        if (P.hasRefl) {
-            RayHit<D> h = intersectRay<D>(P.reflecting, origin, dir, R, false, S, err);
+        if (sc->hasRefl) {
+            RayHit<D> h = intersectRay<D>(sc->reflecting, origin, dir, R, false, S, err);
             if (h.slot >= 0) {
                 hit = true;
                 hitDist = h.t;
                 hitPt = origin + h.t * dir;
-                hitN = primNormal<D>(loadPrim<D>(P.reflecting, h.slot));
+                hitN = primNormal<D>(loadPrim<D>(sc->reflecting, h.slot));
             }
         }
         if (!hit) {
@@ -328,13 +345,13 @@ struct Walker {
             hitN = vzero<D>();
         }
         // reflecting boundary contribution (walk_on_stars.h:190-250)
-        if (P.hasRefl && !ws.ignore_reflecting_boundary_contribution) {
+        if (sc->hasRefl && !ws.ignore_reflecting_boundary_contribution) {
             float u[D];
 #pragma unroll
             for (int i = 0; i < D; i++) u[i] = rng.uniform();
             V<D> bpt, bn;
             float pdf;
-            if (sampleBoundary<D>(P.reflecting, pt, R, u, bpt, bn, pdf)) {
+            if (sampleBoundary<D>(sc->reflecting, pt, R, u, bpt, bn, pdf)) {
                 V<D> toS = bpt - pt;
                 float dS = len(toS);
                 float alpha = onRefl ? 2.0f : 1.0f;
@@ -357,7 +374,7 @@ struct Walker {
                     float sl = len(seg);
                     bool occluded = false;
                     if (sl > 0.0f) {
-                        RayHit<D> oh = intersectRay<D>(P.reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
+                        RayHit<D> oh = intersectRay<D>(sc->reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
                         occluded = oh.slot >= 0;
                     }
                     if (!occluded) {
@@ -385,23 +402,23 @@ struct Walker {
         if (onRefl && prevDist > kFltEps) {
             float kappa = 0.0f;
             V<D> n = nrm;
-            if (!P.pde.are_robin_conditions_pure_neumann) {
+            if (!sc->pde.are_robin_conditions_pure_neumann) {
                 bool f2 = false;
                 if (ws.solve_double_sided) { f2 = dot(prevDir, nrm) < 0.0f; if (f2) n = -n; }
                 kappa = pde.robinCoeff(ws.solve_double_sided && f2);
             }
             float refl = g.reflectance(prevDist, prevDir, n, kappa);
-            float maxRefl = P.pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
+            float maxRefl = sc->pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
             stepThr = fminf(fmaxf(refl, 0.0f), maxRefl);
         } else {
             stepThr = g.directionSampledPoissonKernel(pt);
         }
         thr *= stepThr;
-        if (!onRefl && outsideBox(P, pt.v, D)) return terminate(kEscaped);
+        if (!onRefl && outsideBox(*sc, pt.v, D)) return terminate(kEscaped);
         if (weightWindow()) return terminate(kRussianRoulette);
         wlen++;
         if (wlen >= ws.max_walk_length) return terminate(kExceeded);
-        if (P.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        if (sc->pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
         closestQuery();
         firstStep = false;
         return true;
@@ -437,13 +454,13 @@ ZG_D int warpFindPoint(const SolveParams& P, long long id, int lane) {
     return (int)(lo + 31 - __clz(b));
 }
 
-template <int D, int SOLVER, bool SCREENED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED>
 __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant__ SolveParams P) {
     extern __shared__ int dynStack[];
     TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
                 (int)blockDim.x, P.stackEntries};
     CoopWork* coopWork = reinterpret_cast<CoopWork*>(dynStack + 2 * P.stackEntries * blockDim.x) + (threadIdx.x >> 5);
-    Walker<D, SOLVER, SCREENED> W(P, S);
+    Walker<D, SOLVER, SCREENED, BATCHED> W(P, S);
     W.splitSlots = P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack;
     const int lane = threadIdx.x & 31;
     const long long total = (long long)__ldg(P.walkStart + P.nPoints);
@@ -486,7 +503,7 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
                 for (int i = 0; i < D; i++) x[i] = __shfl_sync(kFull, W.pt[i], src);
                 float d;
                 int slot;
-                coopClosest<D>(P.absorbing, x, *coopWork, lane, d, slot, W.err);
+                coopClosest<D>(P.sc.absorbing, x, *coopWork, lane, d, slot, W.err);
                 if (lane == src) W.setClosest(d, slot);
             }
         }
@@ -517,8 +534,10 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
                 (int)blockDim.x, P.stackEntries};
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.nPoints) return;
-    DevicePde<D> pde; pde.p = &P.pde;
-    const zgpu_walk_settings& ws = P.ws;
+    bool badScene;
+    const SceneDesc& sc = sceneOfPoint(P, i, badScene);
+    DevicePde<D> pde; pde.p = &sc.pde;
+    const zgpu_walk_settings& ws = sc.ws;
     int eq = P.eq ? P.eq[i] : ZGPU_ESTIMATE_SOLUTION;
     int type = P.type ? P.type[i] : ZGPU_SAMPLE_IN_DOMAIN;
     int nPrev = P.statN[i];
@@ -531,7 +550,8 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
     bool aligned = P.aligned ? P.aligned[i] != 0 : false;
     if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && ws.solve_double_sided && type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && aligned)
         flags |= kPointFlip;
-    if (eq == ZGPU_ESTIMATE_SKIP) {
+    if (badScene) atomicOr(P.errorWord, kErrBadInput);
+    if (eq == ZGPU_ESTIMATE_SKIP || badScene) {
         count = 0;
     } else if (type == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) {
         if (nPrev == 0) { flags |= kPointBoundaryValue; P.fsr[i] = 0.0f; }
@@ -549,10 +569,10 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
             } else {
                 uint32_t err = 0;
                 V<D> x = vload<D>(P.pt + (size_t)i * D);
-                r = P.hasRefl ? starRadius<D>(P.reflecting, x, ws.epsilon_shell_for_reflecting_boundary, dAbs,
+                r = sc.hasRefl ? starRadius<D>(sc.reflecting, x, ws.epsilon_shell_for_reflecting_boundary, dAbs,
                                               ws.silhouette_precision, (flags & kPointFlip) != 0, S, err)
                               : dAbs;
-                if (P.hasRefl && ws.epsilon_shell_for_reflecting_boundary <= dAbs)
+                if (sc.hasRefl && ws.epsilon_shell_for_reflecting_boundary <= dAbs)
                     r = fmaxf(kRadiusShrink * r, ws.epsilon_shell_for_reflecting_boundary);
                 if (err) atomicOr(P.errorWord, err);
             }
@@ -568,14 +588,16 @@ template <int D>
 __global__ void finalizeKernel(const __grid_constant__ SolveParams P) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.nPoints) return;
-    DevicePde<D> pde; pde.p = &P.pde;
+    bool badScene;
+    const SceneDesc& sc = sceneOfPoint(P, i, badScene);
+    DevicePde<D> pde; pde.p = &sc.pde;
     int flags = P.pointFlags[i];
     int n2 = P.accN[i];
     double mean2 = 0.0, m22 = 0.0;
     if (flags & kPointBoundaryValue) {
         float v = 0.0f;
-        if (!P.ws.ignore_absorbing_boundary_contribution) {
-            bool aligned = P.ws.solve_double_sided && P.aligned && P.aligned[i] != 0;
+        if (!sc.ws.ignore_absorbing_boundary_contribution) {
+            bool aligned = sc.ws.solve_double_sided && P.aligned && P.aligned[i] != 0;
             v = pde.dirichlet(vload<D>(P.pt + (size_t)i * D), aligned);
         }
         n2 = 1; mean2 = v; m22 = 0.0;
@@ -733,17 +755,30 @@ template <int D, int SOLVER>
 struct WalkLaunch {
     static cudaError_t walk(const SolveParams& p, int blocks, int threads, cudaStream_t s) {
         size_t smem = walkSmemBytes(p, threads);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (p.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true><<<blocks, threads, smem, s>>>(p);
-        else detail::walkKernel<D, SOLVER, false><<<blocks, threads, smem, s>>>(p);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (p.sceneId) {
+            // batched many-solve: each walk reads its row of the scene table (2D scenes)
+            if constexpr (D == 2) {
+                cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (p.batchScreened) detail::walkKernel<D, SOLVER, true, true><<<blocks, threads, smem, s>>>(p);
+                else detail::walkKernel<D, SOLVER, false, true><<<blocks, threads, smem, s>>>(p);
+                return cudaGetLastError();
+            } else {
+                return cudaErrorNotSupported;
+            }
+        }
+        if (p.sc.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true, false><<<blocks, threads, smem, s>>>(p);
+        else detail::walkKernel<D, SOLVER, false, false><<<blocks, threads, smem, s>>>(p);
         return cudaGetLastError();
     }
     static int maxBlocksPerSM(bool screened, int threads, size_t smem) {
         int n = 0;
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        const void* f = screened ? (const void*)detail::walkKernel<D, SOLVER, true> : (const void*)detail::walkKernel<D, SOLVER, false>;
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const void* f = screened ? (const void*)detail::walkKernel<D, SOLVER, true, false>
+                                 : (const void*)detail::walkKernel<D, SOLVER, false, false>;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess) return 1;
         return n > 0 ? n : 1;
     }

@@ -102,17 +102,17 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
         BoundaryView v;
         if (!boundaryView(q->absorbing, &v, &bdim, &bkind) || bdim != D || bkind != ZGPU_BOUNDARY_ABSORBING)
             return fail(ZGPU_ERR_INVALID_ARG, "absorbing boundary does not match the queries");
-        if (v.nPrims > 0) { P.hasAbs = 1; P.absorbing = v; }
+        if (v.nPrims > 0) { P.sc.hasAbs = 1; P.sc.absorbing = v; }
     }
     if (q->reflecting) {
         BoundaryView v;
         if (!boundaryView(q->reflecting, &v, &bdim, &bkind) || bdim != D || bkind == ZGPU_BOUNDARY_ABSORBING)
             return fail(ZGPU_ERR_INVALID_ARG, "reflecting boundary does not match the queries");
-        if (v.nPrims > 0) { P.hasRefl = 1; P.reflecting = v; }
+        if (v.nPrims > 0) { P.sc.hasRefl = 1; P.sc.reflecting = v; }
     }
-    for (int i = 0; i < 3; i++) { P.domainMin[i] = q->domain_min[i]; P.domainMax[i] = q->domain_max[i]; }
-    P.ws = *ws;
-    P.pde = *pde;
+    for (int i = 0; i < 3; i++) { P.sc.domainMin[i] = q->domain_min[i]; P.sc.domainMax[i] = q->domain_max[i]; }
+    P.sc.ws = *ws;
+    P.sc.pde = *pde;
     P.nPoints = n;
     P.pt = pts->pt; P.normal = pts->normal; P.type = pts->type; P.eq = pts->estimation_quantity;
     P.distAbs = pts->dist_to_absorbing; P.nWalks = pts->n_walks; P.seed = pts->seed;
@@ -121,8 +121,8 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
     P.statLen = (long long*)stats->total_walk_length; P.statSplits = (long long*)stats->total_splits;
     P.splitStack = nullptr;   // never touched: splitting is disabled above
     P.stackEntries = 8;
-    if (P.hasAbs) P.stackEntries = P.absorbing.stackEntries > P.stackEntries ? P.absorbing.stackEntries : P.stackEntries;
-    if (P.hasRefl) P.stackEntries = P.reflecting.stackEntries > P.stackEntries ? P.reflecting.stackEntries : P.stackEntries;
+    if (P.sc.hasAbs) P.stackEntries = P.sc.absorbing.stackEntries > P.stackEntries ? P.sc.absorbing.stackEntries : P.stackEntries;
+    if (P.sc.hasRefl) P.stackEntries = P.sc.reflecting.stackEntries > P.stackEntries ? P.sc.reflecting.stackEntries : P.stackEntries;
 
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);

@@ -12,7 +12,9 @@ The compute (walks, training, inference) runs in libzgpu.so; this module is the 
    se_c^2))), is the error the cache adds to a solve; it must stay below `error_bound`,
    otherwise solves fall back to the plain walk.  (The pointwise error of the cache is the
    wrong measure: its high-frequency part averages out over the first step's sphere.)
-4. solve: zgpu_solve_cached when the gate passed, zgpu_solve otherwise.
+4. calibration (before the gate, on other held-out points): the cache's global offset is
+   measured against plain walks and removed from its output bias;
+5. solve: zgpu_solve_cached when the gate passed, zgpu_solve otherwise.
 """
 import time
 
@@ -99,6 +101,25 @@ class NeuralCacheSolver:
         self.gate_report = dict(solve_error=err, mean_difference=float(np.mean(d)), mean_difference_se=mean_se,
                                 cache_pointwise_error=pointwise, bound=self.error_bound, enabled=self.enabled)
         return self.gate_report
+
+    def calibrate(self, x, dist, spp, seed_base=1 << 54):
+        """Removes the cache's global offset, which dominates the error it adds to a solve: the
+        plain walk measures the mean difference d of cached and plain estimates at x; the same
+        cached walks (same seeds, so the same termination points) rerun with the output bias
+        raised by 1 measure the mean throughput tau at termination; the output bias then
+        drops by d / tau.  Returns (d, tau)."""
+        yp, _, _ = self.estimate(x, dist, spp, seed_base, use_cache=False)
+        yc, _, _ = self.estimate(x, dist, spp, seed_base + 1, use_cache=True)
+        p = self.cache.get_parameters()
+        b3 = self.cache.split(p)["b3"]
+        b3 += 1.0
+        self.cache.set_parameters(p)
+        yc1, _, _ = self.estimate(x, dist, spp, seed_base + 1, use_cache=True)
+        tau = float(np.mean(yc1 - yc))
+        d = float(np.mean(yc - yp))
+        b3 -= 1.0 + (d / tau if tau > 1e-6 else 0.0)
+        self.cache.set_parameters(p)
+        return d, tau
 
     def solve_arrays(self, arrays):
         return self.solver.solve_arrays(self.pde, self.settings, arrays, cache=self.cache if self.enabled else None,

@@ -347,6 +347,51 @@ def mixed_wost_2d(n_segments=4096, grid=256, spp=512, sigma=0.0, eps=1e-3, max_l
     return pr
 
 
+def mixed_star_scene(seed, n_segments, n_points, spp, eps=1e-3, max_len=1024):
+    """One scene of the batched many-solve: a seeded random star polygon (about the origin)
+    with Neumann conditions on the half theta in [a, a + pi) for a random split angle a,
+    Dirichlet on the rest, u = e^x cos y + 0.25 (x^2 + y^2), f = -1; n_points uniform
+    interior points clear of the epsilon shell; spp walks each."""
+    rng = np.random.default_rng(seed)
+    amp, freq, phase = rng.uniform(0.1, 0.35), int(rng.integers(3, 8)), rng.uniform(0, 2 * np.pi)
+    split = rng.uniform(0, 2 * np.pi)
+    pr = Problem(2, f"mixed_star_s{seed}_n{n_segments}_p{n_points}_w{spp}")
+    pos, idx = star_polygon(n_segments, amp=amp, freq=freq, phase=phase)
+    absorbing, reflecting = partition_boundary_mesh(
+        lambda m: np.mod(np.arctan2(m[:, 1], m[:, 0]) - split, 2 * np.pi) < np.pi, pos, idx)
+    pr.absorbing, pr.reflecting = absorbing, reflecting
+    pr.domain_min, pr.domain_max = bounding_box(pos)
+    pr.solution = solution_expcos(0.25)
+    pr.pde = make_pde(pr.solution, sigma=0.0, robin=True, constant_source=-1.0)
+    pr.settings = default_walk_settings(eps_abs=eps, eps_refl=eps, max_len=max_len)
+    pts = []
+    have = 0
+    while have < n_points:
+        p = rng.uniform(pr.domain_min[:2], pr.domain_max[:2], (2 * (n_points - have) + 64, 2))
+        inside, rad = polygon_inside_and_radius(p, pos)
+        keep = inside & (rad - np.linalg.norm(p, axis=1) > 4 * eps)
+        pts.append(p[keep]); have += int(keep.sum())
+    pr.points = np.concatenate(pts)[:n_points].astype(np.float32)
+    pr.n_walks = np.full(n_points, spp, np.int32)
+    pr.solver = A.ZGPU_SOLVER_WALK_ON_STARS
+    return pr
+
+
+def batched_scenes(n_scenes=64, seed=0, point_scale=1.0, segments=(256, 16384), points=(10_000, 500_000),
+                   spps=(64, 128, 256, 512)):
+    """The batched many-solve workload: n_scenes independent 2D mixed problems with segment
+    counts log-uniform in `segments`, evaluation point counts log-uniform in `points` (times
+    point_scale) and walk counts uniform over `spps`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_scenes):
+        nseg = int(np.exp(rng.uniform(np.log(segments[0]), np.log(segments[1]))))
+        npts = max(16, int(point_scale * np.exp(rng.uniform(np.log(points[0]), np.log(points[1])))))
+        spp = int(rng.choice(spps))
+        out.append(mixed_star_scene(int(rng.integers(1 << 31)), nseg, npts, spp))
+    return out
+
+
 def _interior_grid_2d(pos, lo, hi, grid, eps):
     xs = lo[0] + (np.arange(grid) + 0.5) * (hi[0] - lo[0]) / grid
     ys = lo[1] + (np.arange(grid) + 0.5) * (hi[1] - lo[1]) / grid

@@ -74,3 +74,53 @@ def summarize(arrays, exact):
     err = mean - exact
     return dict(rmse=float(np.sqrt(np.mean(err ** 2))), mean=mean, se=se, n=n, err=err,
                 mean_walk_length=float(host(arrays["total_walk_length"]).sum() / max(1.0, n.sum())))
+
+
+class GpuBatch:
+    """Independent problems solved in one launch (zgpu_solve_batched): each point carries the
+    row of its problem in the scene table.  Per-point seeds are those of the single-problem
+    solves, so a batched solve runs the same walks as solving each problem alone."""
+
+    def __init__(self, problems, context=None, seed_base=0x5eed, options=None):
+        from . import _abi as A
+        self.ctx = context or default_context()
+        self.problems = [GpuProblem(p, context=self.ctx, seed_base=seed_base) for p in problems]
+        self.solver_id = problems[0].solver
+        if any(p.solver != self.solver_id for p in problems) or any(p.dim != 2 for p in problems):
+            raise ValueError("a batch holds 2D problems of one solver")
+        self.options = options
+        n = len(self.problems)
+        self.q = (A.GeometricQueriesC * n)(*[g.queries.to_c() for g in self.problems])
+        self.pde = (A.Pde * n)(*[g.pde.to_c() for g in self.problems])
+        self.ws = (A.WalkSettingsC * n)(*[g.problem.settings for g in self.problems])
+        self.offsets = np.cumsum([0] + [g.points.shape[0] for g in self.problems])
+
+    @property
+    def n_points(self):
+        return int(self.offsets[-1])
+
+    def device_arrays(self):
+        import torch
+        parts = [g.device_arrays() for g in self.problems]
+        dev = {}
+        for k in parts[0].arrays:
+            dev[k] = torch.cat([p.arrays[k] for p in parts])
+        sid = np.concatenate([np.full(g.points.shape[0], i, np.int32) for i, g in enumerate(self.problems)])
+        dev["scene_id"] = torch.from_numpy(sid).to(dev["pt"].device)
+        return SampleArrays(**dev)
+
+    def solve(self, arrays, options=None):
+        import ctypes as C
+        from . import _abi as A
+        from ._lib import check, lib
+        from .api import SolveReport
+        sp, st = arrays.to_c()
+        opt = options or self.options
+        rep = A.SolveReport()
+        check(lib().zgpu_solve_batched(self.ctx.h, self.solver_id, len(self.problems), self.q, self.pde, self.ws,
+                                       C.byref(sp), C.byref(st), C.byref(opt) if opt is not None else None,
+                                       C.byref(rep)))
+        return SolveReport(rep)
+
+    def exact(self):
+        return np.concatenate([g.problem.exact() for g in self.problems])
