@@ -40,6 +40,13 @@ WORKLOADS = {
                                 desc="profiling case: 3D Robin WoSt, icosphere L6, 4096 points, 16 spp, kappa=2"),
     "screened_wos_3d": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=4_000_000, spp=64),
                             desc="3D screened Poisson WoS sigma=4, icosphere L8 (1,310,720 tris), 4M points, 64 spp"),
+    "batched_64": dict(fn="batched_scenes", kw=dict(n_scenes=64, seed=0, point_scale=0.1),
+                       desc="64 independent 2D mixed WoSt problems in one launch: seeded star polygons, "
+                            "256-16384 segments, 1k-50k points (log-uniform; a tenth of the 10k-500k of the "
+                            "full workload), 64-512 walks/point"),
+    "batched_64_full": dict(fn="batched_scenes", kw=dict(n_scenes=64, seed=0),
+                            desc="64 independent 2D mixed WoSt problems in one launch: seeded star polygons, "
+                                 "256-16384 segments, 10k-500k points (log-uniform), 64-512 walks/point"),
     "screened_wos_3d_small": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=16384, spp=4),
                                   desc="profiling case: 3D screened WoS sigma=4, icosphere L8, 16384 points, 4 spp"),
 }
@@ -205,6 +212,54 @@ def make_problem(name):
     from zombie_gb300 import problems as P
     w = WORKLOADS[name]
     return getattr(P, w["fn"])(**w["kw"]), w["desc"]
+
+
+def run_batched(args):
+    """The batched many-solve workload: all scenes in one zgpu_solve_batched call per step."""
+    import torch
+    from zombie_gb300 import Context
+    from zombie_gb300.runner import GpuBatch
+    pr_list, desc = make_problem(args.workload)
+    ctx = Context(0)
+    batch = GpuBatch(pr_list, context=ctx)
+    dev = batch.device_arrays()
+    zero_keys = ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
+                 "first_sphere_radius")
+    for _ in range(args.warmup):
+        for k in zero_keys:
+            dev[k].zero_()
+        batch.solve(dev)
+    torch.cuda.synchronize()
+    steps, kms = 0, []
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            for k in zero_keys:
+                dev[k].zero_()
+            rep = batch.solve(dev)
+            steps += rep.total_steps
+            kms.append(rep.kernel_ms)
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    value = steps / (sum(kms) / 1e3)
+    harr = batch.host_arrays()
+    t1 = time.perf_counter()
+    rep = batch.solve(harr)
+    e2e_s = time.perf_counter() - t1
+    n = dev["n_solution_estimates"].cpu().numpy().astype(np.float64)
+    err = dev["solution_mean"].cpu().numpy() - batch.exact()
+    line = {"metric": "walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum(kms) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "scenes": len(pr_list),
+                       "points": batch.n_points, "walks": int(sum(int(p.n_walks.sum()) for p in pr_list)),
+                       "l2": "inputs larger than L2"},
+            "rmse_vs_exact": float(np.sqrt(np.mean(err ** 2))),
+            "e2e": {"value": rep.total_steps / e2e_s, "unit": "walk-steps/s",
+                    "h2d_bytes_per_step": int(sum(v.nbytes for v in harr.arrays.values())),
+                    "d2h_bytes_per_step": int(sum(harr.arrays[k].nbytes for k in zero_keys if k in harr.arrays))},
+            "gpu_launches": 6 * args.steps, "clocks": clk.summary(), "wall_s": wall}
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(args):
@@ -456,6 +511,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload.startswith("batched"):
+        run_batched(args)
     else:
         run_gpu(args)
 

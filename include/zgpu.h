@@ -297,6 +297,18 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
                        zgpu_sample_statistics* stats, const zgpu_solve_options* options,
                        zgpu_solve_report* report);
 
+/*
+ * Autotuner (no counterpart in the reference): times launch configurations (block size
+ * 32/64/128 x blocks per SM auto/2/4, and for Walk on Spheres the query mode) on a stride
+ * sample of `sample_points` points with `sample_walks` walks each, and writes the fastest
+ * into `out_options`.  Results are cached in the context per scene signature (dimension,
+ * solver, log2 primitive counts, reflecting kind, screening); a cached answer returns with
+ * *best_steps_per_s = -1.  The BVH width is fixed at 4 in this build.
+ */
+int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries, const zgpu_pde* pde,
+                  const zgpu_walk_settings* settings, const zgpu_sample_points* points, int32_t sample_points,
+                  int32_t sample_walks, zgpu_solve_options* out_options, float* best_steps_per_s);
+
 /* ------------------------- allocation-free solve -------------------------- */
 /*
  * zgpu_solve_static: a variant of zgpu_solve that allocates nothing.  No counterpart in the

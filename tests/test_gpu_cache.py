@@ -85,8 +85,9 @@ def test_cache_forward_and_gradients_match_oracle(zgpu, oracle, dim):
 
 
 def test_cache_training_fits_a_smooth_field(zgpu):
-    # a smooth field wants a coarse grid: at resolution 64 every cell holds many samples
-    c = _cache(3, log2T=16, max_resolution=64.0, learning_rate_grid=1e-2, learning_rate_mlp=5e-3)
+    # a smooth field wants a coarse grid: at resolution 64 every cell holds many samples, and a
+    # 2^19 table indexes every level densely (no hash collisions)
+    c = _cache(3, log2T=19, max_resolution=64.0, learning_rate_grid=1e-2, learning_rate_mlp=5e-3)
     rng = np.random.default_rng(4)
     n = 1 << 17
     x = rng.uniform(-1.2, 1.2, (n, 3)).astype(np.float32)

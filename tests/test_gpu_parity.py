@@ -392,3 +392,31 @@ def test_batched_solve_rejects_scene_ids_outside_the_table(zgpu):
     with pytest.raises(_lib.ZgpuError) as e:
         batch.solve(arr)
     assert e.value.status == A.ZGPU_ERR_DEVICE_STATE
+
+
+def test_autotuned_and_graph_replayed_solves_run_the_same_walks(zgpu):
+    """The autotuner's launch configuration and a solve replayed from its captured CUDA graph
+    run the walks of the default launch (walk randomness depends on walk ids only)."""
+    from zombie_gb300.runner import GpuProblem
+    gp = GpuProblem(P.mixed_wost_2d(n_segments=1024, grid=32, spp=64))
+    ref = gp.device_arrays()
+    gp.solve(ref)
+    opt, rate = gp.solver.autotune(gp.pde, gp.problem.settings, gp.device_arrays(), sample_points=512, sample_walks=8)
+    assert opt.block_size in (32, 64, 128) and rate > 0
+    again, _ = gp.solver.autotune(gp.pde, gp.problem.settings, gp.device_arrays())
+    assert (again.block_size, again.blocks_per_sm) == (opt.block_size, opt.blocks_per_sm)   # cached per scene
+    tuned = gp.device_arrays()
+    gp.solve(tuned, options=opt)
+    opt.use_graph = 1
+    graph = gp.device_arrays()
+    for call in range(3):                      # the first call captures, the others replay
+        for k in ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
+                  "first_sphere_radius"):
+            graph[k].zero_()
+        rep = gp.solve(graph, options=opt)
+        assert rep.error_word == 0 and rep.total_steps > 0
+        for d in (tuned, graph):
+            for k in ("n_solution_estimates", "total_walk_length"):
+                assert np.array_equal(ref[k].cpu().numpy(), d[k].cpu().numpy()), (call, k)
+            for k in ("solution_mean", "solution_m2"):
+                assert np.allclose(ref[k].cpu().numpy(), d[k].cpu().numpy(), rtol=1e-12, atol=1e-15), (call, k)

@@ -644,6 +644,20 @@ class _Solver:
         self.last_report = SolveReport(rep)
         return self.last_report
 
+    def autotune(self, pde, walk_settings, arrays, sample_points=4096, sample_walks=16):
+        """Fastest launch configuration for this problem (zgpu_autotune); also becomes this
+        solver's default options."""
+        q = self.queries.to_c()
+        p = pde.to_c() if isinstance(pde, PDE) else pde
+        ws = walk_settings.to_c() if isinstance(walk_settings, WalkSettings) else walk_settings
+        sp, _ = arrays.to_c()
+        opt = A.SolveOptions()
+        rate = C.c_float()
+        check(lib().zgpu_autotune(self.ctx.h, self.solver_id, C.byref(q), C.byref(p), C.byref(ws), C.byref(sp),
+                                  int(sample_points), int(sample_walks), C.byref(opt), C.byref(rate)))
+        self.options = opt
+        return opt, rate.value
+
     def solve(self, pde, walk_settings, n_walks, sample_pts, statistics, run_single_threaded=False,
               report_progress=None):
         """solve(pde, walk_settings, n_walks, sample_pts, statistics[, run_single_threaded, report_progress])

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,12 @@ struct zgpu_context {
            kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
+    // use_graph: the captured prepare/scan/walk/finalize sequence, replayed while the solve's
+    // parameters (pointers, sizes, settings) are those it was captured with
+    cudaGraphExec_t graphExec = nullptr;
+    std::vector<unsigned char> graphKey;
+    // autotuner results by scene signature
+    std::map<std::string, zgpu_solve_options> tuned;
 };
 
 struct zgpu_boundary {
@@ -183,6 +190,7 @@ int zgpu_context_destroy(zgpu_context* c) {
     for (auto& b : c->bufs) if (b.p) cudaFree(b.p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
+    if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return ZGPU_OK;
@@ -624,6 +632,34 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
 
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
+    if (opt && opt->use_graph && !cache) {
+        // the four launches as one CUDA graph: re-captured when anything they read changed
+        SolveParams Pwalk = P;
+        if (Pwalk.coop) Pwalk.stackEntries = 0;
+        std::vector<unsigned char> key(sizeof(SolveParams) * 2 + 4 * sizeof(int64_t));
+        const int64_t dims[4] = {(int64_t)D, (int64_t)blocks, (int64_t)threads, (int64_t)(intptr_t)blockSums};
+        std::memcpy(key.data(), &P, sizeof(P));
+        std::memcpy(key.data() + sizeof(P), &Pwalk, sizeof(P));
+        std::memcpy(key.data() + 2 * sizeof(P), dims, sizeof(dims));
+        if (!ctx->graphExec || ctx->graphKey != key) {
+            if (ctx->graphExec) { cudaGraphExecDestroy(ctx->graphExec); ctx->graphExec = nullptr; }
+            cudaGraph_t g = nullptr;
+            ZG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            cudaError_t e = launchPrepare(P, D, s);
+            if (e == cudaSuccess) e = launchScan(P.walkStart, n, blockSums, s);
+            if (e == cudaSuccess && n > 0) e = launchWalk(Pwalk, D, blocks, threads, s);
+            if (e == cudaSuccess) e = launchFinalize(Pwalk, D, s);
+            cudaError_t e2 = cudaStreamEndCapture(s, &g);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->graphExec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            ZG_CUDA(e);
+            ctx->graphKey = key;
+        }
+        ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
+        ZG_CUDA(cudaGraphLaunch(ctx->graphExec, s));
+        ZG_CUDA(cudaEventRecord(ctx->ev[2], s));
+    } else {
     ZG_CUDA(launchPrepare(P, D, s));
     ZG_CUDA(launchScan(P.walkStart, n, blockSums, s));
     if (cache) {
@@ -643,6 +679,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
                                       P.accN, P.accLen, s));
     ZG_CUDA(cudaEventRecord(ctx->ev[2], s));
     ZG_CUDA(launchFinalize(P, D, s));
+    }
     ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
     ZG_TRY(stageOut<double>(ctx, P.statMean, stats->solution_mean, (size_t)n, mem));
     ZG_TRY(stageOut<double>(ctx, P.statM2, stats->solution_m2, (size_t)n, mem));
@@ -695,6 +732,102 @@ int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_querie
         return fail(ZGPU_ERR_UNSUPPORTED, "walk splitting is not supported with the cache (splitting_threshold must be FLT_MAX)");
     if (cacheStream(cache) != ctx->stream) return fail(ZGPU_ERR_INVALID_ARG, "cache belongs to another context");
     return solveImpl(ctx, solver, 1, q, pde, ws, pts, stats, opt, cache, min_distance, report);
+}
+
+// Autotuner: times candidate launch configurations on a stride sample of the points and
+// keeps the fastest (walk steps per kernel millisecond) per scene signature.
+int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
+                  const zgpu_walk_settings* ws, const zgpu_sample_points* pts, int32_t sample_points,
+                  int32_t sample_walks, zgpu_solve_options* out, float* best_rate) {
+    if (!ctx || !q || !pde || !ws || !pts || !out) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (pts->n <= 0) return fail(ZGPU_ERR_INVALID_ARG, "autotuning needs points");
+    if (sample_points <= 0 || sample_walks <= 0) return fail(ZGPU_ERR_INVALID_ARG, "sample sizes must be positive");
+    const int D = q->dim;
+    if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3");
+    auto lg = [](int64_t v) { int b = 0; while (v > 1) { v >>= 1; b++; } return b; };
+    char sig[160];
+    std::snprintf(sig, sizeof(sig), "D%d s%d a%d r%d k%d x%d", D, solver,
+                  lg(q->absorbing ? q->absorbing->nPrims : 0), lg(q->reflecting ? q->reflecting->nPrims : 0),
+                  q->reflecting ? q->reflecting->kind : -1, pde->absorption_coeff > 0.0f ? 1 : 0);
+    auto it = ctx->tuned.find(sig);
+    if (it != ctx->tuned.end()) { *out = it->second; if (best_rate) *best_rate = -1.0f; return ZGPU_OK; }
+    // stride sample of the points, staged on the host
+    const int64_t n = pts->n;
+    const int64_t m = std::min<int64_t>(n, sample_points);
+    const int64_t stride = n / m;
+    auto pull = [&](const void* src, size_t elem, std::vector<unsigned char>& all) -> int {
+        all.assign((size_t)n * elem, 0);
+        if (!src) { all.clear(); return ZGPU_OK; }
+        if (pts->memory == ZGPU_MEM_DEVICE) { ZG_CUDA(cudaMemcpy(all.data(), src, all.size(), cudaMemcpyDeviceToHost)); }
+        else std::memcpy(all.data(), src, all.size());
+        return ZGPU_OK;
+    };
+    std::vector<unsigned char> aPt, aN, aT, aD, aS, aA;
+    ZG_TRY(pull(pts->pt, sizeof(float) * D, aPt));
+    ZG_TRY(pull(pts->normal, sizeof(float) * D, aN));
+    ZG_TRY(pull(pts->type, sizeof(int32_t), aT));
+    ZG_TRY(pull(pts->dist_to_absorbing, sizeof(float), aD));
+    ZG_TRY(pull(pts->seed, sizeof(uint64_t), aS));
+    ZG_TRY(pull(pts->estimate_normal_aligned, sizeof(int32_t), aA));
+    auto pick = [&](const std::vector<unsigned char>& all, size_t elem) {
+        std::vector<unsigned char> o;
+        if (all.empty()) return o;
+        o.resize((size_t)m * elem);
+        for (int64_t i = 0; i < m; i++) std::memcpy(&o[(size_t)i * elem], &all[(size_t)(i * stride) * elem], elem);
+        return o;
+    };
+    std::vector<unsigned char> sPt = pick(aPt, sizeof(float) * D), sN = pick(aN, sizeof(float) * D),
+                               sT = pick(aT, 4), sD = pick(aD, 4), sS = pick(aS, 8), sA = pick(aA, 4);
+    std::vector<int32_t> nw((size_t)m, sample_walks), cnt((size_t)m);
+    std::vector<double> mean((size_t)m), m2((size_t)m);
+    std::vector<long long> len((size_t)m), spl((size_t)m);
+    zgpu_sample_points sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.n = m; sp.memory = ZGPU_MEM_HOST;
+    sp.pt = (const float*)sPt.data();
+    sp.normal = sN.empty() ? nullptr : (const float*)sN.data();
+    sp.type = sT.empty() ? nullptr : (const int32_t*)sT.data();
+    sp.dist_to_absorbing = (const float*)sD.data();
+    sp.seed = (const uint64_t*)sS.data();
+    sp.estimate_normal_aligned = sA.empty() ? nullptr : (const int32_t*)sA.data();
+    sp.n_walks = nw.data();
+    zgpu_sample_statistics st;
+    std::memset(&st, 0, sizeof(st));
+    st.memory = ZGPU_MEM_HOST;
+    st.solution_mean = mean.data(); st.solution_m2 = m2.data(); st.n_solution_estimates = cnt.data();
+    st.total_walk_length = (int64_t*)len.data(); st.total_splits = (int64_t*)spl.data();
+    const bool wos = solver == ZGPU_SOLVER_WALK_ON_SPHERES && q->absorbing && q->absorbing->nPrims > 0;
+    const int threadsC[3] = {32, 64, 128};
+    const int perSMC[3] = {0, 2, 4};
+    zgpu_solve_options best;
+    std::memset(&best, 0, sizeof(best));
+    double bestRate = -1.0;
+    for (int qm = wos ? 1 : 0; qm <= (wos ? 2 : 0); qm++)
+        for (int ti = 0; ti < 3; ti++)
+            for (int pi = 0; pi < 3; pi++) {
+                zgpu_solve_options o;
+                std::memset(&o, 0, sizeof(o));
+                o.block_size = threadsC[ti];
+                o.blocks_per_sm = perSMC[pi];
+                o.query_mode = qm;
+                double rate = 0.0;
+                for (int rep = 0; rep < 2; rep++) {
+                    std::fill(cnt.begin(), cnt.end(), 0);
+                    std::fill(mean.begin(), mean.end(), 0.0);
+                    std::fill(m2.begin(), m2.end(), 0.0);
+                    std::fill(len.begin(), len.end(), 0);
+                    std::fill(spl.begin(), spl.end(), 0);
+                    zgpu_solve_report r;
+                    int stt = solveImpl(ctx, solver, 1, q, pde, ws, &sp, &st, &o, nullptr, 0.0f, &r);
+                    if (stt != ZGPU_OK) return stt;
+                    if (r.kernel_ms > 0.0f) rate = std::max(rate, (double)r.total_steps / r.kernel_ms);
+                }
+                if (rate > bestRate) { bestRate = rate; best = o; }
+            }
+    ctx->tuned[sig] = best;
+    *out = best;
+    if (best_rate) *best_rate = (float)(bestRate * 1e3);
+    return ZGPU_OK;
 }
 
 int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_geometric_queries* queries,

@@ -109,6 +109,12 @@ class GpuBatch:
         dev["scene_id"] = torch.from_numpy(sid).to(dev["pt"].device)
         return SampleArrays(**dev)
 
+    def host_arrays(self):
+        parts = [g.host_arrays() for g in self.problems]
+        arr = {k: np.concatenate([p.arrays[k] for p in parts]) for k in parts[0].arrays}
+        arr["scene_id"] = np.concatenate([np.full(g.points.shape[0], i, np.int32) for i, g in enumerate(self.problems)])
+        return SampleArrays(**arr)
+
     def solve(self, arrays, options=None):
         import ctypes as C
         from . import _abi as A
