@@ -171,8 +171,9 @@ typedef struct zgpu_solve_options {
     int32_t block_size;        /* 0 -> autotuned / default */
     int32_t blocks_per_sm;     /* 0 -> occupancy-derived */
     int32_t use_graph;         /* capture prepare+walk+finalize in a CUDA graph and replay */
-    int32_t query_mode;        /* closest-point queries of Walk on Spheres: 0 auto, 1 one lane per
-                                  query, 2 the whole warp per query (large scenes) */
+    int32_t query_mode;        /* closest-point queries of Walk on Spheres and Robin star radii of
+                                  Walk on Stars: 0 auto, 1 one lane per query, 2 the whole warp
+                                  per query (large scenes) */
     int64_t step_budget;       /* per-walk-state hard cap on device loop iterations (0 -> max_walk_length+1) */
 } zgpu_solve_options;
 

@@ -94,9 +94,12 @@ def test_cache_training_fits_a_smooth_field(zgpu):
     f = lambda q: np.exp(0.5 * q[:, 0]) * np.cos(q[:, 1]) + q[:, 2] ** 2
     t = f(x).astype(np.float32)
     first = c.train(x, t, steps=20, batch_size=1 << 14)
-    c.train(x, t, steps=600, batch_size=1 << 14)
-    last = c.train(x, t, steps=20, batch_size=1 << 14)
-    assert last < 1e-3 * first
+    c.train(x, t, steps=500, batch_size=1 << 14)
+    # Adam at a fixed step keeps jittering around the minimum: decay it to converge
+    for scale in (0.3, 0.1, 0.03):
+        c.set_learning_rates(1e-2 * scale, 5e-3 * scale)
+        last = c.train(x, t, steps=150, batch_size=1 << 14)
+    assert last < 1e-4 * first
     xt = rng.uniform(-1.0, 1.0, (20000, 3)).astype(np.float32)
     err = c.evaluate(xt) - f(xt)
     assert np.sqrt(np.mean(err ** 2)) < 1e-2

@@ -623,6 +623,10 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     const int walkStackEntries = P.stackEntries;
     if (solver == ZGPU_SOLVER_WALK_ON_SPHERES && P.sc.hasAbs && !batched)
         P.coop = queryMode == 2 || (queryMode == 0 && D == 3 && q->absorbing->nPrims >= kCoopMinPrims);
+    // Walk on Stars with a Robin boundary: its star radius visits thousands of primitives from
+    // interior points under the reflectance bounds, the case the warp-wide traversal serves
+    if (solver == ZGPU_SOLVER_WALK_ON_STARS && P.sc.hasRefl && q->reflecting->kind == ZGPU_BOUNDARY_ROBIN && !batched)
+        P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
     if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
                                               : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f || P.batchScreened,

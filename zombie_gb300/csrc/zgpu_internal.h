@@ -73,12 +73,16 @@ struct SolveParams {
     // Walk on Spheres: closest-point queries answered by the whole warp (CoopWork per warp in
     // shared memory after the per-thread stacks)
     int coop;
+    // Walk on Stars on a Robin boundary: star radii answered by the whole warp
+    int coopStar;
 };
 
 constexpr int kSplitStack = 8;
 // Walk on Spheres in 3D answers closest-point queries with a whole warp from this many
 // absorbing primitives on (query_mode 0)
 constexpr int kCoopMinPrims = 20000;
+// Walk on Stars in 3D answers Robin star radii with a whole warp from this many primitives
+constexpr int kCoopStarMinPrims = 4096;
 
 // kernels / launchers (zgpu_walk.cu)
 cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);

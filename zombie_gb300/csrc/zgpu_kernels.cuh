@@ -81,6 +81,9 @@ struct Walker {
     float distAbs, fsr;
     bool firstStep, cpValid;
     bool queryPending;      // cooperative mode: the closest-point query of this state is due
+    bool radiusPending;     // cooperative mode: the Robin star radius of this step is due
+    bool radiusReady;       // ... and answered (pendingR) -- the step resumes from there
+    float pendingR;
     int pendingCode;        // cooperative mode: terminate(code) once the query is answered (-1: none)
     V<D> cpPt, cpN;
     Greens<D, SCREENED> g;
@@ -148,6 +151,8 @@ struct Walker {
         firstStep = true;
         cpValid = false;
         queryPending = false;
+        radiusPending = false;
+        radiusReady = false;
         pendingCode = -1;
         resetGreens();
     }
@@ -294,14 +299,22 @@ struct Walker {
     }
 
     // --------------------------------------------------------------- Walk on Stars step
+    // answer of a cooperative Robin star-radius query (the shrink of walk_on_stars.h:393-397)
+    ZG_D void setStarRadius(float r) {
+        const float eps = sc->ws.epsilon_shell_for_reflecting_boundary;
+        pendingR = eps <= distAbs ? fmaxf(kRadiusShrink * r, eps) : r;
+        radiusPending = false;
+        radiusReady = true;
+    }
+
     ZG_D bool stepWoSt() {
         const zgpu_walk_settings& ws = sc->ws;
+        if (radiusReady) { radiusReady = false; return stepWoStFrom(pendingR); }
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
         if (P.cacheMinDist > 0.0f && wlen > 0 && !onRefl && distAbs >= P.cacheMinDist) {
             bool far = !sc->hasRefl || closestPoint<D>(sc->reflecting, pt, S, err).d >= P.cacheMinDist;
             if (far && cacheTerminate()) return false;
         }
-        steps++;
         float R;
         if (firstStep && fsr > 0.0f) {
             R = fsr;
@@ -315,6 +328,9 @@ struct Walker {
                 R = distAbs;
             } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
                 R = ws.epsilon_shell_for_reflecting_boundary;
+            } else if (P.coopStar && sc->hasRefl) {
+                radiusPending = true;          // the warp answers, the step resumes in stepWoStFrom
+                return true;
             } else {
                 R = sc->hasRefl ? starRadius<D>(sc->reflecting, pt, ws.epsilon_shell_for_reflecting_boundary, distAbs,
                                               ws.silhouette_precision, flip, S, err)
@@ -323,6 +339,13 @@ struct Walker {
                     R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
             }
         }
+        return stepWoStFrom(R);
+    }
+
+    // the Walk on Stars step from its star radius R on
+    __device__ __noinline__ bool stepWoStFrom(float R) {
+        const zgpu_walk_settings& ws = sc->ws;
+        steps++;
         g.update(pt, R);
         V<D> dir = sampleSphere<D>(rng);
         if (onRefl && dot(nrm, dir) > 0.0f) dir = -dir;
@@ -492,6 +515,22 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
         }
         if (!__any_sync(kFull, active)) break;
         if (active) active = W.step();
+        if (SOLVER == ZGPU_SOLVER_WALK_ON_STARS && P.coopStar) {
+            // Robin star radii of this round, one at a time with the whole warp
+            unsigned qm = __ballot_sync(kFull, active && W.radiusPending);
+            while (qm) {
+                const int src = __ffs(qm) - 1;
+                qm &= qm - 1;
+                V<D> x;
+#pragma unroll
+                for (int i = 0; i < D; i++) x[i] = __shfl_sync(kFull, W.pt[i], src);
+                const float maxR = __shfl_sync(kFull, W.distAbs, src);
+                const bool flip = __shfl_sync(kFull, (int)W.flip, src) != 0;
+                const float r = coopRobinStarRadius<D>(P.sc.reflecting, x, P.sc.ws.epsilon_shell_for_reflecting_boundary,
+                                                       maxR, P.sc.ws.silhouette_precision, flip, *coopWork, lane, W.err);
+                if (lane == src) W.setStarRadius(r);
+            }
+        }
         if (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && P.coop) {
             // closest-point queries of this round, one at a time with the whole warp
             unsigned qm = __ballot_sync(kFull, active && W.queryPending);
@@ -747,7 +786,7 @@ inline unsigned gridFor(int64_t n, int t) { return (unsigned)((n + t - 1) / t); 
 inline size_t smemBytes(int stackEntries, int threads) { return (size_t)stackEntries * threads * 8; }
 // walk kernel: per-thread stacks, then one CoopWork per warp in cooperative mode
 inline size_t walkSmemBytes(const SolveParams& p, int threads) {
-    return smemBytes(p.stackEntries, threads) + (p.coop ? sizeof(CoopWork) * (size_t)(threads / 32) : 0);
+    return smemBytes(p.stackEntries, threads) + ((p.coop || p.coopStar) ? sizeof(CoopWork) * (size_t)(threads / 32) : 0);
 }
 
 // walk kernel launchers, explicitly instantiated per (dimension, solver) in zgpu_walk_<D>d_<solver>.cu

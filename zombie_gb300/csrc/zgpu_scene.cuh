@@ -716,16 +716,16 @@ ZG_D bool coneMayHoldSilhouette(float4 cone, const WideNode<D>& w, int k, V<D> x
 // range straddles pi/2 (a silhouette is possible); otherwise minAbsCos = |cos| of the range
 // end nearest to pi/2 (reflectance_boundary_bvh/bvh.h:382-392 with FCPW's cone overlap).
 template <int D>
-ZG_D bool coneAngleRange(float4 cone, const WideNode<D>& w, int k, V<D> x, float& minAbsCos) {
+ZG_D bool coneAngleRangeBox(float4 cone, const float* lo, const float* hi, V<D> x, float& minAbsCos) {
     if (cone.w < 0.0f) { minAbsCos = 1.0f; return true; }      // no silhouette candidate at all
     if (cone.w >= 1.5707963f) return false;
     V<D> v;
     float rb2 = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        float h = 0.5f * (w.hi[i][k] - w.lo[i][k]);
+        float h = 0.5f * (hi[i] - lo[i]);
         rb2 += h * h;
-        v[i] = x[i] - 0.5f * (w.lo[i][k] + w.hi[i][k]);
+        v[i] = x[i] - 0.5f * (lo[i] + hi[i]);
     }
     float dv2 = len2(v);
     if (dv2 <= rb2) return false;
@@ -744,6 +744,13 @@ ZG_D bool coneAngleRange(float4 cone, const WideNode<D>& w, int k, V<D> x, float
     if (cHi > 0.0f) { minAbsCos = cHi; return true; }       // every face front-facing
     if (cLo < 0.0f) { minAbsCos = -cLo; return true; }      // every face back-facing
     return false;
+}
+template <int D>
+ZG_D bool coneAngleRange(float4 cone, const WideNode<D>& w, int k, V<D> x, float& minAbsCos) {
+    float lo[D], hi[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) { lo[i] = w.lo[i][k]; hi[i] = w.hi[i][k]; }
+    return coneAngleRangeBox<D>(cone, lo, hi, x, minAbsCos);
 }
 
 // node bounds on the squared star radius of every primitive below a node without
@@ -908,6 +915,104 @@ __device__ __noinline__ float starRadius(const BoundaryView& b, V<D> x, float mi
             node = next >= 0 ? next : popWithin(r2, S, sp);
             if (node < 0) break;
         }
+    }
+    return fmaxf(sqrtf(r2), minR);
+}
+
+// Robin star radius answered by the whole warp (the caller loops over the lanes that need
+// one); the rules are those of starRadius above.  Each round takes up to 8 stack entries and
+// tests their 4 children in parallel: the children's upper bounds (perfectly absorbing
+// subtrees, Robin node bounds) are folded into the radius by a warp minimum before their
+// lower bounds are compared with it; internal children within the radius are pushed, leaf
+// primitives are tested 32 at a time and their radii folded the same way.  A primitive never
+// lowers the radius below its own closest distance, so the result does not depend on the
+// order primitives are met in, up to the node upper bounds.
+template <int D>
+__device__ __noinline__ float coopRobinStarRadius(const BoundaryView& b, V<D> x, float minR, float maxR, float prec,
+                                                  bool flip, CoopWork& W, int lane, uint32_t& err) {
+    if (minR > maxR) return maxR;
+    float r2 = maxR < kFltMax ? maxR * maxR : kFltMax;
+    if (b.nNodes == 0) return fmaxf(sqrtf(r2), minR);
+    const int c = lane & 3;
+    if (lane == 0) { W.node[0] = 0; W.key[0] = 0.0f; }
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int take = min(8, sp);
+        sp -= take;
+        const int e = lane >> 2;
+        int node = -1;
+        float key = kFltMax;
+        if (e < take) { node = W.node[sp + e]; key = W.key[sp + e]; }
+        __syncwarp();
+        int child = kEmptyChild;
+        float ckey = kFltMax, cap = kFltMax;
+        bool ok = false;
+        if (node >= 0 && key <= r2) {
+            const float4* p = b.nodes + (size_t)node * 8;
+            float lo[D], hi[D], d2 = 0.0f, far2 = 0.0f;
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                lo[i] = comp4(__ldg(p + i), c);
+                hi[i] = comp4(__ldg(p + D + i), c);
+                float dn = fmaxf(fmaxf(lo[i] - x[i], 0.0f), x[i] - hi[i]);
+                float df = fmaxf(fabsf(x[i] - lo[i]), fabsf(x[i] - hi[i]));
+                d2 += dn * dn;
+                far2 += df * df;
+            }
+            child = comp4i(__ldg(reinterpret_cast<const int4*>(p + 2 * D)), c);
+            if (child != kEmptyChild && d2 <= r2) {
+                ok = true;
+                ckey = d2;
+                const float kmin = comp4(__ldg(b.cones + (size_t)node * 8 + 5), c);
+                const float kmax = comp4(__ldg(b.cones + (size_t)node * 8 + 4), c);
+                if (kmin >= kFltMax - kReflEps) {
+                    cap = far2;                         // perfectly absorbing subtree
+                } else {
+                    float minCos;
+                    if (coneAngleRangeBox<D>(__ldg(b.cones + (size_t)node * 8 + c), lo, hi, x, minCos)) {
+                        if (kmax <= kReflEps) {
+                            ok = false;                 // purely reflecting, no silhouette below
+                        } else {
+                            float r2Min, r2Max;
+                            robinNodeBounds(D, sqrtf(d2), sqrtf(far2), kmin, kmax, minCos, r2Min, r2Max);
+                            ckey = fmaxf(d2, r2Min);
+                            cap = r2Max;
+                        }
+                    }
+                }
+            }
+        }
+        // upper bounds first (cap >= 0: float bits order as values), then the lower bounds
+        if (!ok) cap = kFltMax;
+        r2 = fminf(r2, __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(cap))));
+        ok = ok && ckey <= r2;
+        const bool inner = ok && !isLeaf(child), leaf = ok && isLeaf(child);
+        const unsigned im = __ballot_sync(0xffffffffu, inner);
+        const int nIn = __popc(im);
+        if (sp + nIn > kCoopStack) { err |= kErrStackOverflow; break; }
+        if (inner) {
+            int pos = sp + __popc(im & ((1u << lane) - 1u));
+            W.node[pos] = child;
+            W.key[pos] = ckey;
+        }
+        sp += nIn;
+        int cnt = leaf ? leafCount(child) : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int j = 0; j < cnt; j++) W.prim[incl - cnt + j] = leafFirst(child) + j;
+        __syncwarp();
+        for (int base = 0; base < total; base += 32) {
+            float mine = r2;
+            if (base + lane < total) primStarRadius(b, W.prim[base + lane], x, mine, flip, prec);
+            r2 = fminf(r2, __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(mine))));
+        }
+        __syncwarp();
     }
     return fmaxf(sqrtf(r2), minR);
 }
