@@ -264,9 +264,23 @@ class SampleStatistics:
         self.n_solution_estimates = 0
         self.total_walk_length = 0
         self.total_splits = 0
+        self.gradient_mean = None        # per-dimension lists once gradients are estimated
+        self.gradient_m2 = None
+        self.n_gradient_estimates = 0
 
     def get_estimated_solution(self):
         return self.solution_mean
+
+    def get_estimated_gradient(self):
+        return list(self.gradient_mean) if self.gradient_mean is not None else []
+
+    def get_estimated_gradient_variance(self):
+        if self.gradient_m2 is None:
+            return []
+        return [m / max(1, self.n_gradient_estimates - 1) for m in self.gradient_m2]
+
+    def get_gradient_estimate_count(self):
+        return self.n_gradient_estimates
 
     def get_estimated_solution_variance(self):
         return self.solution_m2 / max(1, self.n_solution_estimates - 1)
@@ -291,7 +305,8 @@ class SampleArrays:
 
     POINT_FIELDS = ("pt", "normal", "type", "estimation_quantity", "dist_to_absorbing", "dist_to_reflecting",
                     "n_walks", "seed", "first_sphere_radius", "estimate_normal_aligned", "scene_id")
-    STAT_FIELDS = ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits")
+    STAT_FIELDS = ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
+                   "gradient_mean", "gradient_m2", "n_gradient_estimates")
 
     def __init__(self, **arrays):
         self.arrays = arrays
@@ -300,7 +315,7 @@ class SampleArrays:
         self.memory = A.ZGPU_MEM_DEVICE if hasattr(first, "is_cuda") and first.is_cuda else A.ZGPU_MEM_HOST
 
     @staticmethod
-    def host(points, dist, n_walks, seeds, normals=None, types=None, first_sphere_radius=True):
+    def host(points, dist, n_walks, seeds, normals=None, types=None, first_sphere_radius=True, gradients=False):
         n = points.shape[0]
         arr = dict(pt=np.ascontiguousarray(points, np.float32),
                    dist_to_absorbing=np.ascontiguousarray(dist, np.float32),
@@ -309,6 +324,12 @@ class SampleArrays:
                    solution_mean=np.zeros(n), solution_m2=np.zeros(n),
                    n_solution_estimates=np.zeros(n, np.int32), total_walk_length=np.zeros(n, np.int64),
                    total_splits=np.zeros(n, np.int64))
+        if gradients:
+            d = points.shape[1]
+            arr["estimation_quantity"] = np.full(n, int(EstimationQuantity.SolutionAndGradient), np.int32)
+            arr["gradient_mean"] = np.zeros((n, d))
+            arr["gradient_m2"] = np.zeros((n, d))
+            arr["n_gradient_estimates"] = np.zeros(n, np.int32)
         if first_sphere_radius:
             arr["first_sphere_radius"] = np.zeros(n, np.float32)
         if normals is not None:
@@ -693,7 +714,12 @@ class _Solver:
             total_splits=np.array([s.total_splits for s in stats], np.int64),
         )
         if any(p.estimation_quantity == EstimationQuantity.SolutionAndGradient for p in pts):
-            raise ZgpuError(A.ZGPU_ERR_UNSUPPORTED, "gradient estimation is not available in this build")
+            # estimateSolutionAndGradient: per-dimension gradient moments
+            arr["gradient_mean"] = np.array([s.gradient_mean if s.gradient_mean is not None else [0.0] * D
+                                             for s in stats], np.float64).reshape(n, D)
+            arr["gradient_m2"] = np.array([s.gradient_m2 if s.gradient_m2 is not None else [0.0] * D
+                                           for s in stats], np.float64).reshape(n, D)
+            arr["n_gradient_estimates"] = np.array([s.n_gradient_estimates for s in stats], np.int32)
         rep = self.solve_arrays(pde, walk_settings, SampleArrays(**arr))
         for i, (p, s) in enumerate(zip(pts, stats)):
             p.first_sphere_radius = float(arr["first_sphere_radius"][i])
@@ -702,6 +728,10 @@ class _Solver:
             s.n_solution_estimates = int(arr["n_solution_estimates"][i])
             s.total_walk_length = int(arr["total_walk_length"][i])
             s.total_splits = int(arr["total_splits"][i])
+            if "gradient_mean" in arr:
+                s.gradient_mean = [float(v) for v in arr["gradient_mean"][i]]
+                s.gradient_m2 = [float(v) for v in arr["gradient_m2"][i]]
+                s.n_gradient_estimates = int(arr["n_gradient_estimates"][i])
         if report_progress is not None:
             report_progress(n, 0)
         return rep

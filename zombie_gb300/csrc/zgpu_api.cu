@@ -66,7 +66,8 @@ struct zgpu_context {
     // scratch (indexed by role)
     enum { kPt, kNormal, kType, kEq, kDist, kNWalks, kSeed, kFsr, kAligned, kMean, kM2, kN, kLen, kSplits,
            kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
-           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId, kNumBufs };
+           kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId,
+           kDistRefl, kGMean, kGM2, kGN, kAccGrad, kAccGradSq, kAccGradN, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
     // use_graph: the captured prepare/scan/walk/finalize sequence, replayed while the solve's
@@ -596,6 +597,21 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_TRY(stageInOut<int>(ctx, C::kN, stats->n_solution_estimates, (size_t)n, mem, &P.statN));
     ZG_TRY(stageInOut<long long>(ctx, C::kLen, (long long*)stats->total_walk_length, (size_t)n, mem, &P.statLen));
     ZG_TRY(stageInOut<long long>(ctx, C::kSplits, (long long*)stats->total_splits, (size_t)n, mem, &P.statSplits));
+    // estimateSolutionAndGradient: needs the gradient statistics arrays
+    const bool gradients = stats->gradient_mean && stats->n_gradient_estimates && pts->estimation_quantity;
+    if (gradients) {
+        for (int k = 0; k < nScenes; k++)
+            if (ws[k].use_cosine_sampling_for_derivatives)
+                return fail(ZGPU_ERR_UNSUPPORTED, "cosine sampling for derivatives needs directionForDerivative, "
+                                                  "which zgpu_sample_points does not carry");
+        ZG_TRY(stageInOut<double>(ctx, C::kGMean, stats->gradient_mean, (size_t)n * D, mem, &P.statGradMean));
+        ZG_TRY(stageInOut<double>(ctx, C::kGM2, stats->gradient_m2, (size_t)n * D, mem, &P.statGradM2));
+        ZG_TRY(stageInOut<int>(ctx, C::kGN, stats->n_gradient_estimates, (size_t)n, mem, &P.statGradN));
+        ZG_TRY(stageIn<float>(ctx, C::kDistRefl, pts->dist_to_reflecting, (size_t)n, mem, &P.distRefl));
+        ZG_TRY(scratch<double>(ctx, C::kAccGrad, (size_t)n * D, &P.accGrad));
+        ZG_TRY(scratch<double>(ctx, C::kAccGradSq, (size_t)n * D, &P.accGradSq));
+        ZG_TRY(scratch<int>(ctx, C::kAccGradN, (size_t)n, &P.accGradN));
+    }
     long long* blockSums = nullptr;
     ZG_TRY(scratch<long long>(ctx, C::kWalkStart, (size_t)n + 1, &P.walkStart));
     ZG_TRY(scratch<int>(ctx, C::kFlags, (size_t)n, &P.pointFlags));
@@ -691,6 +707,11 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_TRY(stageOut<long long>(ctx, P.statLen, (long long*)stats->total_walk_length, (size_t)n, mem));
     ZG_TRY(stageOut<long long>(ctx, P.statSplits, (long long*)stats->total_splits, (size_t)n, mem));
     if (P.fsrPersistent) ZG_TRY(stageOut<float>(ctx, P.fsr, pts->first_sphere_radius, (size_t)n, mem));
+    if (gradients) {
+        ZG_TRY(stageOut<double>(ctx, P.statGradMean, stats->gradient_mean, (size_t)n * D, mem));
+        if (stats->gradient_m2) ZG_TRY(stageOut<double>(ctx, P.statGradM2, stats->gradient_m2, (size_t)n * D, mem));
+        ZG_TRY(stageOut<int>(ctx, P.statGradN, stats->n_gradient_estimates, (size_t)n, mem));
+    }
     ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters, P.counters, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters + 12, P.walkStart + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
     ZG_CUDA(cudaStreamSynchronize(s));

@@ -15,7 +15,7 @@ enum : int { kCtrNext = 0, kCtrSteps = 1, kCtrEscaped = 2, kCtrExceeded = 3, kCt
              kCtrCount = 8 };
 
 // per-point flags written by the prepare kernel
-enum : int { kPointBoundaryValue = 1, kPointFlip = 2 };
+enum : int { kPointBoundaryValue = 1, kPointFlip = 2, kPointGradient = 4 };
 
 // what a walk needs of its problem: boundaries, domain box, settings and PDE
 struct SceneDesc {
@@ -49,6 +49,10 @@ struct SolveParams {
     double* statMean;
     double* statM2;
     int* statN;
+    double* statGradMean;       // [n][D] (estimateSolutionAndGradient points)
+    double* statGradM2;
+    int* statGradN;
+    const float* distRefl;      // gradient points of Walk on Stars: distance to the reflecting boundary
     long long* statLen;
     long long* statSplits;
     // scratch
@@ -60,6 +64,9 @@ struct SolveParams {
     int* accN;
     long long* accLen;
     long long* accSplits;
+    double* accGrad;            // [n][D] sums and sums of squares of gradient estimates
+    double* accGradSq;
+    int* accGradN;
     unsigned long long* counters;
     unsigned int* errorWord;
     float4* splitStack;         // walk threads x kSplitStack x 3 float4

@@ -72,6 +72,11 @@ struct Walker {
     int wlen;
     bool onRefl, flip, pointFlip;
     float totRefl, totSrc;
+    // estimateSolutionAndGradient: this walk's first-step source contribution, control
+    // variate and gradient directions
+    bool gradMode;
+    float firstSrc, cvB;
+    V<D> bGradDir, sGradDir;
     // per-walk accumulation across split states
     float walkTotal;
     bool success;
@@ -150,11 +155,77 @@ struct Walker {
         fsr = P.fsr[point];
         firstStep = true;
         cpValid = false;
+        gradMode = false;
         queryPending = false;
         radiusPending = false;
         radiusReady = false;
         pendingCode = -1;
         resetGreens();
+        if (flags & kPointGradient) startGradient(w);
+    }
+
+    // First step of estimateSolutionAndGradient (walk_on_spheres.h:417-515,
+    // walk_on_stars.h:665-790): a ball of radius 0.99 x the distance to the boundary; a
+    // source point sampled along a stratified direction, a boundary point on a stratified
+    // direction, and the gradient directions of both.  With antithetic variates walks 2k and
+    // 2k+1 share pcg32 stream k: the odd walk draws the same first step and mirrors it
+    // through the centre, then both continue on identical random numbers.  Stratification is
+    // a Latin hypercube over the point's 2M first-step samples of this call (M = walks, or
+    // pairs), the strata assigned by a per-point permutation.
+    __device__ __noinline__ void startGradient(long long w) {
+        const zgpu_walk_settings& ws = sc->ws;
+        const bool anti = ws.use_gradient_antithetic_variates != 0;
+        const long long pair = anti ? (w >> 1) : w;
+        const bool mirror = anti && (w & 1);
+        const int nPrev = __ldg(P.nPrev + point);
+        if (anti) rng.seed(__ldg(P.seed + point), (uint64_t)pair + (uint64_t)nPrev);
+        const long long walks = __ldg(P.walkStart + point + 1) - __ldg(P.walkStart + point);
+        const uint32_t m = (uint32_t)(2 * (anti ? walks / 2 : walks));
+        const uint64_t key = __ldg(P.seed + point) ^ (uint64_t)nPrev;
+        gradMode = true;
+        cvB = (ws.use_gradient_control_variates && nPrev > 0) ? (float)P.statMean[point] : 0.0f;
+        const V<D> x0 = pt;
+        const float R0 = fsr;
+        g.update(x0, R0);
+        float us[D], ub[D];
+#pragma unroll
+        for (int j = 0; j < D - 1; j++) {
+            us[j] = fminf(((float)lhsStratum(key, j, (uint32_t)(2 * pair), m) + rng.uniform()) / (float)m, 0.99999994f);
+            ub[j] = fminf(((float)lhsStratum(key, j, (uint32_t)(2 * pair + 1), m) + rng.uniform()) / (float)m, 0.99999994f);
+        }
+        firstSrc = 0.0f;
+        sGradDir = vzero<D>();
+        if (!ws.ignore_source_contribution) {
+            const float nrmG = g.norm();
+            if (sc->pde.is_source_constant) {
+                firstSrc = nrmG * pde.source(x0);
+            } else {
+                const V<D> dirS = sphereFromUniform<D>(us);
+                const float r = g.sampleRadius(rng);
+                const float pdf = g.evaluate(r) / nrmG;
+                const V<D> ys = mirror ? x0 - r * dirS : x0 + r * dirS;
+                firstSrc = nrmG * pde.source(ys);
+                sGradDir = (1.0f / (pdf * nrmG)) * g.gradient(r, ys);
+            }
+            totSrc += thr * firstSrc;
+        }
+        V<D> dirB = sphereFromUniform<D>(ub);
+        if (mirror) dirB = -dirB;
+        const float bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
+        const V<D> yb = x0 + R0 * dirB;
+        thr *= g.poissonKernelCentre() / bPdf;
+        bGradDir = (1.0f / (bPdf * thr)) * g.poissonKernelGradient(yb);
+        pt = yb;
+        if (SOLVER == ZGPU_SOLVER_WALK_ON_STARS) {
+            prevDist = R0;
+            prevDir = dirB;
+            nrm = vzero<D>();
+            onRefl = false;
+        }
+        firstStep = false;
+        fsr = 0.0f;
+        resetGreens();
+        closestQuery();
     }
 
     // answer of a cooperative closest-point query
@@ -238,6 +309,7 @@ struct Walker {
         }
         if (nStack > 0) { beginSplit(); return true; }
         if (success) {
+            if (gradMode) addGradient();
             atomicAdd(P.accSum + point, (double)walkTotal);
             atomicAdd(P.accSq + point, (double)walkTotal * (double)walkTotal);
             atomicAdd(P.accN + point, 1);
@@ -257,6 +329,20 @@ struct Walker {
         r[0] = make_float4(pt[0], pt[1], D == 3 ? pt[D - 1] : 0.0f, thr);
         r[1] = make_float4(walkTotal + totRefl + totSrc, __int_as_float(point), __int_as_float((int)(lenSum + wlen)), 0.0f);
         return true;
+    }
+
+    // gradient estimate of a completed walk (walk_on_spheres.h:567-580): the boundary part of
+    // its total (minus the control variate) along the boundary gradient direction plus the
+    // first source contribution along the source gradient direction
+    __device__ __noinline__ void addGradient() {
+        const float bc = walkTotal - firstSrc;
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const double gi = (double)((bc - cvB) * bGradDir[i] + firstSrc * sGradDir[i]);
+            atomicAdd(P.accGrad + (size_t)point * D + i, gi);
+            atomicAdd(P.accGradSq + (size_t)point * D + i, gi * gi);
+        }
+        atomicAdd(P.accGradN + point, 1);
     }
 
     // --------------------------------------------------------------- Walk on Spheres step
@@ -582,6 +668,10 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
     int nPrev = P.statN[i];
     P.nPrev[i] = nPrev;
     P.accSum[i] = 0.0; P.accSq[i] = 0.0; P.accN[i] = 0; P.accLen[i] = 0; P.accSplits[i] = 0;
+    if (P.accGrad) {
+        for (int k = 0; k < D; k++) { P.accGrad[i * D + k] = 0.0; P.accGradSq[i * D + k] = 0.0; }
+        P.accGradN[i] = 0;
+    }
     bool hasPrev = nPrev > 0 && P.fsrPersistent;
     int flags = 0;
     long long count = 0;
@@ -590,6 +680,29 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
     if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && ws.solve_double_sided && type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && aligned)
         flags |= kPointFlip;
     if (badScene) atomicOr(P.errorWord, kErrBadInput);
+    if (eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT && type == ZGPU_SAMPLE_IN_DOMAIN && !badScene && P.accGrad) {
+        // estimateSolutionAndGradient (walk_on_spheres.h:422-430, walk_on_stars.h:670-684):
+        // first ball 0.99 x the distance to the boundary; antithetic pairs halve the draws
+        float dB = dAbs;
+        if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && sc.hasRefl) {
+            float dR;
+            if (P.distRefl) {
+                dR = P.distRefl[i];
+            } else {
+                uint32_t err = 0;
+                dR = closestPoint<D>(sc.reflecting, vload<D>(P.pt + (size_t)i * D), S, err).d;
+                if (err) atomicOr(P.errorWord, err);
+            }
+            dB = fminf(dB, dR);
+        }
+        const int nw = max(P.nWalks[i], 0);
+        count = nw == 0 ? 0 : (ws.use_gradient_antithetic_variates ? 2 * max(1, nw / 2) : nw);
+        P.fsr[i] = kRadiusShrink * dB;
+        if (count > 0 && P.fsr[i] > 0.0f) flags |= kPointGradient;
+        P.pointFlags[i] = flags;
+        P.walkStart[i] = count;
+        return;
+    }
     if (eq == ZGPU_ESTIMATE_SKIP || badScene) {
         count = 0;
     } else if (type == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) {
@@ -661,6 +774,27 @@ __global__ void finalizeKernel(const __grid_constant__ SolveParams P) {
     }
     P.statLen[i] += P.accLen[i];
     P.statSplits[i] += P.accSplits[i];
+    if (P.accGrad && P.statGradMean && P.statGradN) {
+        const int g2 = P.accGradN[i];
+        if (g2 > 0) {
+            const int g1 = P.statGradN[i];
+            const int gt = g1 + g2;
+            for (int k = 0; k < D; k++) {
+                const double s = P.accGrad[i * D + k], q = P.accGradSq[i * D + k];
+                const double m2mean = s / g2, m2m2 = fmax(0.0, q - s * m2mean);
+                if (g1 == 0) {
+                    P.statGradMean[i * D + k] = m2mean;
+                    if (P.statGradM2) P.statGradM2[i * D + k] = m2m2;
+                } else {
+                    const double m1 = P.statGradMean[i * D + k], delta = m2mean - m1;
+                    P.statGradMean[i * D + k] = m1 + delta * ((double)g2 / gt);
+                    if (P.statGradM2)
+                        P.statGradM2[i * D + k] += m2m2 + delta * delta * ((double)g1 * (double)g2 / gt);
+                }
+            }
+            P.statGradN[i] = gt;
+        }
+    }
 }
 
 // ------------------------------------------------------------------------- query kernels

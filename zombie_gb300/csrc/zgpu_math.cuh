@@ -86,6 +86,39 @@ ZG_D V<3> sampleSphere(Pcg32& rng, V<3>) {
     V<3> v; v[0] = r * c; v[1] = r * s; v[2] = z; return v;
 }
 template <int D> ZG_D V<D> sampleSphere(Pcg32& rng) { return sampleSphere(rng, V<D>()); }
+// the same maps from given uniforms (stratified first steps of the gradient estimator)
+ZG_D V<2> sphereFromUniform(const float* u, V<2>) {
+    float s, c;
+    sincospif(2.0f * u[0], &s, &c);
+    V<2> r; r[0] = c; r[1] = s; return r;
+}
+ZG_D V<3> sphereFromUniform(const float* u, V<3>) {
+    float z = 1.0f - 2.0f * u[0];
+    float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float s, c;
+    sincospif(2.0f * u[1], &s, &c);
+    V<3> v; v[0] = r * c; v[1] = r * s; v[2] = z; return v;
+}
+template <int D> ZG_D V<D> sphereFromUniform(const float* u) { return sphereFromUniform(u, V<D>()); }
+
+// Latin-hypercube stratum of sample k among m for dimension j of point `key`: an affine
+// permutation k -> (a k + b) mod m with a coprime to m, a and b hashed from (key, j)
+ZG_D uint32_t lhsStratum(uint64_t key, int j, uint32_t k, uint32_t m) {
+    if (m <= 1) return 0;
+    uint64_t h = key ^ (0x9E3779B97F4A7C15ull * (uint64_t)(j + 1));
+    h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
+    h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
+    h ^= h >> 31;
+    uint32_t a = 1u + (uint32_t)(h % (uint64_t)(m - 1));
+    for (int guard = 0; guard < 64; guard++) {          // next a coprime to m
+        uint32_t x = a, y = m;
+        while (y) { uint32_t t = x % y; x = y; y = t; }
+        if (x == 1u) break;
+        a = a + 1u < m ? a + 1u : 1u;
+    }
+    const uint32_t b = (uint32_t)((h >> 32) % m);
+    return (uint32_t)(((uint64_t)a * k + b) % m);
+}
 template <int D> ZG_D float pdfSphere(float r) { return D == 2 ? 1.0f / (2.0f * kPi * r) : 1.0f / (4.0f * kPi * r * r); }
 
 // -----------------------------------------------------------------------------------
@@ -250,6 +283,50 @@ struct Greens {
                                 : fmaxf(fminf(2.0f / R, 2.0f / lambda), fminf(0.5f * sqrtf(R), 0.5f * sqrtLambda));
         }
         return rejectionRadius(rng, bound);
+    }
+
+    // ---- the gradient estimator's first step (estimateSolutionAndGradient)
+    // Poisson kernel of the ball centre (distributions.h:514-516, :621-623, :769-771, :934-936)
+    ZG_D float poissonKernelCentre() const {
+        const float s = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
+        if (!SCREENED || !yukawa) return s;
+        if (D == 2) return s / i0R;
+        return s * R * sqrtLambda / i0R;                     // muR / (4 pi sinh(muR))
+    }
+    // 2D: K1(muR), I1(muR); 3D: K_{3/2}, I_{3/2} of muR up to the factors the formulas share
+    ZG_D void outerTerms(float& kR, float& iR) const {
+        const float muR = R * sqrtLambda;
+        if (D == 2) { kR = besselK1(muR); iR = besselI1(muR); return; }
+        const float e = expf(-muR), e2 = e * e;
+        const float coshmuR = (1.0f + e2) / (2.0f * e), sinhmuR = (1.0f - e2) / (2.0f * e);
+        kR = e * (1.0f + 1.0f / muR);
+        iR = coshmuR - sinhmuR / muR;
+    }
+    // |grad G| / r at distance r (distributions.h:493-497, :600-604, :744-752, :905-918)
+    ZG_D float gradientNorm(float r) const {
+        if (!SCREENED || !yukawa) {
+            if (D == 2) return (1.0f / (r * r) - 1.0f / (R * R)) / (2.0f * kPi);
+            return (1.0f / (r * r * r) - 1.0f / (R * R * R)) / (4.0f * kPi);
+        }
+        float kR, iR;
+        outerTerms(kR, iR);
+        const float mur = r * sqrtLambda;
+        if (D == 2) return sqrtLambda * (besselK1(mur) - besselI1(mur) * kR / iR) / (2.0f * kPi * r);
+        const float e = expf(-mur), e2 = e * e;
+        const float coshmur = (1.0f + e2) / (2.0f * e), sinhmur = (1.0f - e2) / (2.0f * e);
+        const float K32 = e * (1.0f + 1.0f / mur), I32 = coshmur - sinhmur / mur;
+        return sqrtLambda * (K32 - I32 * kR / iR) / (4.0f * kPi * r * r);
+    }
+    ZG_D V<D> gradient(float r, V<D> y) const { return gradientNorm(r) * (y - c); }
+    // gradient of the Poisson kernel at a point y of the sphere (distributions.h:546-550,
+    // :655-659, :817-822, :988-994)
+    ZG_D V<D> poissonKernelGradient(V<D> y) const {
+        const V<D> d = y - c;
+        if (!SCREENED || !yukawa) return (D == 2 ? 2.0f / (2.0f * kPi * R * R) : 3.0f / (4.0f * kPi * R * R)) * d;
+        float kR, iR;
+        outerTerms(kR, iR);
+        if (D == 2) return (sqrtLambda / (R * iR) / (2.0f * kPi)) * d;
+        return (sqrtLambda * sqrtLambda / iR / (4.0f * kPi)) * d;
     }
 };
 

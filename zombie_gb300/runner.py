@@ -40,14 +40,14 @@ class GpuProblem:
         self.dist = self.queries.compute_dist_to_absorbing_boundary(self.points)
         self.seeds = P.seeds_for(self.points.shape[0], seed_base)
 
-    def host_arrays(self, n_walks=None):
+    def host_arrays(self, n_walks=None, gradients=False):
         nw = self.problem.n_walks if n_walks is None else np.broadcast_to(np.asarray(n_walks, np.int32),
                                                                           (self.points.shape[0],))
-        return SampleArrays.host(self.points, self.dist, nw, self.seeds)
+        return SampleArrays.host(self.points, self.dist, nw, self.seeds, gradients=gradients)
 
-    def device_arrays(self, n_walks=None):
+    def device_arrays(self, n_walks=None, gradients=False):
         import torch
-        h = self.host_arrays(n_walks)
+        h = self.host_arrays(n_walks, gradients)
         dev = {}
         for k, v in h.arrays.items():
             t = torch.from_numpy(np.ascontiguousarray(v).view(np.int64) if v.dtype == np.uint64 else np.ascontiguousarray(v))
