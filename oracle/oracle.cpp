@@ -80,10 +80,38 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
                 bool aligned = pts->estimate_normal_aligned ? pts->estimate_normal_aligned[i] != 0 : false;
                 float fsr = pts->first_sphere_radius ? pts->first_sphere_radius[i] : 0.0f;
                 PointStats ps;
-                if (solver == ZGPU_SOLVER_WALK_ON_SPHERES)
+                GradStats gs;
+                const bool gradient = eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT && type == ZGPU_SAMPLE_IN_DOMAIN &&
+                                      st->gradient_mean && st->n_gradient_estimates;
+                if (gradient) {
+                    float dB = pts->dist_to_absorbing[i];
+                    if (solver == ZGPU_SOLVER_WALK_ON_STARS && q.hasNonEmptyReflectingBoundary()) {
+                        float dR;
+                        if (pts->dist_to_reflecting) dR = pts->dist_to_reflecting[i];
+                        else { Vec<D> cp, cn; int pi; q.reflecting->closestPoint(p, cp, cn, dR, pi); }
+                        dB = std::min(dB, dR);
+                    }
+                    const float cvB = (ws->use_gradient_control_variates && nPrev > 0) ? (float)st->solution_mean[i] : 0.0f;
+                    s.gradEstimate(solver, p, dB, pts->n_walks[i], pts->seed[i], nPrev, cvB, ps, gs);
+                    fsr = 0.99f * dB;
+                } else if (solver == ZGPU_SOLVER_WALK_ON_SPHERES)
                     s.wosEstimate(p, type, pts->dist_to_absorbing[i], pts->n_walks[i], pts->seed[i], nPrev > 0, aligned, fsr, ps);
                 else
                     s.wostEstimate(p, nrm, type, pts->dist_to_absorbing[i], pts->n_walks[i], pts->seed[i], nPrev > 0, aligned, fsr, ps);
+                if (gradient && gs.n > 0) {
+                    int g1 = st->n_gradient_estimates[i], g2 = gs.n, gt = g1 + g2;
+                    for (int k = 0; k < D; k++) {
+                        double* gm = st->gradient_mean + (size_t)i * D + k;
+                        double* g2m = st->gradient_m2 ? st->gradient_m2 + (size_t)i * D + k : nullptr;
+                        if (g1 == 0) { *gm = gs.mean[k]; if (g2m) *g2m = gs.m2[k]; }
+                        else {
+                            double delta = gs.mean[k] - *gm;
+                            *gm += delta * ((double)g2 / gt);
+                            if (g2m) *g2m += gs.m2[k] + delta * delta * ((double)g1 * g2 / gt);
+                        }
+                    }
+                    st->n_gradient_estimates[i] = gt;
+                }
                 if (pts->first_sphere_radius) pts->first_sphere_radius[i] = fsr;
                 localSteps += ps.steps;
                 // SampleStatistics::merge (common.h:268-310) in FP64

@@ -215,8 +215,9 @@ def solve(solver, dim, absorbing, reflecting, domain_min, domain_max, pde, setti
         setattr(sp, name, A.ptr(points.get(name)))
     st = A.SampleStatisticsC()
     st.memory = A.ZGPU_MEM_HOST
-    for name in ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits"):
-        setattr(st, name, A.ptr(stats[name]))
+    for name in ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
+                 "gradient_mean", "gradient_m2", "n_gradient_estimates"):
+        setattr(st, name, A.ptr(stats.get(name)))
     steps = C.c_uint64(0)
     if n_threads is None:
         n_threads = max(1, lib().orc_hardware_threads())

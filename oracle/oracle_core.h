@@ -183,6 +183,12 @@ struct GreensFnBall {
     virtual float norm() const = 0;
     virtual float directionSampledPoissonKernel(const Vec<D>& y) const = 0;
     virtual float reflectance(float r, const Vec<D>& dir, const Vec<D>& n, float robinCoeff) const = 0;
+    // the gradient estimator's first step: |grad G| / r, the Poisson kernel at the centre and
+    // its gradient at a point of the sphere (distributions.h:493-550, :600-659, :744-822, :905-994)
+    virtual float gradientNorm(float r) const = 0;
+    virtual float poissonKernelCentre() const = 0;
+    virtual Vec<D> poissonKernelGradient(const Vec<D>& y) const = 0;
+    Vec<D> gradient(float r, const Vec<D>& y) const { return gradientNorm(r) * (y - c); }
 
     // distributions.h:419-440
     Vec<D> rejectionSampleGreensFn(const Vec<D>& dir, float bound, Pcg32& rng, float& r, float& pdf) {
@@ -216,6 +222,9 @@ template <> struct HarmonicGreensFnBall<2> : GreensFnBall<2> {
     }
     float evaluate(float r) const override { return std::log(R / r) / (2.0f * kPi); }
     float norm() const override { return R * R / 4.0f; }
+    float gradientNorm(float r) const override { return (1.0f / (r * r) - 1.0f / (R * R)) / (2.0f * kPi); }
+    float poissonKernelCentre() const override { return 1.0f / (2.0f * kPi); }
+    Vec<2> poissonKernelGradient(const Vec<2>& y) const override { return (2.0f / (2.0f * kPi * R * R)) * (y - c); }
     float directionSampledPoissonKernel(const Vec<2>&) const override { return 1.0f; }
     float reflectance(float r, const Vec<2>& dir, const Vec<2>& n, float robinCoeff) const override {
         if (std::fabs(robinCoeff) > 0.0f) {
@@ -241,6 +250,9 @@ template <> struct HarmonicGreensFnBall<3> : GreensFnBall<3> {
     }
     float evaluate(float r) const override { return (1.0f / r - 1.0f / R) / (4.0f * kPi); }
     float norm() const override { return R * R / 6.0f; }
+    float gradientNorm(float r) const override { return (1.0f / (r * r * r) - 1.0f / (R * R * R)) / (4.0f * kPi); }
+    float poissonKernelCentre() const override { return 1.0f / (4.0f * kPi); }
+    Vec<3> poissonKernelGradient(const Vec<3>& y) const override { return (3.0f / (4.0f * kPi * R * R)) * (y - c); }
     float directionSampledPoissonKernel(const Vec<3>&) const override { return 1.0f; }
     float reflectance(float r, const Vec<3>& dir, const Vec<3>& n, float robinCoeff) const override {
         if (std::fabs(robinCoeff) > 0.0f) {
@@ -279,6 +291,15 @@ template <> struct YukawaGreensFnBall<2> : GreensFnBall<2> {
         return (K0mur - I0mur * K0muR / I0muR) / (2.0f * kPi);
     }
     float poissonKernel() const { return 1.0f / (2.0f * kPi * I0muR); }
+    float poissonKernelCentre() const override { return poissonKernel(); }
+    float gradientNorm(float r) const override {
+        float mur = r * sqrtLambda;
+        float Qr = sqrtLambda * ((float)bessel::k1(mur) - (float)bessel::i1(mur) * K1muR / I1muR);
+        return Qr / (2.0f * kPi * r);
+    }
+    Vec<2> poissonKernelGradient(const Vec<2>& y) const override {
+        return (sqrtLambda / (R * I1muR) / (2.0f * kPi)) * (y - c);
+    }
     float norm() const override { return (1.0f - 2.0f * kPi * poissonKernel()) / (sqrtLambda * sqrtLambda); }
     float dampening(float r) const {
         float mur = r * sqrtLambda;
@@ -332,6 +353,21 @@ template <> struct YukawaGreensFnBall<3> : GreensFnBall<3> {
         return (expmur - expmuR * sinhmur / sinhmuR) / (4.0f * kPi * r);
     }
     float poissonKernel() const { return muR / (4.0f * kPi * sinhmuR); }
+    float poissonKernelCentre() const override { return poissonKernel(); }
+    float gradientNorm(float r) const override {
+        float mur = r * sqrtLambda;
+        float expmur = std::exp(-mur);
+        float exp2mur = expmur * expmur;
+        float coshmur = (1.0f + exp2mur) / (2.0f * expmur);
+        float sinhmur = (1.0f - exp2mur) / (2.0f * expmur);
+        float K32mur = expmur * (1.0f + 1.0f / mur);
+        float I32mur = coshmur - sinhmur / mur;
+        float Qr = sqrtLambda * (K32mur - I32mur * K32muR / I32muR);
+        return Qr / (4.0f * kPi * r * r);
+    }
+    Vec<3> poissonKernelGradient(const Vec<3>& y) const override {
+        return (sqrtLambda * sqrtLambda / I32muR / (4.0f * kPi)) * (y - c);
+    }
     float norm() const override { return (1.0f - 4.0f * kPi * poissonKernel()) / (sqrtLambda * sqrtLambda); }
     float dampening(float r) const {
         float mur = r * sqrtLambda;

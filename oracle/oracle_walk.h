@@ -164,6 +164,15 @@ struct PointStats {
     void add(double x) { n += 1; double d = x - mean; mean += d / n; double d2 = x - mean; m2 += d * d2; }
 };
 
+struct GradStats {
+    double mean[3] = {0, 0, 0}, m2[3] = {0, 0, 0};
+    int n = 0;
+    void add(const double* x, int D) {
+        n += 1;
+        for (int i = 0; i < D; i++) { double d = x[i] - mean[i]; mean[i] += d / n; m2[i] += d * (x[i] - mean[i]); }
+    }
+};
+
 template <int D>
 struct Solver {
     const Queries<D>& q;
@@ -454,6 +463,116 @@ struct Solver {
                 }
             }
             if (success) { st.add((double)total); st.splits += splits; }
+        }
+    }
+
+    // ------------------------------- solution and gradient ----------------------------
+    // Latin-hypercube stratum of sample k among m for dimension j of point `key` (the device's
+    // permutation: k -> (a k + b) mod m, a coprime to m, a and b hashed from (key, j))
+    static uint32_t lhsStratum(uint64_t key, int j, uint32_t k, uint32_t m) {
+        if (m <= 1) return 0;
+        uint64_t h = key ^ (0x9E3779B97F4A7C15ull * (uint64_t)(j + 1));
+        h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
+        h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
+        h ^= h >> 31;
+        uint32_t a = 1u + (uint32_t)(h % (uint64_t)(m - 1));
+        for (int guard = 0; guard < 64; guard++) {
+            uint32_t x = a, y = m;
+            while (y) { uint32_t t = x % y; x = y; y = t; }
+            if (x == 1u) break;
+            a = a + 1u < m ? a + 1u : 1u;
+        }
+        const uint32_t b = (uint32_t)((h >> 32) % m);
+        return (uint32_t)(((uint64_t)a * k + b) % m);
+    }
+    static Vec<D> sphereFromUniform(const float* u) {
+        Vec<D> v;
+        if (D == 2) { v[0] = std::cos(2.0f * kPi * u[0]); v[1] = std::sin(2.0f * kPi * u[0]); }
+        else {
+            float z = 1.0f - 2.0f * u[0], r = std::sqrt(std::max(0.0f, 1.0f - z * z));
+            v[0] = r * std::cos(2.0f * kPi * u[1]); v[1] = r * std::sin(2.0f * kPi * u[1]); v[D - 1] = z;
+        }
+        return v;
+    }
+
+    // estimateSolutionAndGradient (walk_on_spheres.h:417-593, walk_on_stars.h:665-848) with the
+    // parallel restatement the device uses: antithetic walks 2k, 2k+1 share pcg32 stream k and
+    // mirror the first step; the first-step samples form a Latin hypercube assigned by a
+    // per-point permutation; the control variate cvB is the previous call's estimate.
+    void gradEstimate(int solver, const Vec<D>& pt, float distB, int nWalks, uint64_t seed, int nPrev, float cvB,
+                      PointStats& st, GradStats& gs) const {
+        const bool anti = ws.use_gradient_antithetic_variates != 0;
+        const int count = nWalks <= 0 ? 0 : (anti ? 2 * std::max(1, nWalks / 2) : nWalks);
+        const float R0 = 0.99f * distB;
+        if (count == 0 || !(R0 > 0.0f)) return;
+        const uint32_t m = (uint32_t)(2 * (anti ? count / 2 : count));
+        const uint64_t key = seed ^ (uint64_t)nPrev;
+        std::queue<WalkState<D>> queue;
+        for (int w = 0; w < count; w++) {
+            const uint32_t pair = anti ? (uint32_t)(w >> 1) : (uint32_t)w;
+            const bool mirror = anti && (w & 1);
+            Pcg32 rng(seed, (uint64_t)pair + (uint64_t)nPrev);
+            bool yukawa = pde.p->absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == 0;
+            std::unique_ptr<GreensFnBall<D>> g = makeGreens(yukawa);
+            g->updateBall(pt, R0);
+            float us[3] = {0, 0, 0}, ub[3] = {0, 0, 0};
+            for (int j = 0; j < D - 1; j++) {
+                us[j] = std::min(((float)lhsStratum(key, j, 2 * pair, m) + rng.nextFloat()) / (float)m, 0.99999994f);
+                ub[j] = std::min(((float)lhsStratum(key, j, 2 * pair + 1, m) + rng.nextFloat()) / (float)m, 0.99999994f);
+            }
+            WalkState<D> s(pt, Vec<D>(), Vec<D>(), 0.0f, 1.0f, 0, false);
+            float firstSrc = 0.0f;
+            Vec<D> sDir;
+            if (!ws.ignore_source_contribution) {
+                float nrmG = g->norm();
+                if (pde.p->is_source_constant) {
+                    firstSrc = nrmG * pde.source(pt);
+                } else {
+                    Vec<D> dirS = sphereFromUniform(us);
+                    float r, pdf;
+                    g->sampleVolume(dirS, rng, r, pdf);
+                    pdf = g->evaluate(r) / nrmG;
+                    Vec<D> ys = mirror ? pt - r * dirS : pt + r * dirS;
+                    firstSrc = nrmG * pde.source(ys);
+                    sDir = (1.0f / (pdf * nrmG)) * g->gradient(r, ys);
+                }
+                s.totalSourceContribution += s.throughput * firstSrc;
+            }
+            Vec<D> dirB = sphereFromUniform(ub);
+            if (mirror) dirB = -dirB;
+            const float bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
+            Vec<D> yb = pt + R0 * dirB;
+            s.throughput *= g->poissonKernelCentre() / bPdf;
+            Vec<D> bDir = (1.0f / (bPdf * s.throughput)) * g->poissonKernelGradient(yb);
+            s.currentPt = yb;
+            if (solver == ZGPU_SOLVER_WALK_ON_STARS) { s.prevDistance = R0; s.prevDirection = dirB; }
+            queue.push(s);
+            int splits = -1;
+            float total = 0.0f;
+            bool success = false;
+            while (!queue.empty()) {
+                s = queue.front(); queue.pop();
+                splits++;
+                std::unique_ptr<GreensFnBall<D>> gw = makeGreens(yukawa);
+                float dist = q.computeDistToAbsorbingBoundary(s.currentPt);
+                Code code;
+                if (solver == ZGPU_SOLVER_WALK_ON_SPHERES) code = wosWalk(dist, gw, rng, s, queue, st.steps);
+                else code = wostWalk(dist, 0.0f, false, gw, rng, s, queue, st.steps);
+                if (code != Code::EscapedDomain) {
+                    float term = solver == ZGPU_SOLVER_WALK_ON_SPHERES ? wosTerminal(code, s) : wostTerminal(code, s);
+                    total += s.throughput * term + s.totalReflectingBoundaryContribution + s.totalSourceContribution;
+                    st.walkLength += s.walkLength;
+                    success = true;
+                }
+            }
+            if (success) {
+                st.add((double)total);
+                st.splits += splits;
+                double gv[3] = {0, 0, 0};
+                const float bc = total - firstSrc;
+                for (int i = 0; i < D; i++) gv[i] = (double)((bc - cvB) * bDir[i] + firstSrc * sDir[i]);
+                gs.add(gv, D);
+            }
         }
     }
 

@@ -471,3 +471,32 @@ def test_gradient_estimates_match_the_analytic_gradient(zgpu, make):
     sn = d["n_solution_estimates"].cpu().numpy().astype(np.float64)
     sz = (d["solution_mean"].cpu().numpy() - u) / np.sqrt(d["solution_m2"].cpu().numpy() / np.maximum(sn - 1, 1) / sn)
     assert np.mean(np.abs(sz) <= 4) > 0.99
+
+
+def test_gradient_estimates_match_the_oracle(zgpu, oracle):
+    """GPU and oracle run the same gradient walks (same streams, strata and mirroring): the
+    per-point gradient estimates agree far inside their standard errors."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_oracle_solvers import run_oracle_with
+    from zombie_gb300.runner import GpuProblem
+    pr = P.laplace_wos_2d(n_segments=512, grid=12, spp=128)
+    n, D = pr.points.shape
+    eq = np.full(n, A.ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT, np.int32)
+    extra = dict(gradient_mean=np.zeros((n, D)), gradient_m2=np.zeros((n, D)),
+                 n_gradient_estimates=np.zeros(n, np.int32))
+    st = None
+    for _ in range(2):
+        st = run_oracle_with(oracle, pr, st, estimation_quantity=eq, extra_stats=extra)
+    gp = GpuProblem(pr)
+    d = gp.device_arrays(gradients=True)
+    gp.solve(d)
+    gp.solve(d)
+    assert np.array_equal(d["n_gradient_estimates"].cpu().numpy(), st["n_gradient_estimates"])
+    gg = d["gradient_mean"].cpu().numpy().reshape(n, D)
+    og = st["gradient_mean"].reshape(n, D)
+    se = np.sqrt(st["gradient_m2"].reshape(n, D) / np.maximum(st["n_gradient_estimates"] - 1, 1)[:, None]
+                 / st["n_gradient_estimates"][:, None])
+    assert np.mean(np.abs(gg - og) <= 0.1 * se + 1e-6) > 0.95
+    assert np.all(np.abs(gg - og) <= 3 * se + 1e-6)

@@ -30,6 +30,28 @@ def run_oracle(oracle, pr, n_threads=None, seeds=None):
     return st, steps
 
 
+def run_oracle_with(oracle, pr, st=None, estimation_quantity=None, extra_stats=None, n_threads=None):
+    """run_oracle with extra point fields and statistics, accumulating into st across calls."""
+    D = pr.dim
+    ab = oracle.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
+    rf = None
+    if pr.reflecting is not None and len(pr.reflecting[1]):
+        rf = oracle.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind,
+                             silhouette_precision=pr.ignore_silhouette_precision)
+    n = pr.points.shape[0]
+    d = ab.closest_point(pr.points)[2] if ab is not None else None
+    pts = dict(pt=pr.points, dist_to_absorbing=d, n_walks=pr.n_walks, seed=P.seeds_for(n),
+               first_sphere_radius=np.zeros(n, np.float32))
+    if estimation_quantity is not None:
+        pts["estimation_quantity"] = estimation_quantity
+    if st is None:
+        st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+                  total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
+        st.update({k: v.copy() for k, v in (extra_stats or {}).items()})
+    oracle.solve(pr.solver, D, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, pts, st, n_threads)
+    return st
+
+
 def zscores(st, exact):
     n = st["n_solution_estimates"].astype(np.float64)
     se = np.sqrt(st["solution_m2"] / np.maximum(n - 1, 1) / np.maximum(n, 1))
@@ -110,3 +132,26 @@ def test_russian_roulette_and_splitting_stay_unbiased(oracle):
     z = zscores(st, pr.exact())
     assert abs(z.mean()) < 0.5
     assert np.mean(np.abs(z) > 3.5) < 0.04
+
+
+@pytest.mark.parametrize("make", [lambda: P.laplace_wos_2d(n_segments=512, grid=10, spp=256),
+                                  lambda: P.mixed_wost_2d(n_segments=512, grid=8, spp=256)])
+def test_oracle_gradient_estimates_match_the_analytic_gradient(oracle, make):
+    """The oracle's estimateSolutionAndGradient (antithetic pairs, stratified first steps,
+    control variates from a first call) against grad u of the manufactured solution."""
+    pr = make()
+    n, D = pr.points.shape
+    eq = np.full(n, A.ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT, np.int32)
+    extra = dict(gradient_mean=np.zeros((n, D)), gradient_m2=np.zeros((n, D)),
+                 n_gradient_estimates=np.zeros(n, np.int32))
+    st = None
+    for call in range(2):
+        st = run_oracle_with(oracle, pr, st, estimation_quantity=eq, extra_stats=extra)
+    _, grad, _ = P.eval_analytic(pr.solution, pr.points)
+    g = st["gradient_mean"].reshape(n, D)
+    ng = st["n_gradient_estimates"].astype(np.float64)
+    assert np.all(ng == 2 * pr.n_walks)
+    se = np.sqrt(st["gradient_m2"].reshape(n, D) / np.maximum(ng - 1, 1)[:, None] / ng[:, None])
+    z = (g - grad) / np.maximum(se, 1e-12)
+    assert np.mean(np.abs(z) <= 4) > 0.98
+    assert abs(np.mean(z)) < 0.3
