@@ -276,6 +276,17 @@ int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, cons
                                const float* rand_nums, int32_t* out_found, float* out_pt,
                                float* out_normal, float* out_pdf, int memory);
 
+/*
+ * FcpwDirichletBoundaryHandler::buildAccelerationStructure with the tree built on the GPU
+ * (no counterpart in the reference, which builds on the CPU): a linear BVH over Morton codes
+ * of the primitive centroids, collapsed to the same 4-wide node layout. Absorbing boundaries
+ * only (reflecting boundaries need adjacency, cones and silhouette trees, built on the host).
+ * positions / indices may live in host or device memory (`memory`).  Queries answer as on a
+ * host-built tree; a tree deeper than the traversal stack returns ZGPU_ERR_UNSUPPORTED.
+ */
+int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
+                                   const int* indices, int n_prims, int memory, zgpu_boundary** out);
+
 /* ------------------------------- solve ----------------------------------- */
 /*
  * WalkOnSpheres<T,DIM>::solve (point_estimation/walk_on_spheres.h:38-44, batch over points

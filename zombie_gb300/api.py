@@ -491,8 +491,26 @@ class GpuDirichletBoundaryHandler(_BoundaryHandler):
     kind = A.ZGPU_BOUNDARY_ABSORBING
 
     def build_acceleration_structure(self, positions, indices, build_bvh=True, enable_bvh_vectorization=False,
-                                     print_stats=False):
-        self._build(positions, indices)
+                                     print_stats=False, build_on_device=False):
+        """build_on_device: the tree is built on the GPU (linear BVH over Morton codes,
+        zgpu_boundary_create_on_device); positions/indices may then be CUDA tensors."""
+        if not build_on_device:
+            self._build(positions, indices)
+            return
+        self.close()
+        dev = hasattr(positions, "is_cuda") and positions.is_cuda
+        if dev:
+            pos, idx = positions.contiguous(), indices.contiguous()
+            nv, npr = int(pos.shape[0]), int(idx.shape[0])
+        else:
+            pos = np.ascontiguousarray(positions, np.float32).reshape(-1, self.dim)
+            idx = np.ascontiguousarray(indices, np.int32).reshape(-1, self.dim)
+            nv, npr = pos.shape[0], idx.shape[0]
+        h = C.c_void_p()
+        check(lib().zgpu_boundary_create_on_device(self.ctx.h, self.dim, A.ptr(pos), nv, A.ptr(idx), npr,
+                                                   A.ZGPU_MEM_DEVICE if dev else A.ZGPU_MEM_HOST, C.byref(h)))
+        self.h = h
+        self.n_prims = npr
 
 
 class GpuNeumannBoundaryHandler(_BoundaryHandler):

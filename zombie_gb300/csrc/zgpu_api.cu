@@ -258,6 +258,74 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     return ZGPU_OK;
 }
 
+int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
+                                   const int* indices, int n_prims, int memory, zgpu_boundary** out) {
+    if (!ctx || !out) return fail(ZGPU_ERR_INVALID_ARG, "context/out is NULL");
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
+    if (n_prims < 0 || n_vertices < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative sizes");
+    if (n_prims > 0 && (!positions || !indices)) return fail(ZGPU_ERR_INVALID_ARG, "positions/indices are NULL");
+    if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    // host copies: index validation and the signed volume
+    std::vector<float> hp((size_t)n_vertices * dim);
+    std::vector<int> hi((size_t)n_prims * dim);
+    if (memory == ZGPU_MEM_HOST) {
+        std::memcpy(hp.data(), positions, hp.size() * sizeof(float));
+        std::memcpy(hi.data(), indices, hi.size() * sizeof(int));
+    } else {
+        ZG_CUDA(cudaMemcpy(hp.data(), positions, hp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        ZG_CUDA(cudaMemcpy(hi.data(), indices, hi.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    for (int v : hi)
+        if (v < 0 || v >= n_vertices) return fail(ZGPU_ERR_INVALID_ARG, "index %d outside [0, %d)", v, n_vertices);
+    double vol = 0.0;
+    for (int i = 0; i < n_prims; i++) {
+        const float* a = &hp[(size_t)hi[(size_t)i * dim] * dim];
+        const float* b = &hp[(size_t)hi[(size_t)i * dim + 1] * dim];
+        if (dim == 2) {
+            vol += 0.5 * ((double)a[0] * b[1] - (double)a[1] * b[0]);
+        } else {
+            const float* c = &hp[(size_t)hi[(size_t)i * dim + 2] * dim];
+            vol += (((double)a[1] * b[2] - (double)a[2] * b[1]) * c[0] + ((double)a[2] * b[0] - (double)a[0] * b[2]) * c[1] +
+                    ((double)a[0] * b[1] - (double)a[1] * b[0]) * c[2]) / 6.0;
+        }
+    }
+    const float* dp = positions;
+    const int* di = indices;
+    float* tp = nullptr;
+    int* ti = nullptr;
+    if (memory == ZGPU_MEM_HOST && n_prims > 0) {
+        ZG_CUDA(cudaMalloc(&tp, hp.size() * sizeof(float)));
+        if (cudaMalloc(&ti, hi.size() * sizeof(int)) != cudaSuccess) { cudaFree(tp); return fail(ZGPU_ERR_OUT_OF_MEMORY, "staging"); }
+        cudaMemcpy(tp, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice);
+        cudaMemcpy(ti, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice);
+        dp = tp; di = ti;
+    }
+    float4 *nodes = nullptr, *prims = nullptr;
+    int* primIndex = nullptr;
+    int nNodes = 0, depth = 0;
+    cudaError_t e = buildWideBvhOnDevice(dim, dp, di, n_prims, s, &nodes, &nNodes, &prims, &primIndex, &depth);
+    if (tp) cudaFree(tp);
+    if (ti) cudaFree(ti);
+    if (e == cudaErrorNotSupported)
+        return fail(ZGPU_ERR_UNSUPPORTED, "device-built BVH deeper than the traversal stack (%d levels); build on the host",
+                    kMaxWideDepth);
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? ZGPU_ERR_OUT_OF_MEMORY : ZGPU_ERR_CUDA, "device BVH build: %s",
+                    cudaGetErrorString(e));
+    zgpu_boundary* b = new zgpu_boundary();
+    b->ctx = ctx; b->dim = dim; b->kind = ZGPU_BOUNDARY_ABSORBING; b->nPrims = n_prims; b->nNodes = nNodes;
+    b->depth = depth; b->signedVolume = (float)vol;
+    b->nodes = nodes; b->prims = prims; b->primIndex = primIndex;
+    b->view.nodes = nodes; b->view.prims = prims; b->view.primIndex = primIndex;
+    b->view.nNodes = nNodes; b->view.nPrims = n_prims;
+    b->view.stackEntries = stackEntriesForDepth(std::max(depth, 1));
+    *out = b;
+    return ZGPU_OK;
+}
+
 int zgpu_boundary_destroy(zgpu_boundary* b) {
     if (!b) return ZGPU_OK;
     if (b->ctx) cudaSetDevice(b->ctx->device);

@@ -106,6 +106,10 @@ cudaStream_t cacheStream(const zgpu_cache* c);
 int contextDevice(const zgpu_context* ctx);
 size_t scanScratchElems(int64_t n);
 
+// device-side LBVH build of an absorbing boundary's 4-wide tree (zgpu_devbuild.cu)
+cudaError_t buildWideBvhOnDevice(int D, const float* pos, const int* idx, int nP, cudaStream_t s, float4** outNodes,
+                                 int* outNodeCount, float4** outPrims, int** outPrimIndex, int* outDepth);
+
 // accessors into the C ABI objects (zgpu_api.cu)
 void setLastError(const char* msg);
 bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind);
