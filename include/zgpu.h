@@ -174,7 +174,9 @@ typedef struct zgpu_solve_options {
     int32_t query_mode;        /* closest-point queries of Walk on Spheres and Robin star radii of
                                   Walk on Stars: 0 auto, 1 one lane per query, 2 the whole warp
                                   per query (large scenes) */
-    int64_t step_budget;       /* per-walk-state hard cap on device loop iterations (0 -> max_walk_length+1) */
+    int64_t step_budget;       /* per-walk-state cap on device loop iterations (0: none beyond
+                                  max_walk_length); a walk that reaches it is dropped and the
+                                  solve returns ZGPU_ERR_TIMEOUT_BUDGET */
 } zgpu_solve_options;
 
 /* counters returned by a solve */

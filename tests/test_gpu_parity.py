@@ -538,3 +538,24 @@ def test_device_built_bvh_answers_like_the_host_built_one(zgpu, dim, level):
     h2 = dev.intersect(x, z, d, tm, on)
     assert np.array_equal(h1[0], h2[0]) and np.array_equal(h1[3], h2[3])
     assert np.array_equal(host.count_hits(x, d, tm), dev.count_hits(x, d, tm))
+
+
+def test_step_budget_drops_walks_and_reports_it(zgpu):
+    """zgpu_solve_options.step_budget caps the loop iterations of a walk state: a budget
+    below the walks' lengths returns ZGPU_ERR_TIMEOUT_BUDGET, a generous one changes nothing."""
+    from zombie_gb300 import _lib
+    from zombie_gb300.runner import GpuProblem
+    pr = P.laplace_wos_2d(n_segments=512, grid=16, spp=32)
+    gp = GpuProblem(pr)
+    ref = gp.device_arrays()
+    gp.solve(ref)
+    opt = A.SolveOptions()
+    opt.step_budget = 2
+    with pytest.raises(_lib.ZgpuError) as e:
+        gp.solve(gp.device_arrays(), options=opt)
+    assert e.value.status == A.ZGPU_ERR_TIMEOUT_BUDGET
+    opt.step_budget = 100000
+    d = gp.device_arrays()
+    gp.solve(d, options=opt)
+    for k in ("n_solution_estimates", "total_walk_length"):
+        assert np.array_equal(ref[k].cpu().numpy(), d[k].cpu().numpy())

@@ -703,6 +703,8 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     // (per-query work varies by orders of magnitude between walks, which idles the lanes of
     // a one-lane-per-query traversal); the walk kernel then needs no per-thread stack
     const int queryMode = opt ? opt->query_mode : 0;
+    if (opt && opt->step_budget < 0) return fail(ZGPU_ERR_INVALID_ARG, "step_budget must be >= 0");
+    P.stepBudget = opt ? opt->step_budget : 0;
     if (queryMode < 0 || queryMode > 2) return fail(ZGPU_ERR_INVALID_ARG, "query_mode must be 0, 1 or 2");
     const int walkStackEntries = P.stackEntries;
     if (solver == ZGPU_SOLVER_WALK_ON_SPHERES && P.sc.hasAbs && !batched)
@@ -713,8 +715,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
         P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
     if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
-                                              : walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f || P.batchScreened,
-                                                                         threads, P);
+                                              : walkKernelMaxBlocksPerSM(D, solver, threads, P);
     P.stackEntries = walkStackEntries;
     int blocks = ctx->numSMs * perSM;
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
@@ -796,6 +797,9 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
         cudaEventElapsedTime(&report->kernel_ms, ctx->ev[1], ctx->ev[2]);
         cudaEventElapsedTime(&report->total_ms, ctx->ev[0], ctx->ev[3]);
     }
+    if (errWord & kErrBudget)
+        return fail(ZGPU_ERR_TIMEOUT_BUDGET, "a walk state exceeded step_budget = %lld loop iterations; its walk was "
+                                             "dropped", (long long)P.stepBudget);
     if (errWord)
         return fail(ZGPU_ERR_DEVICE_STATE,
                     "device error word 0x%x (1: traversal stack, 2: split stack, 8: scene id outside the table, "

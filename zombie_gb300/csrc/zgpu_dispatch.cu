@@ -78,13 +78,13 @@ cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, c
     return wos ? WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::walk(p, blocks, threads, s)
                : WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::walk(p, blocks, threads, s);
 }
-int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, const SolveParams& p) {
+int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p) {
     const bool wos = solver == ZGPU_SOLVER_WALK_ON_SPHERES;
     const size_t smem = walkSmemBytes(p, threads);
-    if (dim == 2) return wos ? WalkLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>::maxBlocksPerSM(screened, threads, smem)
-                             : WalkLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::maxBlocksPerSM(screened, threads, smem);
-    return wos ? WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::maxBlocksPerSM(screened, threads, smem)
-               : WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::maxBlocksPerSM(screened, threads, smem);
+    if (dim == 2) return wos ? WalkLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>::maxBlocksPerSM(p, threads, smem)
+                             : WalkLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::maxBlocksPerSM(p, threads, smem);
+    return wos ? WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::maxBlocksPerSM(p, threads, smem)
+               : WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::maxBlocksPerSM(p, threads, smem);
 }
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s) {
     return dim == 2 ? Launch<2>::finalize(p, s) : Launch<3>::finalize(p, s);

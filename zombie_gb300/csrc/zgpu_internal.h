@@ -82,6 +82,9 @@ struct SolveParams {
     int coop;
     // Walk on Stars on a Robin boundary: star radii answered by the whole warp
     int coopStar;
+    // cap on loop iterations per walk state (0: none); a walk that reaches it is dropped and
+    // kErrBudget raised
+    long long stepBudget;
 };
 
 constexpr int kSplitStack = 8;
@@ -96,7 +99,7 @@ cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);
 cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStream_t s);
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
-int walkKernelMaxBlocksPerSM(int dim, int solver, bool screened, int threads, const SolveParams& p);
+int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p);
 // neural cache pass over the walk records (zgpu_cache.cu)
 cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
                                   int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,

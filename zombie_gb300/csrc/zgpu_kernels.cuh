@@ -58,10 +58,20 @@ ZG_D void storeSplit(float4* slot, V<D> pt, V<D> nrm, V<D> prevDir, float prevDi
     slot[2] = make_float4(v[8], v[9], v[10], v[11]);
 }
 
-template <int D, int SOLVER, bool SCREENED, bool BATCHED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED, bool COOP>
 struct Walker {
+    // warp-cooperative queries are compiled into their own kernels: closest points for Walk
+    // on Spheres, Robin star radii for Walk on Stars
+    static constexpr bool kCoopClosest = COOP && SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES;
+    static constexpr bool kCoopStar = COOP && SOLVER == ZGPU_SOLVER_WALK_ON_STARS;
     const SolveParams& P;
-    const SceneDesc* sc;   // the walk's problem: P.sc, or its row of the scene table
+    const SceneDesc* sc;   // batched solves: the walk's row of the scene table
+    // the walk's problem; single-scene kernels read the kernel parameter itself, so its fields
+    // stay parameter-space loads
+    ZG_D const SceneDesc& SC() const {
+        if constexpr (BATCHED) return *sc;
+        else return P.sc;
+    }
     DevicePde<D> pde;
     // walk identity
     int point;
@@ -85,6 +95,7 @@ struct Walker {
     // loop state
     float distAbs, fsr;
     bool firstStep, cpValid;
+    long long iters;        // loop iterations of this walk state (step budget)
     bool queryPending;      // cooperative mode: the closest-point query of this state is due
     bool radiusPending;     // cooperative mode: the Robin star radius of this step is due
     bool radiusReady;       // ... and answered (pendingR) -- the step resumes from there
@@ -101,29 +112,29 @@ struct Walker {
 
     ZG_D Walker(const SolveParams& p, TravStack s) : P(p), S(s) {
         sc = &P.sc;
-        pde.p = &sc->pde;
+        pde.p = &SC().pde;
         steps = escaped = exceeded = rr = 0;
         err = 0;
-        g.sqrtLambda = sqrtf(fmaxf(sc->pde.absorption_coeff, 0.0f));
+        g.sqrtLambda = sqrtf(fmaxf(SC().pde.absorption_coeff, 0.0f));
     }
 
     ZG_D void closestQuery() {
-        if (P.coop && sc->hasAbs) { queryPending = true; cpValid = false; return; }
-        if (sc->hasAbs) {
-            ClosestHit<D> h = closestPoint<D>(sc->absorbing, pt, S, err);
+        if (kCoopClosest && SC().hasAbs) { queryPending = true; cpValid = false; return; }
+        if (SC().hasAbs) {
+            ClosestHit<D> h = closestPoint<D>(SC().absorbing, pt, S, err);
             distAbs = h.d;
             cpPt = h.pt;
-            if (h.slot >= 0) cpN = primNormal<D>(loadPrim<D>(sc->absorbing, h.slot));
+            if (h.slot >= 0) cpN = primNormal<D>(loadPrim<D>(SC().absorbing, h.slot));
             cpValid = true;
         } else {
-            distAbs = bboxDistance<D>(*sc, pt);
+            distAbs = bboxDistance<D>(SC(), pt);
             cpValid = false;
         }
     }
 
     ZG_D void resetGreens() {
         // a new GreensFnBall for every dequeued state (walk_on_spheres.h:376-383, walk_on_stars.h:618-625)
-        g.yukawa = sc->pde.absorption_coeff > 0.0f && sc->ws.steps_before_applying_tikhonov == 0;
+        g.yukawa = SC().pde.absorption_coeff > 0.0f && SC().ws.steps_before_applying_tikhonov == 0;
     }
 
     ZG_D void start(long long id, int pointIndex) {
@@ -160,6 +171,7 @@ struct Walker {
         radiusPending = false;
         radiusReady = false;
         pendingCode = -1;
+        iters = 0;
         resetGreens();
         if (flags & kPointGradient) startGradient(w);
     }
@@ -173,7 +185,7 @@ struct Walker {
     // a Latin hypercube over the point's 2M first-step samples of this call (M = walks, or
     // pairs), the strata assigned by a per-point permutation.
     __device__ __noinline__ void startGradient(long long w) {
-        const zgpu_walk_settings& ws = sc->ws;
+        const zgpu_walk_settings& ws = SC().ws;
         const bool anti = ws.use_gradient_antithetic_variates != 0;
         const long long pair = anti ? (w >> 1) : w;
         const bool mirror = anti && (w & 1);
@@ -197,7 +209,7 @@ struct Walker {
         sGradDir = vzero<D>();
         if (!ws.ignore_source_contribution) {
             const float nrmG = g.norm();
-            if (sc->pde.is_source_constant) {
+            if (SC().pde.is_source_constant) {
                 firstSrc = nrmG * pde.source(x0);
             } else {
                 const V<D> dirS = sphereFromUniform<D>(us);
@@ -233,7 +245,7 @@ struct Walker {
         distAbs = d;
         cpPt = pt;
         if (slot >= 0) {
-            Prim<D> t = loadPrim<D>(sc->absorbing, slot);
+            Prim<D> t = loadPrim<D>(SC().absorbing, slot);
             V<D> q;
             closestOnPrim(t, pt, q);
             cpPt = q;
@@ -259,6 +271,7 @@ struct Walker {
         flip = pointFlip;
         fsr = 0.0f;
         firstStep = true;
+        iters = 0;
         resetGreens();
         closestQuery();
         splits++;
@@ -266,7 +279,7 @@ struct Walker {
 
     // weight window (walk_on_spheres.h:193-226, walk_on_stars.h:309-343); true -> terminated
     ZG_D bool weightWindow() {
-        const float sT = sc->ws.splitting_threshold, rT = sc->ws.russian_roulette_threshold;
+        const float sT = SC().ws.splitting_threshold, rT = SC().ws.russian_roulette_threshold;
         if (thr > sT) {
             float left = thr - sT;
             thr = sT;
@@ -292,12 +305,12 @@ struct Walker {
             if (code == kRussianRoulette) rr++;
             float term = 0.0f;
             bool payTerminal = code == kReached || (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && code == kExceeded);
-            if (payTerminal && !sc->ws.ignore_absorbing_boundary_contribution) {
+            if (payTerminal && !SC().ws.ignore_absorbing_boundary_contribution) {
                 // projectToAbsorbingBoundary then pde.dirichlet (walk_on_spheres.h:294-318, walk_on_stars.h:493-516)
-                if (sc->hasAbs) {
-                    if (!cpValid && !P.coop) closestQuery();
+                if (SC().hasAbs) {
+                    if (!cpValid && !kCoopClosest) closestQuery();
                     bool aligned = false;
-                    if (sc->ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
+                    if (SC().ws.solve_double_sided) aligned = dot(pt - cpPt, cpN) > 0.0f;
                     term = pde.dirichlet(cpPt, aligned);
                 } else {
                     term = pde.dirichlet(pt, false);
@@ -347,10 +360,10 @@ struct Walker {
 
     // --------------------------------------------------------------- Walk on Spheres step
     ZG_D bool stepWoS() {
-        const zgpu_walk_settings& ws = sc->ws;
+        const zgpu_walk_settings& ws = SC().ws;
         if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) {
             // the terminal value needs the projection: in cooperative mode the warp answers first
-            if (P.coop && sc->hasAbs && !cpValid) { pendingCode = kReached; closestQuery(); return true; }
+            if (kCoopClosest && SC().hasAbs && !cpValid) { pendingCode = kReached; closestQuery(); return true; }
             return terminate(kReached);
         }
         if (P.cacheMinDist > 0.0f && wlen > 0 && distAbs >= P.cacheMinDist && cacheTerminate()) return false;
@@ -358,7 +371,7 @@ struct Walker {
         g.update(pt, distAbs);
         if (!ws.ignore_source_contribution) {
             float src;
-            if (sc->pde.is_source_constant) {
+            if (SC().pde.is_source_constant) {
                 src = g.norm() * pde.source(pt);
             } else {
                 V<D> d = sampleSphere<D>(rng);
@@ -371,15 +384,15 @@ struct Walker {
         pt = pt + distAbs * dir;
         cpValid = false;
         thr *= g.directionSampledPoissonKernel(pt);
-        if (outsideBox(*sc, pt.v, D)) return terminate(kEscaped);
+        if (outsideBox(SC(), pt.v, D)) return terminate(kEscaped);
         if (weightWindow()) return terminate(kRussianRoulette);
         wlen++;
         if (wlen >= ws.max_walk_length) {
             // WoS pays the terminal value of the projected point: query first when cooperative
-            if (P.coop && sc->hasAbs) { pendingCode = kExceeded; closestQuery(); return true; }
+            if (kCoopClosest && SC().hasAbs) { pendingCode = kExceeded; closestQuery(); return true; }
             return terminate(kExceeded);
         }
-        if (sc->pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        if (SC().pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
         closestQuery();
         return true;
     }
@@ -387,50 +400,49 @@ struct Walker {
     // --------------------------------------------------------------- Walk on Stars step
     // answer of a cooperative Robin star-radius query (the shrink of walk_on_stars.h:393-397)
     ZG_D void setStarRadius(float r) {
-        const float eps = sc->ws.epsilon_shell_for_reflecting_boundary;
+        const float eps = SC().ws.epsilon_shell_for_reflecting_boundary;
         pendingR = eps <= distAbs ? fmaxf(kRadiusShrink * r, eps) : r;
         radiusPending = false;
         radiusReady = true;
     }
 
     ZG_D bool stepWoSt() {
-        const zgpu_walk_settings& ws = sc->ws;
-        if (radiusReady) { radiusReady = false; return stepWoStFrom(pendingR); }
-        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
-        if (P.cacheMinDist > 0.0f && wlen > 0 && !onRefl && distAbs >= P.cacheMinDist) {
-            bool far = !sc->hasRefl || closestPoint<D>(sc->reflecting, pt, S, err).d >= P.cacheMinDist;
-            if (far && cacheTerminate()) return false;
-        }
+        const zgpu_walk_settings& ws = SC().ws;
         float R;
-        if (firstStep && fsr > 0.0f) {
-            R = fsr;
+        if (kCoopStar && radiusReady) {
+            // resumed after the warp answered this step's Robin star radius
+            radiusReady = false;
+            R = pendingR;
         } else {
-            flip = false;
-            if (ws.solve_double_sided && onRefl && prevDist > 0.0f && dot(prevDir, nrm) < 0.0f) {
-                nrm = -nrm;
-                flip = true;
+            if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+            if (P.cacheMinDist > 0.0f && wlen > 0 && !onRefl && distAbs >= P.cacheMinDist) {
+                bool far = !SC().hasRefl || closestPoint<D>(SC().reflecting, pt, S, err).d >= P.cacheMinDist;
+                if (far && cacheTerminate()) return false;
             }
-            if (ws.steps_before_using_maximal_spheres <= wlen) {
-                R = distAbs;
-            } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
-                R = ws.epsilon_shell_for_reflecting_boundary;
-            } else if (P.coopStar && sc->hasRefl) {
-                radiusPending = true;          // the warp answers, the step resumes in stepWoStFrom
-                return true;
+            if (firstStep && fsr > 0.0f) {
+                R = fsr;
             } else {
-                R = sc->hasRefl ? starRadius<D>(sc->reflecting, pt, ws.epsilon_shell_for_reflecting_boundary, distAbs,
-                                              ws.silhouette_precision, flip, S, err)
-                              : distAbs;
-                if (sc->hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
-                    R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
+                flip = false;
+                if (ws.solve_double_sided && onRefl && prevDist > 0.0f && dot(prevDir, nrm) < 0.0f) {
+                    nrm = -nrm;
+                    flip = true;
+                }
+                if (ws.steps_before_using_maximal_spheres <= wlen) {
+                    R = distAbs;
+                } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
+                    R = ws.epsilon_shell_for_reflecting_boundary;
+                } else if (kCoopStar && SC().hasRefl) {
+                    radiusPending = true;      // the warp answers, then the step resumes here
+                    return true;
+                } else {
+                    R = SC().hasRefl ? starRadius<D>(SC().reflecting, pt, ws.epsilon_shell_for_reflecting_boundary,
+                                                     distAbs, ws.silhouette_precision, flip, S, err)
+                                     : distAbs;
+                    if (SC().hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
+                        R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
+                }
             }
         }
-        return stepWoStFrom(R);
-    }
-
-    // the Walk on Stars step from its star radius R on
-    __device__ __noinline__ bool stepWoStFrom(float R) {
-        const zgpu_walk_settings& ws = sc->ws;
         steps++;
         g.update(pt, R);
         V<D> dir = sampleSphere<D>(rng);
@@ -439,13 +451,13 @@ struct Walker {
         V<D> hitPt, hitN;
         float hitDist;
         bool hit = false;
-        if (sc->hasRefl) {
-            RayHit<D> h = intersectRay<D>(sc->reflecting, origin, dir, R, false, S, err);
+        if (SC().hasRefl) {
+            RayHit<D> h = intersectRay<D>(SC().reflecting, origin, dir, R, false, S, err);
             if (h.slot >= 0) {
                 hit = true;
                 hitDist = h.t;
                 hitPt = origin + h.t * dir;
-                hitN = primNormal<D>(loadPrim<D>(sc->reflecting, h.slot));
+                hitN = primNormal<D>(loadPrim<D>(SC().reflecting, h.slot));
             }
         }
         if (!hit) {
@@ -454,13 +466,13 @@ struct Walker {
             hitN = vzero<D>();
         }
         // reflecting boundary contribution (walk_on_stars.h:190-250)
-        if (sc->hasRefl && !ws.ignore_reflecting_boundary_contribution) {
+        if (SC().hasRefl && !ws.ignore_reflecting_boundary_contribution) {
             float u[D];
 #pragma unroll
             for (int i = 0; i < D; i++) u[i] = rng.uniform();
             V<D> bpt, bn;
             float pdf;
-            if (sampleBoundary<D>(sc->reflecting, pt, R, u, bpt, bn, pdf)) {
+            if (sampleBoundary<D>(SC().reflecting, pt, R, u, bpt, bn, pdf)) {
                 V<D> toS = bpt - pt;
                 float dS = len(toS);
                 float alpha = onRefl ? 2.0f : 1.0f;
@@ -483,7 +495,7 @@ struct Walker {
                     float sl = len(seg);
                     bool occluded = false;
                     if (sl > 0.0f) {
-                        RayHit<D> oh = intersectRay<D>(sc->reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
+                        RayHit<D> oh = intersectRay<D>(SC().reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
                         occluded = oh.slot >= 0;
                     }
                     if (!occluded) {
@@ -511,31 +523,39 @@ struct Walker {
         if (onRefl && prevDist > kFltEps) {
             float kappa = 0.0f;
             V<D> n = nrm;
-            if (!sc->pde.are_robin_conditions_pure_neumann) {
+            if (!SC().pde.are_robin_conditions_pure_neumann) {
                 bool f2 = false;
                 if (ws.solve_double_sided) { f2 = dot(prevDir, nrm) < 0.0f; if (f2) n = -n; }
                 kappa = pde.robinCoeff(ws.solve_double_sided && f2);
             }
             float refl = g.reflectance(prevDist, prevDir, n, kappa);
-            float maxRefl = sc->pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
+            float maxRefl = SC().pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
             stepThr = fminf(fmaxf(refl, 0.0f), maxRefl);
         } else {
             stepThr = g.directionSampledPoissonKernel(pt);
         }
         thr *= stepThr;
-        if (!onRefl && outsideBox(*sc, pt.v, D)) return terminate(kEscaped);
+        if (!onRefl && outsideBox(SC(), pt.v, D)) return terminate(kEscaped);
         if (weightWindow()) return terminate(kRussianRoulette);
         wlen++;
         if (wlen >= ws.max_walk_length) return terminate(kExceeded);
-        if (sc->pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        if (SC().pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
         closestQuery();
         firstStep = false;
         return true;
     }
 
     ZG_D bool step() {
+        if (P.stepBudget > 0 && ++iters > P.stepBudget) {
+            // the iteration budget of this state ran out: drop the walk and report it
+            err |= kErrBudget;
+            success = false;
+            nStack = 0;
+            queryPending = radiusPending = false;
+            return false;
+        }
         if (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES) {
-            if (pendingCode >= 0) { const int code = pendingCode; pendingCode = -1; return terminate(code); }
+            if (kCoopClosest && pendingCode >= 0) { const int code = pendingCode; pendingCode = -1; return terminate(code); }
             return stepWoS();
         }
         return stepWoSt();
@@ -563,13 +583,14 @@ ZG_D int warpFindPoint(const SolveParams& P, long long id, int lane) {
     return (int)(lo + 31 - __clz(b));
 }
 
-template <int D, int SOLVER, bool SCREENED, bool BATCHED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED, bool COOP>
 __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant__ SolveParams P) {
     extern __shared__ int dynStack[];
     TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
                 (int)blockDim.x, P.stackEntries};
     CoopWork* coopWork = reinterpret_cast<CoopWork*>(dynStack + 2 * P.stackEntries * blockDim.x) + (threadIdx.x >> 5);
-    Walker<D, SOLVER, SCREENED, BATCHED> W(P, S);
+    using WalkerT = Walker<D, SOLVER, SCREENED, BATCHED, COOP>;
+    WalkerT W(P, S);
     W.splitSlots = P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack;
     const int lane = threadIdx.x & 31;
     const long long total = (long long)__ldg(P.walkStart + P.nPoints);
@@ -601,7 +622,7 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
         }
         if (!__any_sync(kFull, active)) break;
         if (active) active = W.step();
-        if (SOLVER == ZGPU_SOLVER_WALK_ON_STARS && P.coopStar) {
+        if constexpr (WalkerT::kCoopStar) {
             // Robin star radii of this round, one at a time with the whole warp
             unsigned qm = __ballot_sync(kFull, active && W.radiusPending);
             while (qm) {
@@ -617,7 +638,7 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
                 if (lane == src) W.setStarRadius(r);
             }
         }
-        if (SOLVER == ZGPU_SOLVER_WALK_ON_SPHERES && P.coop) {
+        if constexpr (WalkerT::kCoopClosest) {
             // closest-point queries of this round, one at a time with the whole warp
             unsigned qm = __ballot_sync(kFull, active && W.queryPending);
             while (qm) {
@@ -926,32 +947,42 @@ inline size_t walkSmemBytes(const SolveParams& p, int threads) {
 // walk kernel launchers, explicitly instantiated per (dimension, solver) in zgpu_walk_<D>d_<solver>.cu
 template <int D, int SOLVER>
 struct WalkLaunch {
-    static cudaError_t walk(const SolveParams& p, int blocks, int threads, cudaStream_t s) {
-        size_t smem = walkSmemBytes(p, threads);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (p.sceneId) {
-            // batched many-solve: each walk reads its row of the scene table (2D scenes)
+    // the walk kernel for a solve: screened or not, batched (2D scene tables) or one scene,
+    // warp-cooperative queries or one lane per query; nullptr for a combination not built
+    static const void* kernel(bool screened, bool batched, bool coop) {
+        if (batched) {
             if constexpr (D == 2) {
-                cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (p.batchScreened) detail::walkKernel<D, SOLVER, true, true><<<blocks, threads, smem, s>>>(p);
-                else detail::walkKernel<D, SOLVER, false, true><<<blocks, threads, smem, s>>>(p);
-                return cudaGetLastError();
+                if (coop) return nullptr;
+                return screened ? (const void*)detail::walkKernel<D, SOLVER, true, true, false>
+                                : (const void*)detail::walkKernel<D, SOLVER, false, true, false>;
             } else {
-                return cudaErrorNotSupported;
+                return nullptr;
             }
         }
-        if (p.sc.pde.absorption_coeff > 0.0f) detail::walkKernel<D, SOLVER, true, false><<<blocks, threads, smem, s>>>(p);
-        else detail::walkKernel<D, SOLVER, false, false><<<blocks, threads, smem, s>>>(p);
-        return cudaGetLastError();
+        if (coop) return screened ? (const void*)detail::walkKernel<D, SOLVER, true, false, true>
+                                  : (const void*)detail::walkKernel<D, SOLVER, false, false, true>;
+        return screened ? (const void*)detail::walkKernel<D, SOLVER, true, false, false>
+                        : (const void*)detail::walkKernel<D, SOLVER, false, false, false>;
     }
-    static int maxBlocksPerSM(bool screened, int threads, size_t smem) {
+    static const void* kernelFor(const SolveParams& p) {
+        const bool batched = p.sceneId != nullptr;
+        const bool screened = batched ? p.batchScreened != 0 : p.sc.pde.absorption_coeff > 0.0f;
+        return kernel(screened, batched, p.coop || p.coopStar);
+    }
+    static cudaError_t walk(const SolveParams& p, int blocks, int threads, cudaStream_t s) {
+        const void* f = kernelFor(p);
+        if (!f) return cudaErrorNotSupported;
+        const size_t smem = walkSmemBytes(p, threads);
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        void* args[] = {const_cast<SolveParams*>(&p)};
+        return cudaLaunchKernel(f, dim3(blocks), dim3(threads), args, smem, s);
+    }
+    static int maxBlocksPerSM(const SolveParams& p, int threads, size_t smem) {
         int n = 0;
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(detail::walkKernel<D, SOLVER, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        const void* f = screened ? (const void*)detail::walkKernel<D, SOLVER, true, false>
-                                 : (const void*)detail::walkKernel<D, SOLVER, false, false>;
+        const void* f = kernelFor(p);
+        if (!f) return 1;
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess) return 1;
         return n > 0 ? n : 1;
     }

@@ -153,7 +153,7 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
     int numSMs = 0;
     cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device);
     const int threads = 128;
-    int perSM = walkKernelMaxBlocksPerSM(D, solver, pde->absorption_coeff > 0.0f, threads, P);
+    int perSM = walkKernelMaxBlocksPerSM(D, solver, threads, P);
     int blocks = numSMs * perSM;
 
     // the accumulators are cleared by the prepare kernel; the counters and error word here
