@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define ZGPU_ABI_VERSION 2
+#define ZGPU_ABI_VERSION 3
 
 /* ------------------------------------------------------------------------- */
 /* status codes                                                               */
@@ -72,13 +72,22 @@ typedef struct zgpu_analytic {
     float d;
 } zgpu_analytic;
 
-/* A dense grid field (utils/dense_grid.h): row-major values over [grid_min, grid_max]. */
+/*
+ * A dense grid field (DenseGrid<float, 1, DIM>, utils/dense_grid.h) over the box
+ * [grid_min, grid_max], cell-centred samples, row-major with the last axis fastest
+ * (value of cell (i, j[, k]) at (i * shape[1] + j)[* shape[2] + k]).  Lookups clamp to the
+ * grid: nearest cell, or (enable_interpolation) bi/trilinear between cell centres with the
+ * blend fractions clamped to [0, 1] (dense_grid.h:264-355).  values_aligned is the grid
+ * returned for returnBoundaryNormalAlignedValue = true (getDenseGridCallback2/4,
+ * dense_grid.h:442-560); NULL -> values.
+ */
 typedef struct zgpu_grid {
-    const float* values;   /* device or host pointer, see zgpu_pde.memory */
+    const float* values;          /* device or host pointer, see zgpu_pde.memory */
+    const float* values_aligned;
     int32_t shape[3];
     float grid_min[3];
     float grid_max[3];
-    int32_t bilinear;      /* 1: (bi/tri)linear lookup, 0: nearest */
+    int32_t enable_interpolation;
 } zgpu_grid;
 
 /*
@@ -100,7 +109,9 @@ typedef struct zgpu_pde {
     zgpu_grid source_grid;
     zgpu_grid dirichlet_grid;
     zgpu_grid robin_grid;
-    int32_t memory;            /* memory space of the grid value arrays */
+    zgpu_grid robin_coeff_grid;
+    int32_t memory;            /* memory space of the grid value arrays (host arrays are copied
+                                  to the device by each solve) */
 } zgpu_pde;
 
 /* WalkSettings (point_estimation/common.h:19-91): same fields, same order. */
@@ -145,6 +156,8 @@ typedef struct zgpu_sample_points {
     float* first_sphere_radius;
     const int32_t* estimate_normal_aligned;
     const int32_t* scene_id;   /* batched many-solve: index into the scene table, NULL -> 0 */
+    const float* direction_for_derivative;  /* [n*dim] SamplePoint::directionForDerivative
+                                               (common.h:185), NULL -> (1, 0[, 0]) */
 } zgpu_sample_points;
 
 /*
@@ -153,6 +166,9 @@ typedef struct zgpu_sample_points {
  * merges its walks into these arrays with the parallel Welford merge of
  * SampleStatistics::merge (common.h:268-310), in FP64.
  * gradient_mean/gradient_m2 are [n*dim] and may be NULL when no point asks for gradients.
+ * total_first_source_contribution and total_derivative_contribution are the running sums
+ * behind getMeanFirstSourceContribution and getEstimatedDerivative (common.h:346-355), added
+ * to by gradient walks; either may be NULL (the source control variate is then 0).
  */
 typedef struct zgpu_sample_statistics {
     int32_t memory;
@@ -164,6 +180,8 @@ typedef struct zgpu_sample_statistics {
     double* gradient_mean;
     double* gradient_m2;
     int32_t* n_gradient_estimates;
+    double* total_first_source_contribution;
+    double* total_derivative_contribution;
 } zgpu_sample_statistics;
 
 /* launch and engine options that have no counterpart in the reference */

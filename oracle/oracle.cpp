@@ -91,8 +91,14 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
                         else { Vec<D> cp, cn; int pi; q.reflecting->closestPoint(p, cp, cn, dR, pi); }
                         dB = std::min(dB, dR);
                     }
-                    const float cvB = (ws->use_gradient_control_variates && nPrev > 0) ? (float)st->solution_mean[i] : 0.0f;
-                    s.gradEstimate(solver, p, dB, pts->n_walks[i], pts->seed[i], nPrev, cvB, ps, gs);
+                    const bool cv = ws->use_gradient_control_variates && nPrev > 0;
+                    const float cvB = cv ? (float)st->solution_mean[i] : 0.0f;
+                    const float cvS = (cv && st->total_first_source_contribution)
+                                          ? (float)(st->total_first_source_contribution[i] / (double)nPrev) : 0.0f;
+                    Vec<D> dirD;
+                    if (pts->direction_for_derivative) dirD = load<D>(pts->direction_for_derivative + i * D);
+                    else dirD[0] = 1.0f;
+                    s.gradEstimate(solver, p, dB, pts->n_walks[i], pts->seed[i], nPrev, cvB, cvS, dirD, ps, gs);
                     fsr = 0.99f * dB;
                 } else if (solver == ZGPU_SOLVER_WALK_ON_SPHERES)
                     s.wosEstimate(p, type, pts->dist_to_absorbing[i], pts->n_walks[i], pts->seed[i], nPrev > 0, aligned, fsr, ps);
@@ -111,6 +117,10 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
                         }
                     }
                     st->n_gradient_estimates[i] = gt;
+                }
+                if (gradient) {
+                    if (st->total_first_source_contribution) st->total_first_source_contribution[i] += gs.firstSource;
+                    if (st->total_derivative_contribution) st->total_derivative_contribution[i] += gs.derivative;
                 }
                 if (pts->first_sphere_radius) pts->first_sphere_radius[i] = fsr;
                 localSteps += ps.steps;
@@ -329,15 +339,24 @@ extern "C" void orc_offset_point(int dim, const float* p, const float* n, float*
     if (dim == 2) store<2>(offsetPointAlongDirection<2>(load<2>(p), load<2>(n)), out);
     else store<3>(offsetPointAlongDirection<3>(load<3>(p), load<3>(n)), out);
 }
-extern "C" void orc_eval_pde(int dim, const zgpu_pde* pde, int64_t n, const float* x, const float* nrm, float* src, float* dir,
-                  float* rob) {
+// the PDE's fields at n points: source, Dirichlet, Robin data and Robin coefficient (any
+// output may be NULL), the boundary-normal-aligned values when `aligned`
+extern "C" void orc_eval_pde(int dim, const zgpu_pde* pde, int64_t n, const float* x, const float* nrm, int aligned,
+                             float* src, float* dir, float* rob, float* kappa) {
+    const bool al = aligned != 0;
     for (int64_t i = 0; i < n; i++) {
         if (dim == 2) {
             Pde<2> p{pde}; Vec<2> xx = load<2>(x + i * 2), nn = nrm ? load<2>(nrm + i * 2) : Vec<2>();
-            if (src) src[i] = p.source(xx); if (dir) dir[i] = p.dirichlet(xx, false); if (rob) rob[i] = p.robin(xx, nn, false);
+            if (src) src[i] = p.source(xx);
+            if (dir) dir[i] = p.dirichlet(xx, al);
+            if (rob) rob[i] = p.robin(xx, nn, al);
+            if (kappa) kappa[i] = p.robinCoeff(xx, nn, al);
         } else {
             Pde<3> p{pde}; Vec<3> xx = load<3>(x + i * 3), nn = nrm ? load<3>(nrm + i * 3) : Vec<3>();
-            if (src) src[i] = p.source(xx); if (dir) dir[i] = p.dirichlet(xx, false); if (rob) rob[i] = p.robin(xx, nn, false);
+            if (src) src[i] = p.source(xx);
+            if (dir) dir[i] = p.dirichlet(xx, al);
+            if (rob) rob[i] = p.robin(xx, nn, al);
+            if (kappa) kappa[i] = p.robinCoeff(xx, nn, al);
         }
     }
 }

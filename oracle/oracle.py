@@ -65,7 +65,7 @@ def lib():
         L.orc_bessel.argtypes = [i32, C.c_double]
         L.orc_pcg32.argtypes = [u64, u64, i32, vp, vp]
         L.orc_offset_point.argtypes = [i32, vp, vp, vp]
-        L.orc_eval_pde.argtypes = [i32, vp, i64, vp, vp, vp, vp, vp]
+        L.orc_eval_pde.argtypes = [i32, vp, i64, vp, vp, i32, vp, vp, vp, vp]
         L.orc_solve.argtypes = [i32, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_uint64)]
         L.orc_hardware_threads.restype = i32
         L.orc_counters.argtypes = [vp]
@@ -184,13 +184,16 @@ def bessel(which, x):
     return lib().orc_bessel({"i0": 0, "i1": 1, "k0": 2, "k1": 3}[which], float(x))
 
 
-def eval_pde(dim, pde, x, normals=None):
+def eval_pde(dim, pde, x, normals=None, aligned=False, with_robin_coeff=False):
+    """source, dirichlet, robin (and the Robin coefficient) of the oracle's PDE at x."""
     x = _f32(x).reshape(-1, dim)
     n = x.shape[0]
     src = np.zeros(n, np.float32); dr = np.zeros(n, np.float32); rb = np.zeros(n, np.float32)
+    kp = np.zeros(n, np.float32)
     nn = None if normals is None else _f32(normals).reshape(-1, dim)
-    lib().orc_eval_pde(dim, C.byref(pde), n, A.ptr(x), A.ptr(nn), A.ptr(src), A.ptr(dr), A.ptr(rb))
-    return src, dr, rb
+    lib().orc_eval_pde(dim, C.byref(pde), n, A.ptr(x), A.ptr(nn), int(aligned), A.ptr(src), A.ptr(dr), A.ptr(rb),
+                       A.ptr(kp))
+    return (src, dr, rb, kp) if with_robin_coeff else (src, dr, rb)
 
 
 def solve(solver, dim, absorbing, reflecting, domain_min, domain_max, pde, settings, points, stats,
@@ -211,12 +214,14 @@ def solve(solver, dim, absorbing, reflecting, domain_min, domain_max, pde, setti
     sp.n = points["pt"].shape[0]
     sp.memory = A.ZGPU_MEM_HOST
     for name in ("pt", "normal", "type", "estimation_quantity", "dist_to_absorbing", "dist_to_reflecting",
-                 "n_walks", "seed", "first_sphere_radius", "estimate_normal_aligned", "scene_id"):
+                 "n_walks", "seed", "first_sphere_radius", "estimate_normal_aligned", "scene_id",
+                 "direction_for_derivative"):
         setattr(sp, name, A.ptr(points.get(name)))
     st = A.SampleStatisticsC()
     st.memory = A.ZGPU_MEM_HOST
     for name in ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
-                 "gradient_mean", "gradient_m2", "n_gradient_estimates"):
+                 "gradient_mean", "gradient_m2", "n_gradient_estimates", "total_first_source_contribution",
+                 "total_derivative_contribution"):
         setattr(st, name, A.ptr(stats.get(name)))
     steps = C.c_uint64(0)
     if n_threads is None:

@@ -40,11 +40,53 @@ inline AnalyticEval<D> evalAnalytic(const zgpu_analytic& a, const Vec<D>& x) {
     return r;
 }
 
+// DenseGrid<float, 1, DIM>::operator() (utils/dense_grid.h:264-355): cell-centred samples over
+// [grid_min, grid_max], row-major with the last axis fastest; nearest cell, or multilinear
+// between the cell centres with indices clamped to the grid and fractions to [0, 1].  The
+// normal-aligned grid (getDenseGridCallback2/4) answers aligned lookups when given.
+template <int D>
+inline float gridValue(const zgpu_grid& g, const Vec<D>& x, bool aligned) {
+    const float* v = (aligned && g.values_aligned) ? g.values_aligned : g.values;
+    int i0[D], i1[D];
+    float f[D];
+    for (int i = 0; i < D; i++) {
+        int n = g.shape[i];
+        float t = (x[i] - g.grid_min[i]) / (g.grid_max[i] - g.grid_min[i]);
+        if (g.enable_interpolation) {
+            float u = n == 1 ? 0.0f : t * (float)n - 0.5f;
+            i0[i] = std::clamp((int)std::floor(u), 0, n - 1);
+            i1[i] = std::clamp(i0[i] + 1, 0, n - 1);
+            f[i] = std::clamp(u - (float)i0[i], 0.0f, 1.0f);
+        } else {
+            i0[i] = i1[i] = std::clamp((int)std::floor(t * (float)n), 0, n - 1);
+            f[i] = 0.0f;
+        }
+    }
+    if (!g.enable_interpolation) {
+        int64_t k = 0;
+        for (int i = 0; i < D; i++) k = k * g.shape[i] + i0[i];
+        return v[k];
+    }
+    float r = 0.0f;
+    for (int corner = 0; corner < (1 << D); corner++) {
+        int64_t k = 0;
+        float w = 1.0f;
+        for (int i = 0; i < D; i++) {
+            bool hi = (corner >> i) & 1;
+            k = k * g.shape[i] + (hi ? i1[i] : i0[i]);
+            w *= hi ? f[i] : 1.0f - f[i];
+        }
+        r += w * v[k];
+    }
+    return r;
+}
+
 template <int D>
 struct Pde {
     const zgpu_pde* p;
-    float robinCoeff(const Vec<D>&, const Vec<D>&, bool aligned) const {
+    float robinCoeff(const Vec<D>& x, const Vec<D>&, bool aligned) const {
         if (p->robin_coeff_kind == ZGPU_FIELD_ZERO) return 0.0f;
+        if (p->robin_coeff_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->robin_coeff_grid, x, aligned);
         return aligned ? p->robin_coeff_value_aligned : p->robin_coeff_value;
     }
     float source(const Vec<D>& x) const {
@@ -53,11 +95,13 @@ struct Pde {
             AnalyticEval<D> e = evalAnalytic<D>(p->solution, x);
             return -e.lap + p->absorption_coeff * e.u;
         }
+        if (p->source_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->source_grid, x, false);
         return 0.0f;
     }
     float dirichlet(const Vec<D>& x, bool aligned) const {
         if (p->dirichlet_kind == ZGPU_FIELD_CONSTANT) return aligned ? p->dirichlet_value_aligned : p->dirichlet_value;
         if (p->dirichlet_kind == ZGPU_FIELD_ANALYTIC) return evalAnalytic<D>(p->solution, x).u;
+        if (p->dirichlet_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->dirichlet_grid, x, aligned);
         return 0.0f;
     }
     // Robin data h = du/dn + kappa u with n the outward normal (Walkin' Robin, Miller et al. 2024)
@@ -68,6 +112,7 @@ struct Pde {
             float s = aligned ? -1.0f : 1.0f;
             return s * dot(e.grad, n) + robinCoeff(x, n, aligned) * e.u;
         }
+        if (p->robin_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->robin_grid, x, aligned);
         return 0.0f;
     }
     // pde.h:62-78
@@ -167,6 +212,7 @@ struct PointStats {
 struct GradStats {
     double mean[3] = {0, 0, 0}, m2[3] = {0, 0, 0};
     int n = 0;
+    double firstSource = 0.0, derivative = 0.0;   // addFirstSource/DerivativeContribution sums
     void add(const double* x, int D) {
         n += 1;
         for (int i = 0; i < D; i++) { double d = x[i] - mean[i]; mean[i] += d / n; m2[i] += d * (x[i] - mean[i]); }
@@ -495,12 +541,49 @@ struct Solver {
         return v;
     }
 
+    // cosine-weighted hemisphere direction about the last axis (core/sampling.h:124-129,
+    // :186-216: 2D uniform abscissa; 3D Shirley-Chiu concentric disk lifted to the hemisphere)
+    static Vec<D> hemisphereCosine(const float* u) {
+        Vec<D> v;
+        if (D == 2) {
+            float x = 2.0f * u[0] - 1.0f;
+            v[0] = x; v[1] = std::sqrt(std::max(0.0f, 1.0f - x * x));
+        } else {
+            float a = 2.0f * u[0] - 1.0f, b = 2.0f * u[1] - 1.0f, r = 0.0f, phi = 0.0f;
+            if (a != 0.0f || b != 0.0f) {
+                if (std::fabs(a) > std::fabs(b)) { r = a; phi = 0.25f * kPi * (b / a); }
+                else { r = b; phi = 0.5f * kPi - 0.25f * kPi * (a / b); }
+            }
+            v[0] = r * std::cos(phi); v[1] = r * std::sin(phi); v[D - 1] = std::sqrt(std::max(0.0f, 1.0f - r * r));
+        }
+        return v;
+    }
+    static float hemisphereCosinePdf(float c) { return D == 2 ? 0.5f * c : c / kPi; }
+    // direction d given in the frame whose last axis is n (core/sampling.h:151-157, :236-246;
+    // 3D: the orthonormal basis of Duff et al., JCGT 2017)
+    static Vec<D> toFrame(const Vec<D>& n, const Vec<D>& d) {
+        Vec<D> r;
+        if (D == 2) {
+            r[0] = d[0] * n[1] + d[1] * n[0];
+            r[1] = -d[0] * n[0] + d[1] * n[1];
+        } else {
+            float sg = std::copysign(1.0f, n[D - 1]);
+            float a = -1.0f / (sg + n[D - 1]);
+            float b = n[0] * n[1] * a;
+            float t1[3] = {1.0f + sg * n[0] * n[0] * a, sg * b, -sg * n[0]};
+            float t2[3] = {b, sg + n[1] * n[1] * a, -n[1]};
+            for (int i = 0; i < D; i++) r[i] = d[0] * t1[i] + d[1] * t2[i] + d[D - 1] * n[i];
+        }
+        return r;
+    }
+
     // estimateSolutionAndGradient (walk_on_spheres.h:417-593, walk_on_stars.h:665-848) with the
     // parallel restatement the device uses: antithetic walks 2k, 2k+1 share pcg32 stream k and
     // mirror the first step; the first-step samples form a Latin hypercube assigned by a
-    // per-point permutation; the control variate cvB is the previous call's estimate.
+    // per-point permutation; the control variates are the previous call's estimate (cvB) and
+    // mean first source contribution (cvS); dirD is directionForDerivative.
     void gradEstimate(int solver, const Vec<D>& pt, float distB, int nWalks, uint64_t seed, int nPrev, float cvB,
-                      PointStats& st, GradStats& gs) const {
+                      float cvS, const Vec<D>& dirD, PointStats& st, GradStats& gs) const {
         const bool anti = ws.use_gradient_antithetic_variates != 0;
         const int count = nWalks <= 0 ? 0 : (anti ? 2 * std::max(1, nWalks / 2) : nWalks);
         const float R0 = 0.99f * distB;
@@ -538,9 +621,18 @@ struct Solver {
                 }
                 s.totalSourceContribution += s.throughput * firstSrc;
             }
-            Vec<D> dirB = sphereFromUniform(ub);
+            Vec<D> dirB;
+            float bPdf;
+            if (ws.use_cosine_sampling_for_derivatives) {
+                Vec<D> loc = hemisphereCosine(ub);
+                if (rng.nextFloat() < 0.5f) loc[D - 1] = -loc[D - 1];
+                bPdf = 0.5f * hemisphereCosinePdf(std::fabs(loc[D - 1]));
+                dirB = toFrame(dirD, loc);
+            } else {
+                dirB = sphereFromUniform(ub);
+                bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
+            }
             if (mirror) dirB = -dirB;
-            const float bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
             Vec<D> yb = pt + R0 * dirB;
             s.throughput *= g->poissonKernelCentre() / bPdf;
             Vec<D> bDir = (1.0f / (bPdf * s.throughput)) * g->poissonKernelGradient(yb);
@@ -570,8 +662,15 @@ struct Solver {
                 st.splits += splits;
                 double gv[3] = {0, 0, 0};
                 const float bc = total - firstSrc;
-                for (int i = 0; i < D; i++) gv[i] = (double)((bc - cvB) * bDir[i] + firstSrc * sDir[i]);
+                float deriv = 0.0f;
+                for (int i = 0; i < D; i++) {
+                    float gb = (bc - cvB) * bDir[i], gsrc = (firstSrc - cvS) * sDir[i];
+                    deriv += gb * dirD[i] + gsrc * dirD[i];
+                    gv[i] = (double)(gb + gsrc);
+                }
                 gs.add(gv, D);
+                gs.firstSource += firstSrc;
+                gs.derivative += deriv;
             }
         }
     }

@@ -181,6 +181,12 @@ def test_boundary_sampling_is_unbiased(zgpu):
 
 
 # ------------------------------------------------------------------------- solvers
+def _screened_2d(grid=20, spp=512):
+    pr = P.laplace_wos_2d(n_segments=1024, grid=grid, spp=spp)
+    pr.pde = P.make_pde(pr.solution, sigma=2.0, source=True)      # f = 2u: a non-constant source
+    return pr
+
+
 def _gpu_and_oracle(zgpu, oracle, pr):
     from zombie_gb300.runner import GpuProblem, summarize
     import test_oracle_solvers as T
@@ -209,6 +215,16 @@ CASES = {
     "wost_screened_2d": lambda: P.mixed_wost_2d(n_segments=2048, grid=24, spp=256, sigma=1.0),
     "wost_robin_3d": lambda: P.robin_wost_3d(level=4, n_points=400, spp=256),
     "wos_screened_3d": lambda: P.screened_wos_3d(level=4, n_points=400, spp=256),
+    # PDE data from dense grids sampled at cell centres (bilinear / trilinear / nearest)
+    "wos_laplace_2d_grid": lambda: P.with_grid_fields(P.laplace_wos_2d(n_segments=1024, grid=40, spp=256)),
+    "wos_screened_2d_grid": lambda: P.with_grid_fields(_screened_2d(grid=32, spp=256), ("dirichlet", "source")),
+    "wost_mixed_2d_nearest_grid": lambda: P.with_grid_fields(P.mixed_wost_2d(n_segments=2048, grid=24, spp=256),
+                                                             shape=(4096, 4096), interpolate=False),
+    "wost_robin_3d_kappa_grid": lambda: P.with_grid_fields(
+        P.robin_wost_3d(level=4, n_points=400, spp=256), (), shape=(48, 48, 48),
+        robin_coeff=lambda x: 1.5 + 0.5 * np.sin(2.0 * x[:, 0]) * np.cos(x[:, 1])),
+    "wos_screened_3d_grid": lambda: P.with_grid_fields(P.screened_wos_3d(level=4, n_points=400, spp=256),
+                                                       ("dirichlet", "source"), shape=(96, 96, 96)),
 }
 
 
@@ -226,6 +242,47 @@ def test_solver_matches_oracle_and_exact(zgpu, oracle, case):
     ez = _exact_z(g)
     assert abs(ez.mean()) <= 0.5
     assert np.mean(np.abs(ez) > 3.5) <= 0.04
+
+
+@pytest.mark.parametrize("make,fields,shape", [
+    (lambda: P.laplace_wos_2d(n_segments=1024, grid=40, spp=128), ("dirichlet",), (1024, 1024)),
+    (lambda: _screened_2d(grid=32, spp=128), ("dirichlet", "source"), (1024, 1024)),
+    (lambda: P.screened_wos_3d(level=4, n_points=400, spp=128), ("dirichlet", "source"), (128, 128, 128))])
+def test_dense_grid_fields_follow_the_analytic_fields(zgpu, make, fields, shape):
+    """The device's grid lookups (host grids copied by the solve) replace analytic g and f
+    without changing a walk: equal walk lengths, estimates within the interpolation error."""
+    from zombie_gb300.runner import GpuProblem
+    a, b = make(), P.with_grid_fields(make(), fields, shape=shape)
+    ga, gb = GpuProblem(a), GpuProblem(b)
+    xa, xb = ga.host_arrays(), gb.host_arrays()
+    ra, rb = ga.solve(xa), gb.solve(xb)
+    assert ra.total_steps == rb.total_steps and rb.error_word == 0
+    assert np.array_equal(xa["total_walk_length"], xb["total_walk_length"])
+    d = xb["solution_mean"] - xa["solution_mean"]
+    assert np.max(np.abs(d)) < 3e-3
+    assert abs(d.mean()) < 2e-4
+
+
+def test_dense_grid_fields_are_validated(zgpu):
+    """Grid fields with an empty shape, an empty box or no values are rejected; the
+    allocation-free entry point takes device-resident grids only."""
+    from zombie_gb300.runner import GpuProblem
+    from zombie_gb300 import ZgpuError
+    pr = P.with_grid_fields(P.laplace_wos_2d(n_segments=256, grid=8, spp=4), shape=(16, 16))
+    for breakage in ("shape", "box", "values"):
+        pr2 = P.with_grid_fields(P.laplace_wos_2d(n_segments=256, grid=8, spp=4), shape=(16, 16))
+        if breakage == "shape":
+            pr2.pde.dirichlet_grid.shape[1] = 0
+        elif breakage == "box":
+            pr2.pde.dirichlet_grid.grid_max[0] = pr2.pde.dirichlet_grid.grid_min[0]
+        else:
+            pr2.pde.dirichlet_grid.values = None
+        gp = GpuProblem(pr2)
+        with pytest.raises(ZgpuError):
+            gp.solve(gp.host_arrays())
+    gp = GpuProblem(pr)
+    rep = gp.solve(gp.host_arrays())
+    assert rep.error_word == 0 and rep.total_steps > 0
 
 
 def test_wos_walks_reproduce_oracle_walks(zgpu, oracle):
@@ -321,14 +378,19 @@ def test_invalid_arguments_return_errors(zgpu):
     assert st == A.ZGPU_ERR_INVALID_ARG
     st = L.zgpu_solve(ctx.h, 7, None, None, None, None, None, None, None)
     assert st == A.ZGPU_ERR_INVALID_ARG
-    # dense-grid fields are reported as unsupported, not silently ignored
+    # a grid field without values is an error, not silently a zero field
     from zombie_gb300.runner import GpuProblem
     gp = GpuProblem(P.laplace_wos_2d(n_segments=64, grid=4, spp=4))
     pde = gp.pde.to_c()
     pde.source_kind = A.ZGPU_FIELD_GRID
     with pytest.raises(_lib.ZgpuError) as e:
         gp.solver.solve_arrays(pde, gp.problem.settings, gp.host_arrays())
-    assert e.value.status == A.ZGPU_ERR_UNSUPPORTED
+    assert e.value.status == A.ZGPU_ERR_INVALID_ARG and "no values" in str(e.value)
+    # an unknown field kind too
+    pde.source_kind = 9
+    with pytest.raises(_lib.ZgpuError) as e:
+        gp.solver.solve_arrays(pde, gp.problem.settings, gp.host_arrays())
+    assert e.value.status == A.ZGPU_ERR_INVALID_ARG
 
 
 @pytest.mark.parametrize("make", [lambda: P.laplace_wos_2d(n_segments=1024, grid=32, spp=64),
@@ -502,6 +564,90 @@ def test_gradient_estimates_match_the_oracle(zgpu, oracle):
                  / st["n_gradient_estimates"][:, None])
     assert np.mean(np.abs(gg - og) <= 0.1 * se + 1e-6) > 0.95
     assert np.all(np.abs(gg - og) <= 3 * se + 1e-6)
+
+
+def _axis_directions(n, D, seed):
+    rng = np.random.default_rng(seed)
+    axis = rng.integers(0, D, n)
+    v = np.zeros((n, D), np.float32)
+    v[np.arange(n), axis] = rng.choice([-1.0, 1.0], n)
+    return v, axis
+
+
+@pytest.mark.parametrize("make", [lambda: P.laplace_wos_2d(n_segments=1024, grid=24, spp=512), _screened_2d,
+                                  lambda: P.mixed_wost_2d(n_segments=1024, grid=20, spp=512),
+                                  lambda: P.screened_wos_3d(level=4, n_points=300, spp=512)])
+def test_cosine_sampled_directional_derivatives(zgpu, make):
+    """useCosineSamplingForDerivatives: first steps cosine-weighted about each point's
+    directionForDerivative; getEstimatedDerivative (running sum of the walks' directional
+    derivatives) matches grad u . direction within its standard errors and equals the
+    gradient mean projected on the direction."""
+    import torch
+    from zombie_gb300.runner import GpuProblem
+    pr = make()
+    pr.settings.use_cosine_sampling_for_derivatives = 1
+    gp = GpuProblem(pr)
+    d = gp.device_arrays(gradients=True)
+    n, D = pr.points.shape
+    dirs, axis = _axis_directions(n, D, 11)
+    d.arrays["direction_for_derivative"] = torch.from_numpy(dirs).to(d["pt"].device)
+    gp.solve(d)
+    gp.solve(d)
+    ng = d["n_gradient_estimates"].cpu().numpy().astype(np.float64)
+    assert np.all(ng == 2 * pr.n_walks)
+    deriv = d["total_derivative_contribution"].cpu().numpy() / ng
+    g = d["gradient_mean"].cpu().numpy().reshape(n, D)
+    proj = np.sum(g * dirs, axis=1)
+    assert np.max(np.abs(deriv - proj)) <= 1e-4 * np.sqrt(np.mean(proj ** 2))
+    _, grad, _ = P.eval_analytic(pr.solution, pr.points)
+    se = np.sqrt(d["gradient_m2"].cpu().numpy().reshape(n, D)[np.arange(n), axis] / np.maximum(ng - 1, 1) / ng)
+    z = (deriv - np.sum(grad * dirs, axis=1)) / np.maximum(se, 1e-12)
+    assert np.mean(np.abs(z) <= 4) > 0.99
+    assert abs(np.mean(z)) < 4 / np.sqrt(n)
+
+
+def test_cosine_sampled_derivatives_match_the_oracle(zgpu, oracle):
+    """GPU and oracle on the same cosine-sampled gradient walks with a non-constant source
+    (source control variate from the first call's mean first source contribution) and
+    arbitrary unit directions: gradients, directional derivatives and first source sums
+    agree far inside their standard errors."""
+    import sys
+    import os
+    import torch
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_oracle_solvers import run_oracle_with
+    from zombie_gb300.runner import GpuProblem
+    pr = _screened_2d(grid=12, spp=128)
+    pr.settings.use_cosine_sampling_for_derivatives = 1
+    n, D = pr.points.shape
+    v = np.random.default_rng(12).normal(size=(n, D))
+    dirs = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    eq = np.full(n, A.ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT, np.int32)
+    extra = dict(gradient_mean=np.zeros((n, D)), gradient_m2=np.zeros((n, D)), n_gradient_estimates=np.zeros(n, np.int32),
+                 total_first_source_contribution=np.zeros(n), total_derivative_contribution=np.zeros(n))
+    st = None
+    for _ in range(2):
+        st = run_oracle_with(oracle, pr, st, estimation_quantity=eq, extra_stats=extra, direction=dirs)
+    gp = GpuProblem(pr)
+    d = gp.device_arrays(gradients=True)
+    d.arrays["direction_for_derivative"] = torch.from_numpy(dirs).to(d["pt"].device)
+    gp.solve(d)
+    gp.solve(d)
+    ng = st["n_gradient_estimates"].astype(np.float64)
+    assert np.array_equal(d["n_gradient_estimates"].cpu().numpy(), st["n_gradient_estimates"])
+    se = np.sqrt(st["gradient_m2"].reshape(n, D) / np.maximum(ng - 1, 1)[:, None] / ng[:, None])
+    gg = d["gradient_mean"].cpu().numpy().reshape(n, D)
+    og = st["gradient_mean"].reshape(n, D)
+    assert np.mean(np.abs(gg - og) <= 0.1 * se + 1e-6) > 0.95
+    assert np.all(np.abs(gg - og) <= 3 * se + 1e-6)
+    sed = np.sqrt(np.sum(se ** 2, axis=1))
+    gd = d["total_derivative_contribution"].cpu().numpy() / ng
+    od = st["total_derivative_contribution"] / ng
+    assert np.mean(np.abs(gd - od) <= 0.1 * sed + 1e-6) > 0.95
+    fs_g = d["total_first_source_contribution"].cpu().numpy()
+    fs_o = st["total_first_source_contribution"]
+    assert np.any(fs_o != 0.0)
+    assert np.allclose(fs_g, fs_o, rtol=1e-3, atol=1e-3 * np.max(np.abs(fs_o)))
 
 
 @pytest.mark.parametrize("dim,level", [(2, None), (3, 3), (3, 7)])

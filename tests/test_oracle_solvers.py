@@ -11,10 +11,13 @@ def run_oracle(oracle, pr, n_threads=None, seeds=None):
     ab = oracle.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
     rf = None
     if pr.reflecting is not None and len(pr.reflecting[1]):
-        k = None
+        kmin = kmax = None
         if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN:
-            k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32)
-        rf = oracle.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
+            if pr.robin_coeff_range is not None:
+                kmin, kmax = pr.robin_coeff_range
+            else:
+                kmin = kmax = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32)
+        rf = oracle.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=kmin, kmax=kmax,
                              silhouette_precision=pr.ignore_silhouette_precision)
     n = pr.points.shape[0]
     if ab is not None:
@@ -30,7 +33,7 @@ def run_oracle(oracle, pr, n_threads=None, seeds=None):
     return st, steps
 
 
-def run_oracle_with(oracle, pr, st=None, estimation_quantity=None, extra_stats=None, n_threads=None):
+def run_oracle_with(oracle, pr, st=None, estimation_quantity=None, extra_stats=None, n_threads=None, direction=None):
     """run_oracle with extra point fields and statistics, accumulating into st across calls."""
     D = pr.dim
     ab = oracle.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
@@ -44,6 +47,8 @@ def run_oracle_with(oracle, pr, st=None, estimation_quantity=None, extra_stats=N
                first_sphere_radius=np.zeros(n, np.float32))
     if estimation_quantity is not None:
         pts["estimation_quantity"] = estimation_quantity
+    if direction is not None:
+        pts["direction_for_derivative"] = np.ascontiguousarray(direction, np.float32)
     if st is None:
         st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
                   total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
@@ -155,3 +160,102 @@ def test_oracle_gradient_estimates_match_the_analytic_gradient(oracle, make):
     z = (g - grad) / np.maximum(se, 1e-12)
     assert np.mean(np.abs(z) <= 4) > 0.98
     assert abs(np.mean(z)) < 0.3
+
+
+def _axis_directions(n, D, seed):
+    """Signed coordinate axes: the gradient moments of that axis are then exactly the
+    moments of the directional derivative."""
+    rng = np.random.default_rng(seed)
+    axis = rng.integers(0, D, n)
+    v = np.zeros((n, D), np.float32)
+    v[np.arange(n), axis] = rng.choice([-1.0, 1.0], n)
+    return v, axis
+
+
+def _screened_2d():
+    pr = P.laplace_wos_2d(n_segments=512, grid=16, spp=256)
+    pr.pde = P.make_pde(pr.solution, sigma=2.0, source=True)      # f = 2u: a non-constant source
+    return pr
+
+
+@pytest.mark.parametrize("make", [lambda: P.laplace_wos_2d(n_segments=512, grid=16, spp=256), _screened_2d])
+def test_oracle_cosine_sampled_directional_derivatives(oracle, make):
+    """useCosineSamplingForDerivatives (walk_on_spheres.h:500-504): first steps drawn about
+    each point's directionForDerivative; the directional derivative (getEstimatedDerivative,
+    the running sum of (boundary + source gradient) . direction) matches grad u . direction,
+    and equals the gradient mean projected on the direction.  The source control variate is
+    the mean first source contribution of the earlier walks (getMeanFirstSourceContribution)."""
+    pr = make()
+    pr.settings.use_cosine_sampling_for_derivatives = 1
+    n, D = pr.points.shape
+    dirs, axis = _axis_directions(n, D, 3)
+    eq = np.full(n, A.ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT, np.int32)
+    extra = dict(gradient_mean=np.zeros((n, D)), gradient_m2=np.zeros((n, D)), n_gradient_estimates=np.zeros(n, np.int32),
+                 total_first_source_contribution=np.zeros(n), total_derivative_contribution=np.zeros(n))
+    st = None
+    for call in range(2):
+        st = run_oracle_with(oracle, pr, st, estimation_quantity=eq, extra_stats=extra, direction=dirs)
+    u, grad, _ = P.eval_analytic(pr.solution, pr.points)
+    ng = st["n_gradient_estimates"].astype(np.float64)
+    assert np.all(ng == 2 * pr.n_walks)
+    assert np.array_equal(st["n_solution_estimates"], st["n_gradient_estimates"])
+    g = st["gradient_mean"].reshape(n, D)
+    deriv = st["total_derivative_contribution"] / ng
+    proj = np.sum(g * dirs, axis=1)
+    scale = np.sqrt(np.mean(proj ** 2))
+    assert np.max(np.abs(deriv - proj)) <= 1e-4 * scale
+    se = np.sqrt(st["gradient_m2"].reshape(n, D)[np.arange(n), axis] / np.maximum(ng - 1, 1) / ng)
+    z = (deriv - np.sum(grad * dirs, axis=1)) / np.maximum(se, 1e-12)
+    assert np.mean(np.abs(z) <= 3.5) > 0.98
+    assert abs(np.mean(z)) < 4 / np.sqrt(n)
+    if pr.pde.is_source_constant == 0:
+        # the first source contributions are kept: their mean is the source part of u
+        fs = st["total_first_source_contribution"] / st["n_solution_estimates"]
+        assert np.all(np.isfinite(fs)) and np.any(fs != 0.0)
+    else:
+        assert np.all(st["total_first_source_contribution"] == 0.0)
+
+
+def test_oracle_cosine_sampling_concentrates_on_the_direction(oracle):
+    """Cosine-weighted first steps about the direction lower the variance of the directional
+    derivative against uniform first steps (same walks otherwise)."""
+    out = {}
+    for cosine in (0, 1):
+        pr = P.laplace_wos_2d(n_segments=512, grid=10, spp=256)
+        pr.settings.use_cosine_sampling_for_derivatives = cosine
+        pr.settings.use_gradient_control_variates = 0
+        n, D = pr.points.shape
+        dirs = np.tile(np.array([[1.0, 0.0]], np.float32), (n, 1))
+        eq = np.full(n, A.ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT, np.int32)
+        extra = dict(gradient_mean=np.zeros((n, D)), gradient_m2=np.zeros((n, D)),
+                     n_gradient_estimates=np.zeros(n, np.int32))
+        st = run_oracle_with(oracle, pr, None, estimation_quantity=eq, extra_stats=extra, direction=dirs)
+        out[cosine] = np.median(st["gradient_m2"].reshape(n, D)[:, 0] / np.maximum(st["n_gradient_estimates"] - 1, 1))
+    assert out[1] < out[0]
+
+
+@pytest.mark.parametrize("make,fields", [(lambda: P.laplace_wos_2d(n_segments=512, grid=10, spp=256), ("dirichlet",)),
+                                         (_screened_2d, ("dirichlet", "source"))])
+def test_oracle_dense_grid_fields_follow_the_analytic_fields(oracle, make, fields):
+    """g and f read from 512^2 bilinear grids sampled from the same fields: the walks are the
+    same (same streams, same lengths) and the estimates differ by the interpolation error."""
+    a = make()
+    b = P.with_grid_fields(make(), fields, shape=(512, 512))
+    sa, _ = run_oracle(oracle, a)
+    sb, _ = run_oracle(oracle, b)
+    assert np.array_equal(sa["total_walk_length"], sb["total_walk_length"])
+    d = sb["solution_mean"] - sa["solution_mean"]
+    assert np.max(np.abs(d)) < 3e-3
+    assert abs(d.mean()) < 2e-4
+
+
+def test_oracle_robin_coefficient_grid_is_unbiased(oracle):
+    """A spatially varying Robin coefficient read from a trilinear grid (Robin data h = du/dn
+    + kappa(x) u, per-primitive coefficient bounds from the grid's range): estimates stay
+    within their standard errors of u."""
+    pr = P.with_grid_fields(P.robin_wost_3d(level=3, n_points=60, spp=128), (), shape=(24, 24, 24),
+                            robin_coeff=lambda x: 1.5 + 0.5 * np.sin(2.0 * x[:, 0]) * np.cos(x[:, 1]))
+    st, _ = run_oracle(oracle, pr)
+    z = zscores(st, pr.exact())
+    assert abs(z.mean()) < 0.5
+    assert np.mean(np.abs(z) > 3.5) < 0.05

@@ -8,11 +8,13 @@ include/zgpu.h; there is no CPU fallback.
 import types as _types
 
 from . import _abi
-from .api import (BranchTraversalWeight, Context, EstimationQuantity, Field, GeometricQueries,
+from .api import (BranchTraversalWeight, Context, DenseGrid, EstimationQuantity, Field, GeometricQueries,
                   GpuDirichletBoundaryHandler, GpuNeumannBoundaryHandler, GpuRobinBoundaryHandler,
                   IgnoreCandidateSilhouette, NeuralCache, PDE, SampleArrays, SamplePoint, SampleStatistics, SampleType,
                   WalkCompletionCode, WalkOnSpheres, WalkOnStars, WalkSettings, create_sample_statistics_list,
-                  default_context, populate_geometric_queries_for_dirichlet_boundary,
+                  default_context, get_dense_grid_dirichlet_callback, get_dense_grid_robin_callback,
+                  get_dense_grid_robin_coefficient_callback, get_dense_grid_source_callback,
+                  populate_geometric_queries_for_dirichlet_boundary,
                   populate_geometric_queries_for_neumann_boundary, populate_geometric_queries_for_robin_boundary)
 from ._lib import ZgpuError
 
@@ -63,6 +65,11 @@ Solvers = _types.SimpleNamespace(
 )
 
 Utils = _types.SimpleNamespace(
+    DenseGrid=_dim_factory(DenseGrid),
+    get_dense_grid_source_callback=get_dense_grid_source_callback,
+    get_dense_grid_dirichlet_callback=get_dense_grid_dirichlet_callback,
+    get_dense_grid_robin_callback=get_dense_grid_robin_callback,
+    get_dense_grid_robin_coefficient_callback=get_dense_grid_robin_coefficient_callback,
     FcpwDirichletBoundaryHandler=_dim_factory(GpuDirichletBoundaryHandler),
     FcpwNeumannBoundaryHandler=_dim_factory(GpuNeumannBoundaryHandler),
     FcpwRobinBoundaryHandler=_dim_factory(GpuRobinBoundaryHandler),

@@ -5,7 +5,7 @@ offsets against the compiled library.
 """
 import ctypes as C
 
-ZGPU_ABI_VERSION = 2
+ZGPU_ABI_VERSION = 3
 
 ZGPU_OK = 0
 ZGPU_ERR_INVALID_ARG = 1
@@ -67,10 +67,11 @@ class Analytic(C.Structure):
 class Grid(C.Structure):
     _fields_ = [
         ("values", C.c_void_p),
+        ("values_aligned", C.c_void_p),
         ("shape", C.c_int32 * 3),
         ("grid_min", C.c_float * 3),
         ("grid_max", C.c_float * 3),
-        ("bilinear", C.c_int32),
+        ("enable_interpolation", C.c_int32),
     ]
 
 
@@ -88,6 +89,7 @@ class Pde(C.Structure):
         ("source_grid", Grid),
         ("dirichlet_grid", Grid),
         ("robin_grid", Grid),
+        ("robin_coeff_grid", Grid),
         ("memory", C.c_int32),
     ]
 
@@ -128,6 +130,7 @@ class SamplePointsC(C.Structure):
         ("first_sphere_radius", C.c_void_p),
         ("estimate_normal_aligned", C.c_void_p),
         ("scene_id", C.c_void_p),
+        ("direction_for_derivative", C.c_void_p),
     ]
 
 
@@ -142,6 +145,8 @@ class SampleStatisticsC(C.Structure):
         ("gradient_mean", C.c_void_p),
         ("gradient_m2", C.c_void_p),
         ("n_gradient_estimates", C.c_void_p),
+        ("total_first_source_contribution", C.c_void_p),
+        ("total_derivative_contribution", C.c_void_p),
     ]
 
 

@@ -106,13 +106,134 @@ class WalkCompletionCode(enum.IntEnum):
 
 
 # ----------------------------------------------------------------------- PDE fields
+class DenseGrid:
+    """DenseGrid<float, 1, DIM> (utils/dense_grid.h:29-72): cell-centred samples over the box
+    [grid_min, grid_max], row-major with the last axis fastest.  The walk kernels read the
+    values on the device; __call__ is the same lookup on the host for inspection.
+
+    DenseGrid(grid_min, grid_max, enable_interpolation=False) or
+    DenseGrid(grid_data, grid_shape, grid_min, grid_max, enable_interpolation=False)."""
+
+    def __init__(self, *args, enable_interpolation=False, dim=None):
+        if len(args) in (2, 3):
+            grid_min, grid_max = args[0], args[1]
+            data, shape = None, None
+            if len(args) == 3:
+                enable_interpolation = args[2]
+        elif len(args) in (4, 5):
+            data, shape, grid_min, grid_max = args[:4]
+            if len(args) == 5:
+                enable_interpolation = args[4]
+        else:
+            raise TypeError("DenseGrid(grid_min, grid_max[, interp]) or DenseGrid(data, shape, grid_min, grid_max[, interp])")
+        self.origin = np.asarray(grid_min, np.float32).ravel()
+        self.extent = (np.asarray(grid_max, np.float32).ravel() - self.origin).astype(np.float32)
+        self.dim = int(self.origin.size if dim is None else dim)
+        if self.dim not in (2, 3) or self.extent.size != self.dim:
+            raise ValueError("grid_min / grid_max must have 2 or 3 entries")
+        self.interpolation_enabled = bool(enable_interpolation)
+        self.data = np.zeros(0, np.float32)
+        self.shape = np.zeros(self.dim, np.int32)
+        if data is not None:
+            self.set(data, shape)
+
+    def set(self, grid_data, grid_shape=None):
+        """set(grid_data, grid_shape), or set(callback, grid_shape) with callback(x) -> value
+        evaluated at every cell centre (dense_grid.h:157-190)."""
+        shape = np.asarray(grid_shape, np.int64).ravel()
+        if shape.size != self.dim or np.any(shape < 1):
+            raise ValueError("grid_shape must hold dim positive entries")
+        if callable(grid_data):
+            centres = self.get(np.arange(int(np.prod(shape))), shape)
+            grid_data = np.array([grid_data(c) for c in centres], np.float32)
+        data = np.ascontiguousarray(np.asarray(grid_data, np.float32).ravel())
+        if data.size != int(np.prod(shape)):
+            raise ValueError(f"grid data has {data.size} values, the shape holds {int(np.prod(shape))}")
+        self.data = data
+        self.shape = shape.astype(np.int32)
+
+    def get(self, index, shape=None):
+        """Cell centre(s) of flat index(es) (dense_grid.h:224-240)."""
+        shape = self.shape if shape is None else np.asarray(shape)
+        idx = np.asarray(index, np.int64)
+        out = np.zeros(idx.shape + (self.dim,), np.float32)
+        rem = idx.copy()
+        for i in range(self.dim - 1, -1, -1):
+            out[..., i] = self.origin[i] + (rem % shape[i] + 0.5) * (self.extent[i] / shape[i])
+            rem //= shape[i]
+        return out
+
+    def __call__(self, x):
+        x = np.asarray(x, np.float32)
+        one = x.ndim == 1
+        x = x.reshape(-1, self.dim)
+        t = (x - self.origin) / self.extent
+        n = self.shape.astype(np.int64)
+        if not self.interpolation_enabled:
+            idx = np.clip(np.floor(t * n).astype(np.int64), 0, n - 1)
+            flat = np.zeros(len(x), np.int64)
+            for i in range(self.dim):
+                flat = flat * n[i] + idx[:, i]
+            r = self.data[flat]
+        else:
+            u = np.where(n == 1, 0.0, t * n - 0.5).astype(np.float32)
+            i0 = np.clip(np.floor(u).astype(np.int64), 0, n - 1)
+            i1 = np.clip(i0 + 1, 0, n - 1)
+            f = np.clip(u - i0, 0.0, 1.0)
+            r = np.zeros(len(x), np.float32)
+            for corner in range(1 << self.dim):
+                flat = np.zeros(len(x), np.int64)
+                w = np.ones(len(x), np.float32)
+                for i in range(self.dim):
+                    hi = (corner >> i) & 1
+                    flat = flat * n[i] + (i1[:, i] if hi else i0[:, i])
+                    w = w * (f[:, i] if hi else 1.0 - f[:, i])
+                r = r + w * self.data[flat]
+        return float(r[0]) if one else r
+
+    def min(self):
+        return float(self.data.min())
+
+    def max(self):
+        return float(self.data.max())
+
+    def to_c(self, aligned=None):
+        g = A.Grid()
+        g.values = A.ptr(self.data)
+        g.values_aligned = A.ptr(aligned.data) if aligned is not None else None
+        for i in range(self.dim):
+            g.shape[i] = int(self.shape[i])
+            g.grid_min[i] = float(self.origin[i])
+            g.grid_max[i] = float(self.origin[i] + self.extent[i])
+        g.enable_interpolation = int(self.interpolation_enabled)
+        return g
+
+
 class Field:
     """Device-evaluable replacement for one PDE std::function member."""
 
-    def __init__(self, kind, value=0.0, value_aligned=None):
+    def __init__(self, kind, value=0.0, value_aligned=None, grid=None, grid_aligned=None, raw_grid=None):
         self.kind = kind
         self.value = float(value)
         self.value_aligned = float(value if value_aligned is None else value_aligned)
+        self.grid = grid                  # DenseGrid (kind GRID)
+        self.grid_aligned = grid_aligned  # DenseGrid for returnBoundaryNormalAlignedValue = true
+        self.raw_grid = raw_grid          # a zgpu_grid given directly (its arrays owned by the caller)
+
+    @staticmethod
+    def dense_grid(grid, grid_aligned=None):
+        """A DenseGrid field (getDenseGridCallback0-4, utils/dense_grid.h:374-560)."""
+        if grid_aligned is not None and (grid_aligned.data.size != grid.data.size or
+                                         np.any(grid_aligned.shape != grid.shape)):
+            raise ValueError("the normal-aligned grid must have the grid's shape")
+        return Field(A.ZGPU_FIELD_GRID, grid=grid, grid_aligned=grid_aligned)
+
+    def grid_to_c(self):
+        if self.raw_grid is not None:
+            return self.raw_grid
+        if self.grid is None:
+            return A.Grid()
+        return self.grid.to_c(self.grid_aligned)
 
     @staticmethod
     def zero():
@@ -126,6 +247,51 @@ class Field:
     def analytic():
         """Derived from PDE.solution: g = u, h = du/dn + kappa u, f = -Lap u + sigma u."""
         return Field(A.ZGPU_FIELD_ANALYTIC)
+
+
+def _dense_grid_field(args, kw, aligned):
+    """The get_dense_grid_*_callback overloads (python/zombie_bindings.h:852-1125): a DenseGrid
+    (plus its normal-aligned twin), or raw data (plus aligned data), shape, min, max and the
+    interpolation flag."""
+    interp = kw.pop("enable_interpolation", False)
+    kw.pop("dim", None)
+    kw.pop("channels", None)
+    if args and isinstance(args[0], DenseGrid):
+        g = args[0]
+        ga = args[1] if len(args) > 1 else kw.pop("grid_boundary_normal_aligned", None)
+        if ga is not None and not aligned:
+            raise TypeError("this field has no normal-aligned variant")
+        return Field.dense_grid(g, ga)
+    args = list(args)
+    data = args.pop(0) if args else kw.pop("grid_data")
+    da = None
+    if aligned and (len(args) >= 4 and not isinstance(args[3], (bool, np.bool_)) or
+                    "grid_data_boundary_normal_aligned" in kw):
+        da = args.pop(0) if "grid_data_boundary_normal_aligned" not in kw else kw.pop("grid_data_boundary_normal_aligned")
+    shape = args.pop(0) if args else kw.pop("grid_shape")
+    gmin = args.pop(0) if args else kw.pop("grid_min")
+    gmax = args.pop(0) if args else kw.pop("grid_max")
+    if args:
+        interp = args.pop(0)
+    g = DenseGrid(data, shape, gmin, gmax, bool(interp))
+    ga = DenseGrid(da, shape, gmin, gmax, bool(interp)) if da is not None else None
+    return Field.dense_grid(g, ga)
+
+
+def get_dense_grid_source_callback(*args, **kw):
+    return _dense_grid_field(args, kw, aligned=False)
+
+
+def get_dense_grid_dirichlet_callback(*args, **kw):
+    return _dense_grid_field(args, kw, aligned=True)
+
+
+def get_dense_grid_robin_callback(*args, **kw):
+    return _dense_grid_field(args, kw, aligned=True)
+
+
+def get_dense_grid_robin_coefficient_callback(*args, **kw):
+    return _dense_grid_field(args, kw, aligned=True)
 
 
 class PDE:
@@ -143,11 +309,19 @@ class PDE:
         self.dirichlet = Field.zero()
         self.robin = Field.zero()
         self.robin_coeff = Field.zero()
+        self.grid_memory = A.ZGPU_MEM_HOST   # where raw zgpu_grid values live (DenseGrid data is host)
 
     def has_non_zero_robin_coeff(self, x=None):
+        """PDE::hasNonZeroRobinCoeff (core/pde.h:62-78) at x (grids need x)."""
         if self.are_robin_conditions_pure_neumann:
             return False
-        return self.robin_coeff.kind != A.ZGPU_FIELD_ZERO and (self.robin_coeff.value != 0 or self.robin_coeff.value_aligned != 0)
+        rc = self.robin_coeff
+        if rc.kind == A.ZGPU_FIELD_GRID and rc.grid is not None and x is not None:
+            g = rc.grid_aligned or rc.grid
+            return abs(rc.grid(x)) > 0 or abs(g(x)) > 0
+        if rc.kind == A.ZGPU_FIELD_GRID:
+            return True
+        return rc.kind != A.ZGPU_FIELD_ZERO and (rc.value != 0 or rc.value_aligned != 0)
 
     def to_c(self):
         p = A.Pde()
@@ -162,7 +336,11 @@ class PDE:
         p.robin_kind, p.robin_value, p.robin_value_aligned = self.robin.kind, self.robin.value, self.robin.value_aligned
         p.robin_coeff_kind, p.robin_coeff_value, p.robin_coeff_value_aligned = \
             self.robin_coeff.kind, self.robin_coeff.value, self.robin_coeff.value_aligned
-        p.memory = A.ZGPU_MEM_HOST
+        p.source_grid = self.source.grid_to_c()
+        p.dirichlet_grid = self.dirichlet.grid_to_c()
+        p.robin_grid = self.robin.grid_to_c()
+        p.robin_coeff_grid = self.robin_coeff.grid_to_c()
+        p.memory = self.grid_memory
         return p
 
     @staticmethod
@@ -173,10 +351,15 @@ class PDE:
         pde.are_robin_conditions_pure_neumann = bool(p.are_robin_conditions_pure_neumann)
         pde.are_robin_coeffs_nonnegative = bool(p.are_robin_coeffs_nonnegative)
         pde.solution = p.solution
-        pde.source = Field(p.source_kind, p.source_value)
-        pde.dirichlet = Field(p.dirichlet_kind, p.dirichlet_value, p.dirichlet_value_aligned)
-        pde.robin = Field(p.robin_kind, p.robin_value, p.robin_value_aligned)
-        pde.robin_coeff = Field(p.robin_coeff_kind, p.robin_coeff_value, p.robin_coeff_value_aligned)
+        def raw(kind, g):
+            return g if kind == A.ZGPU_FIELD_GRID else None
+        pde.source = Field(p.source_kind, p.source_value, raw_grid=raw(p.source_kind, p.source_grid))
+        pde.dirichlet = Field(p.dirichlet_kind, p.dirichlet_value, p.dirichlet_value_aligned,
+                              raw_grid=raw(p.dirichlet_kind, p.dirichlet_grid))
+        pde.robin = Field(p.robin_kind, p.robin_value, p.robin_value_aligned, raw_grid=raw(p.robin_kind, p.robin_grid))
+        pde.robin_coeff = Field(p.robin_coeff_kind, p.robin_coeff_value, p.robin_coeff_value_aligned,
+                                raw_grid=raw(p.robin_coeff_kind, p.robin_coeff_grid))
+        pde.grid_memory = p.memory
         return pde
 
 
@@ -267,6 +450,8 @@ class SampleStatistics:
         self.gradient_mean = None        # per-dimension lists once gradients are estimated
         self.gradient_m2 = None
         self.n_gradient_estimates = 0
+        self.total_first_source_contribution = 0.0
+        self.total_derivative_contribution = 0.0
 
     def get_estimated_solution(self):
         return self.solution_mean
@@ -281,6 +466,12 @@ class SampleStatistics:
 
     def get_gradient_estimate_count(self):
         return self.n_gradient_estimates
+
+    def get_mean_first_source_contribution(self):
+        return self.total_first_source_contribution / max(1, self.n_solution_estimates)
+
+    def get_estimated_derivative(self):
+        return self.total_derivative_contribution / max(1, self.n_solution_estimates)
 
     def get_estimated_solution_variance(self):
         return self.solution_m2 / max(1, self.n_solution_estimates - 1)
@@ -304,9 +495,11 @@ class SampleArrays:
     torch CUDA tensors).  Field names follow zgpu_sample_points / zgpu_sample_statistics."""
 
     POINT_FIELDS = ("pt", "normal", "type", "estimation_quantity", "dist_to_absorbing", "dist_to_reflecting",
-                    "n_walks", "seed", "first_sphere_radius", "estimate_normal_aligned", "scene_id")
+                    "n_walks", "seed", "first_sphere_radius", "estimate_normal_aligned", "scene_id",
+                    "direction_for_derivative")
     STAT_FIELDS = ("solution_mean", "solution_m2", "n_solution_estimates", "total_walk_length", "total_splits",
-                   "gradient_mean", "gradient_m2", "n_gradient_estimates")
+                   "gradient_mean", "gradient_m2", "n_gradient_estimates", "total_first_source_contribution",
+                   "total_derivative_contribution")
 
     def __init__(self, **arrays):
         self.arrays = arrays
@@ -330,6 +523,8 @@ class SampleArrays:
             arr["gradient_mean"] = np.zeros((n, d))
             arr["gradient_m2"] = np.zeros((n, d))
             arr["n_gradient_estimates"] = np.zeros(n, np.int32)
+            arr["total_first_source_contribution"] = np.zeros(n)
+            arr["total_derivative_contribution"] = np.zeros(n)
         if first_sphere_radius:
             arr["first_sphere_radius"] = np.zeros(n, np.float32)
         if normals is not None:
@@ -738,6 +933,12 @@ class _Solver:
             arr["gradient_m2"] = np.array([s.gradient_m2 if s.gradient_m2 is not None else [0.0] * D
                                            for s in stats], np.float64).reshape(n, D)
             arr["n_gradient_estimates"] = np.array([s.n_gradient_estimates for s in stats], np.int32)
+            arr["direction_for_derivative"] = np.array([p.direction_for_derivative for p in pts],
+                                                       np.float32).reshape(n, D)
+            arr["total_first_source_contribution"] = np.array([s.total_first_source_contribution for s in stats],
+                                                              np.float64)
+            arr["total_derivative_contribution"] = np.array([s.total_derivative_contribution for s in stats],
+                                                            np.float64)
         rep = self.solve_arrays(pde, walk_settings, SampleArrays(**arr))
         for i, (p, s) in enumerate(zip(pts, stats)):
             p.first_sphere_radius = float(arr["first_sphere_radius"][i])
@@ -750,6 +951,8 @@ class _Solver:
                 s.gradient_mean = [float(v) for v in arr["gradient_mean"][i]]
                 s.gradient_m2 = [float(v) for v in arr["gradient_m2"][i]]
                 s.n_gradient_estimates = int(arr["n_gradient_estimates"][i])
+                s.total_first_source_contribution = float(arr["total_first_source_contribution"][i])
+                s.total_derivative_contribution = float(arr["total_derivative_contribution"][i])
         if report_progress is not None:
             report_progress(n, 0)
         return rep

@@ -67,7 +67,8 @@ struct zgpu_context {
     enum { kPt, kNormal, kType, kEq, kDist, kNWalks, kSeed, kFsr, kAligned, kMean, kM2, kN, kLen, kSplits,
            kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
            kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId,
-           kDistRefl, kGMean, kGM2, kGN, kAccGrad, kAccGradSq, kAccGradN, kNumBufs };
+           kDistRefl, kGMean, kGM2, kGN, kAccGrad, kAccGradSq, kAccGradN, kDirDeriv, kFirstSrc, kDeriv, kAccFirstSrc,
+           kAccDeriv, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
     // use_graph: the captured prepare/scan/walk/finalize sequence, replayed while the solve's
@@ -76,6 +77,7 @@ struct zgpu_context {
     std::vector<unsigned char> graphKey;
     // autotuner results by scene signature
     std::map<std::string, zgpu_solve_options> tuned;
+    std::vector<Buf> gridBufs;   // device copies of host-memory PDE grids
 };
 
 struct zgpu_boundary {
@@ -138,13 +140,44 @@ int checkBoundary(zgpu_boundary* b, int dim, const char* what) {
     return ZGPU_OK;
 }
 
-int checkField(int kind, const char* name) {
-    if (kind == ZGPU_FIELD_GRID) return fail(ZGPU_ERR_UNSUPPORTED, "%s: dense-grid fields are not supported by this build", name);
+int checkField(int kind, const zgpu_grid& g, int D, const char* name) {
     if (kind < ZGPU_FIELD_ZERO || kind > ZGPU_FIELD_GRID) return fail(ZGPU_ERR_INVALID_ARG, "%s: unknown field kind %d", name, kind);
+    if (kind != ZGPU_FIELD_GRID) return ZGPU_OK;
+    if (!g.values) return fail(ZGPU_ERR_INVALID_ARG, "%s: grid has no values", name);
+    int64_t cells = 1;
+    for (int i = 0; i < D; i++) {
+        if (g.shape[i] < 1) return fail(ZGPU_ERR_INVALID_ARG, "%s: grid shape[%d] = %d must be >= 1", name, i, g.shape[i]);
+        if (!(g.grid_max[i] > g.grid_min[i])) return fail(ZGPU_ERR_INVALID_ARG, "%s: grid_max[%d] must exceed grid_min[%d]", name, i, i);
+        cells *= g.shape[i];
+        if (cells > ((int64_t)1 << 40)) return fail(ZGPU_ERR_INVALID_ARG, "%s: grid has too many cells", name);
+    }
     return ZGPU_OK;
 }
 
+int64_t gridCells(const zgpu_grid& g, int D) {
+    int64_t c = 1;
+    for (int i = 0; i < D; i++) c *= g.shape[i];
+    return c;
+}
+
 }  // namespace
+
+namespace zg {
+// the PDE's fields: kinds, grid shapes and boxes, and where the grid values live
+int checkPdeFields(const zgpu_pde* pde, int D, bool hostGrids) {
+    ZG_TRY(checkField(pde->source_kind, pde->source_grid, D, "source"));
+    ZG_TRY(checkField(pde->dirichlet_kind, pde->dirichlet_grid, D, "dirichlet"));
+    ZG_TRY(checkField(pde->robin_kind, pde->robin_grid, D, "robin"));
+    ZG_TRY(checkField(pde->robin_coeff_kind, pde->robin_coeff_grid, D, "robin_coeff"));
+    if (pde->robin_coeff_kind == ZGPU_FIELD_ANALYTIC) return fail(ZGPU_ERR_UNSUPPORTED, "robin_coeff must be ZERO, CONSTANT or GRID");
+    const bool grids = pde->source_kind == ZGPU_FIELD_GRID || pde->dirichlet_kind == ZGPU_FIELD_GRID ||
+                       pde->robin_kind == ZGPU_FIELD_GRID || pde->robin_coeff_kind == ZGPU_FIELD_GRID;
+    if (grids && pde->memory != ZGPU_MEM_DEVICE && (!hostGrids || pde->memory != ZGPU_MEM_HOST))
+        return fail(ZGPU_ERR_INVALID_ARG, hostGrids ? "pde.memory must be ZGPU_MEM_HOST or ZGPU_MEM_DEVICE"
+                                                    : "grid values must be in device memory here");
+    return ZGPU_OK;
+}
+}  // namespace zg
 
 // internal accessors used by the allocation-free entry point (zgpu_static.cu) and the cache
 namespace zg {
@@ -189,6 +222,7 @@ int zgpu_context_destroy(zgpu_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& b : c->bufs) if (b.p) cudaFree(b.p);
+    for (auto& b : c->gridBufs) if (b.p) cudaFree(b.p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
     if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
@@ -570,15 +604,36 @@ int checkScene(const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_
     if (!(ws->epsilon_shell_for_absorbing_boundary >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "epsilon shell must be >= 0");
     if (!(ws->splitting_threshold > 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "splitting threshold must be > 0");
     if (!(pde->absorption_coeff >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "absorption coefficient must be >= 0");
-    ZG_TRY(checkField(pde->source_kind, "source"));
-    ZG_TRY(checkField(pde->dirichlet_kind, "dirichlet"));
-    ZG_TRY(checkField(pde->robin_kind, "robin"));
-    ZG_TRY(checkField(pde->robin_coeff_kind, "robin_coeff"));
-    if (pde->robin_coeff_kind == ZGPU_FIELD_ANALYTIC) return fail(ZGPU_ERR_UNSUPPORTED, "robin_coeff must be ZERO or CONSTANT");
+    ZG_TRY(zg::checkPdeFields(pde, D, true));
     if (pde->solution.n_terms < 0 || pde->solution.n_terms > ZGPU_MAX_TERMS)
         return fail(ZGPU_ERR_INVALID_ARG, "analytic solution has %d terms (max %d)", pde->solution.n_terms, ZGPU_MAX_TERMS);
     return ZGPU_OK;
 }
+
+namespace {
+// Grids given in host memory are copied into device buffers of the context (four fields x
+// two orientations per scene) and the descriptor is pointed at the copies.
+int stageGrids(zgpu_context* ctx, zgpu_pde& pde, int D, int scene) {
+    if (pde.memory != ZGPU_MEM_HOST) return ZGPU_OK;
+    const int kinds[4] = {pde.source_kind, pde.dirichlet_kind, pde.robin_kind, pde.robin_coeff_kind};
+    zgpu_grid* grids[4] = {&pde.source_grid, &pde.dirichlet_grid, &pde.robin_grid, &pde.robin_coeff_grid};
+    for (int f = 0; f < 4; f++) {
+        if (kinds[f] != ZGPU_FIELD_GRID) continue;
+        const size_t bytes = (size_t)gridCells(*grids[f], D) * sizeof(float);
+        const float** src[2] = {&grids[f]->values, &grids[f]->values_aligned};
+        for (int a = 0; a < 2; a++) {
+            if (!*src[a]) continue;
+            const size_t slot = ((size_t)scene * 4 + f) * 2 + a;
+            if (ctx->gridBufs.size() <= slot) ctx->gridBufs.resize(slot + 1);
+            ZG_CUDA(ensure(ctx->gridBufs[slot], bytes));
+            ZG_CUDA(cudaMemcpyAsync(ctx->gridBufs[slot].p, *src[a], bytes, cudaMemcpyHostToDevice, ctx->stream));
+            *src[a] = (const float*)ctx->gridBufs[slot].p;
+        }
+    }
+    pde.memory = ZGPU_MEM_DEVICE;
+    return ZGPU_OK;
+}
+}  // namespace
 
 SceneDesc sceneOf(const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_walk_settings* ws) {
     SceneDesc d;
@@ -626,6 +681,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     std::memset(&P, 0, sizeof(P));
     P.solver = solver;
     P.sc = sceneOf(q, pde, ws);
+    ZG_TRY(stageGrids(ctx, P.sc.pde, D, 0));
     P.nPoints = n;
     using C = zgpu_context;
     int sceneStack = 8;
@@ -634,6 +690,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
         std::vector<SceneDesc> table(nScenes);
         for (int k = 0; k < nScenes; k++) {
             table[k] = sceneOf(q + k, pde + k, ws + k);
+            ZG_TRY(stageGrids(ctx, table[k].pde, D, k));
             if (table[k].hasAbs) sceneStack = std::max(sceneStack, table[k].absorbing.stackEntries);
             if (table[k].hasRefl) sceneStack = std::max(sceneStack, table[k].reflecting.stackEntries);
             P.batchScreened |= pde[k].absorption_coeff > 0.0f;
@@ -668,10 +725,6 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     // estimateSolutionAndGradient: needs the gradient statistics arrays
     const bool gradients = stats->gradient_mean && stats->n_gradient_estimates && pts->estimation_quantity;
     if (gradients) {
-        for (int k = 0; k < nScenes; k++)
-            if (ws[k].use_cosine_sampling_for_derivatives)
-                return fail(ZGPU_ERR_UNSUPPORTED, "cosine sampling for derivatives needs directionForDerivative, "
-                                                  "which zgpu_sample_points does not carry");
         ZG_TRY(stageInOut<double>(ctx, C::kGMean, stats->gradient_mean, (size_t)n * D, mem, &P.statGradMean));
         ZG_TRY(stageInOut<double>(ctx, C::kGM2, stats->gradient_m2, (size_t)n * D, mem, &P.statGradM2));
         ZG_TRY(stageInOut<int>(ctx, C::kGN, stats->n_gradient_estimates, (size_t)n, mem, &P.statGradN));
@@ -679,6 +732,15 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
         ZG_TRY(scratch<double>(ctx, C::kAccGrad, (size_t)n * D, &P.accGrad));
         ZG_TRY(scratch<double>(ctx, C::kAccGradSq, (size_t)n * D, &P.accGradSq));
         ZG_TRY(scratch<int>(ctx, C::kAccGradN, (size_t)n, &P.accGradN));
+        ZG_TRY(stageIn<float>(ctx, C::kDirDeriv, pts->direction_for_derivative, (size_t)n * D, mem, &P.dirDeriv));
+        if (stats->total_first_source_contribution) {
+            ZG_TRY(stageInOut<double>(ctx, C::kFirstSrc, stats->total_first_source_contribution, (size_t)n, mem, &P.statFirstSrc));
+            ZG_TRY(scratch<double>(ctx, C::kAccFirstSrc, (size_t)n, &P.accFirstSrc));
+        }
+        if (stats->total_derivative_contribution) {
+            ZG_TRY(stageInOut<double>(ctx, C::kDeriv, stats->total_derivative_contribution, (size_t)n, mem, &P.statDeriv));
+            ZG_TRY(scratch<double>(ctx, C::kAccDeriv, (size_t)n, &P.accDeriv));
+        }
     }
     long long* blockSums = nullptr;
     ZG_TRY(scratch<long long>(ctx, C::kWalkStart, (size_t)n + 1, &P.walkStart));
@@ -780,6 +842,8 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
         ZG_TRY(stageOut<double>(ctx, P.statGradMean, stats->gradient_mean, (size_t)n * D, mem));
         if (stats->gradient_m2) ZG_TRY(stageOut<double>(ctx, P.statGradM2, stats->gradient_m2, (size_t)n * D, mem));
         ZG_TRY(stageOut<int>(ctx, P.statGradN, stats->n_gradient_estimates, (size_t)n, mem));
+        if (P.statFirstSrc) ZG_TRY(stageOut<double>(ctx, P.statFirstSrc, stats->total_first_source_contribution, (size_t)n, mem));
+        if (P.statDeriv) ZG_TRY(stageOut<double>(ctx, P.statDeriv, stats->total_derivative_contribution, (size_t)n, mem));
     }
     ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters, P.counters, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ZG_CUDA(cudaMemcpyAsync(ctx->hostCounters + 12, P.walkStart + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
@@ -893,13 +957,17 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
     st.memory = ZGPU_MEM_HOST;
     st.solution_mean = mean.data(); st.solution_m2 = m2.data(); st.n_solution_estimates = cnt.data();
     st.total_walk_length = (int64_t*)len.data(); st.total_splits = (int64_t*)spl.data();
-    const bool wos = solver == ZGPU_SOLVER_WALK_ON_SPHERES && q->absorbing && q->absorbing->nPrims > 0;
+    // query modes worth sweeping: warp-wide closest points (Walk on Spheres) and warp-wide
+    // Robin star radii (Walk on Stars)
+    const bool sweepQuery = (solver == ZGPU_SOLVER_WALK_ON_SPHERES && q->absorbing && q->absorbing->nPrims > 0) ||
+                            (solver == ZGPU_SOLVER_WALK_ON_STARS && q->reflecting && q->reflecting->nPrims > 0 &&
+                             q->reflecting->kind == ZGPU_BOUNDARY_ROBIN);
     const int threadsC[3] = {32, 64, 128};
     const int perSMC[3] = {0, 2, 4};
     zgpu_solve_options best;
     std::memset(&best, 0, sizeof(best));
     double bestRate = -1.0;
-    for (int qm = wos ? 1 : 0; qm <= (wos ? 2 : 0); qm++)
+    for (int qm = sweepQuery ? 1 : 0; qm <= (sweepQuery ? 2 : 0); qm++)
         for (int ti = 0; ti < 3; ti++)
             for (int pi = 0; pi < 3; pi++) {
                 zgpu_solve_options o;

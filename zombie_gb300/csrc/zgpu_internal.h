@@ -53,6 +53,9 @@ struct SolveParams {
     double* statGradM2;
     int* statGradN;
     const float* distRefl;      // gradient points of Walk on Stars: distance to the reflecting boundary
+    const float* dirDeriv;      // [n][D] directionForDerivative (NULL: the first axis)
+    double* statFirstSrc;       // running sums of first source contributions (NULL: not kept)
+    double* statDeriv;          // running sums of directional derivative contributions
     long long* statLen;
     long long* statSplits;
     // scratch
@@ -67,6 +70,8 @@ struct SolveParams {
     double* accGrad;            // [n][D] sums and sums of squares of gradient estimates
     double* accGradSq;
     int* accGradN;
+    double* accFirstSrc;        // this call's sums of the two above (NULL when not kept)
+    double* accDeriv;
     unsigned long long* counters;
     unsigned int* errorWord;
     float4* splitStack;         // walk threads x kSplitStack x 3 float4
@@ -100,6 +105,8 @@ cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStr
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p);
+// validates a PDE's field kinds and grids (hostGrids: grid values may be in host memory)
+int checkPdeFields(const zgpu_pde* pde, int D, bool hostGrids);
 // neural cache pass over the walk records (zgpu_cache.cu)
 cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
                                   int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,

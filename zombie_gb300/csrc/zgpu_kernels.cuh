@@ -85,7 +85,7 @@ struct Walker {
     // estimateSolutionAndGradient: this walk's first-step source contribution, control
     // variate and gradient directions
     bool gradMode;
-    float firstSrc, cvB;
+    float firstSrc, cvB, cvS;
     V<D> bGradDir, sGradDir;
     // per-walk accumulation across split states
     float walkTotal;
@@ -195,7 +195,11 @@ struct Walker {
         const uint32_t m = (uint32_t)(2 * (anti ? walks / 2 : walks));
         const uint64_t key = __ldg(P.seed + point) ^ (uint64_t)nPrev;
         gradMode = true;
-        cvB = (ws.use_gradient_control_variates && nPrev > 0) ? (float)P.statMean[point] : 0.0f;
+        // control variates (walk_on_spheres.h:444-450): the previous estimate and the mean
+        // first source contribution of the earlier walks
+        const bool cv = ws.use_gradient_control_variates && nPrev > 0;
+        cvB = cv ? (float)P.statMean[point] : 0.0f;
+        cvS = (cv && P.statFirstSrc) ? (float)(P.statFirstSrc[point] / (double)nPrev) : 0.0f;
         const V<D> x0 = pt;
         const float R0 = fsr;
         g.update(x0, R0);
@@ -221,9 +225,20 @@ struct Walker {
             }
             totSrc += thr * firstSrc;
         }
-        V<D> dirB = sphereFromUniform<D>(ub);
+        V<D> dirB;
+        float bPdf;
+        if (ws.use_cosine_sampling_for_derivatives) {
+            // cosine-weighted about directionForDerivative, either hemisphere with probability
+            // 1/2 (walk_on_spheres.h:500-504)
+            V<D> loc = hemisphereCosine<D>(ub);
+            if (rng.uniform() < 0.5f) loc[D - 1] = -loc[D - 1];
+            bPdf = 0.5f * hemisphereCosinePdf<D>(fabsf(loc[D - 1]));
+            dirB = toFrame(derivativeDirection(), loc);
+        } else {
+            dirB = sphereFromUniform<D>(ub);
+            bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
+        }
         if (mirror) dirB = -dirB;
-        const float bPdf = D == 2 ? 1.0f / (2.0f * kPi) : 1.0f / (4.0f * kPi);
         const V<D> yb = x0 + R0 * dirB;
         thr *= g.poissonKernelCentre() / bPdf;
         bGradDir = (1.0f / (bPdf * thr)) * g.poissonKernelGradient(yb);
@@ -349,13 +364,27 @@ struct Walker {
     // first source contribution along the source gradient direction
     __device__ __noinline__ void addGradient() {
         const float bc = walkTotal - firstSrc;
+        const V<D> dd = derivativeDirection();
+        float deriv = 0.0f;
 #pragma unroll
         for (int i = 0; i < D; i++) {
-            const double gi = (double)((bc - cvB) * bGradDir[i] + firstSrc * sGradDir[i]);
+            const float gb = (bc - cvB) * bGradDir[i], gs = (firstSrc - cvS) * sGradDir[i];
+            deriv += gb * dd[i] + gs * dd[i];
+            const double gi = (double)(gb + gs);
             atomicAdd(P.accGrad + (size_t)point * D + i, gi);
             atomicAdd(P.accGradSq + (size_t)point * D + i, gi * gi);
         }
         atomicAdd(P.accGradN + point, 1);
+        if (P.accFirstSrc) atomicAdd(P.accFirstSrc + point, (double)firstSrc);
+        if (P.accDeriv) atomicAdd(P.accDeriv + point, (double)deriv);
+    }
+
+    // SamplePoint::directionForDerivative (common.h:185), the first axis by default
+    ZG_D V<D> derivativeDirection() const {
+        V<D> d = vzero<D>();
+        if (P.dirDeriv) d = vload<D>(P.dirDeriv + (size_t)point * D);
+        else d[0] = 1.0f;
+        return d;
     }
 
     // --------------------------------------------------------------- Walk on Spheres step
@@ -429,7 +458,7 @@ struct Walker {
                 }
                 if (ws.steps_before_using_maximal_spheres <= wlen) {
                     R = distAbs;
-                } else if (onRefl && pde.hasNonZeroRobinCoeff()) {
+                } else if (onRefl && pde.hasNonZeroRobinCoeff(pt)) {
                     R = ws.epsilon_shell_for_reflecting_boundary;
                 } else if (kCoopStar && SC().hasRefl) {
                     radiusPending = true;      // the warp answers, then the step resumes here
@@ -526,7 +555,7 @@ struct Walker {
             if (!SC().pde.are_robin_conditions_pure_neumann) {
                 bool f2 = false;
                 if (ws.solve_double_sided) { f2 = dot(prevDir, nrm) < 0.0f; if (f2) n = -n; }
-                kappa = pde.robinCoeff(ws.solve_double_sided && f2);
+                kappa = pde.robinCoeff(pt, ws.solve_double_sided && f2);
             }
             float refl = g.reflectance(prevDist, prevDir, n, kappa);
             float maxRefl = SC().pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
@@ -692,6 +721,8 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
     if (P.accGrad) {
         for (int k = 0; k < D; k++) { P.accGrad[i * D + k] = 0.0; P.accGradSq[i * D + k] = 0.0; }
         P.accGradN[i] = 0;
+        if (P.accFirstSrc) P.accFirstSrc[i] = 0.0;
+        if (P.accDeriv) P.accDeriv[i] = 0.0;
     }
     bool hasPrev = nPrev > 0 && P.fsrPersistent;
     int flags = 0;
@@ -737,7 +768,7 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
                 r = dAbs;
             } else if (dAbs <= ws.epsilon_shell_for_absorbing_boundary || ws.steps_before_using_maximal_spheres == 0) {
                 r = dAbs;
-            } else if (type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && pde.hasNonZeroRobinCoeff()) {
+            } else if (type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && pde.hasNonZeroRobinCoeff(vload<D>(P.pt + (size_t)i * D))) {
                 r = ws.epsilon_shell_for_reflecting_boundary;
             } else {
                 uint32_t err = 0;
@@ -815,6 +846,8 @@ __global__ void finalizeKernel(const __grid_constant__ SolveParams P) {
             }
             P.statGradN[i] = gt;
         }
+        if (P.accFirstSrc && P.statFirstSrc) P.statFirstSrc[i] += P.accFirstSrc[i];
+        if (P.accDeriv && P.statDeriv) P.statDeriv[i] += P.accDeriv[i];
     }
 }
 

@@ -101,6 +101,52 @@ ZG_D V<3> sphereFromUniform(const float* u, V<3>) {
 }
 template <int D> ZG_D V<D> sphereFromUniform(const float* u) { return sphereFromUniform(u, V<D>()); }
 
+// Cosine-weighted direction on the unit hemisphere about the last axis from uniforms u
+// (SphereSampler::sampleUnitHemisphereCosine, core/sampling.h:124-129, :211-216).  2D: the
+// abscissa x = 2u - 1 is uniform, so the angle from the axis has density cos / 2.  3D:
+// Shirley and Chiu's concentric map of the square onto the disk (JGT 1997), lifted to the
+// hemisphere (Malley's method), density cos / pi.
+ZG_D V<2> hemisphereCosine(const float* u, V<2>) {
+    const float x = 2.0f * u[0] - 1.0f;
+    V<2> r; r[0] = x; r[1] = sqrtf(fmaxf(0.0f, 1.0f - x * x)); return r;
+}
+ZG_D V<3> hemisphereCosine(const float* u, V<3>) {
+    const float a = 2.0f * u[0] - 1.0f, b = 2.0f * u[1] - 1.0f;
+    float rad = 0.0f, ang = 0.0f;                   // angle in units of pi
+    if (a != 0.0f || b != 0.0f) {
+        if (fabsf(a) > fabsf(b)) { rad = a; ang = 0.25f * (b / a); }
+        else { rad = b; ang = 0.5f - 0.25f * (a / b); }
+    }
+    float s, c;
+    sincospif(ang, &s, &c);
+    V<3> v; v[0] = rad * c; v[1] = rad * s; v[2] = sqrtf(fmaxf(0.0f, 1.0f - rad * rad)); return v;
+}
+template <int D> ZG_D V<D> hemisphereCosine(const float* u) { return hemisphereCosine(u, V<D>()); }
+// density of hemisphereCosine over directions at angle acos(cosTheta) from the axis
+template <int D> ZG_D float hemisphereCosinePdf(float cosTheta) {
+    return D == 2 ? 0.5f * cosTheta : cosTheta * (1.0f / kPi);
+}
+
+// d given in a frame whose last axis is the unit vector n, expressed in world coordinates
+// (SphereSampler::transformCoordinates, core/sampling.h:151-157, :236-246).  2D: tangent
+// (n1, -n0).  3D: the branchless orthonormal basis of Duff et al., "Building an Orthonormal
+// Basis, Revisited" (JCGT 2017).
+ZG_D V<2> toFrame(const V<2>& n, const V<2>& d) {
+    V<2> r; r[0] = d[0] * n[1] + d[1] * n[0]; r[1] = -d[0] * n[0] + d[1] * n[1]; return r;
+}
+ZG_D V<3> toFrame(const V<3>& n, const V<3>& d) {
+    const float sg = copysignf(1.0f, n[2]);
+    const float a = -1.0f / (sg + n[2]);
+    const float b = n[0] * n[1] * a;
+    V<3> t1, t2;
+    t1[0] = 1.0f + sg * n[0] * n[0] * a; t1[1] = sg * b; t1[2] = -sg * n[0];
+    t2[0] = b; t2[1] = sg + n[1] * n[1] * a; t2[2] = -n[1];
+    V<3> r;
+#pragma unroll
+    for (int i = 0; i < 3; i++) r[i] = d[0] * t1[i] + d[1] * t2[i] + d[2] * n[i];
+    return r;
+}
+
 // Latin-hypercube stratum of sample k among m for dimension j of point `key`: an affine
 // permutation k -> (a k + b) mod m with a coprime to m, a and b hashed from (key, j)
 ZG_D uint32_t lhsStratum(uint64_t key, int j, uint32_t k, uint32_t m) {
@@ -388,11 +434,60 @@ __device__ __noinline__ FieldEval<D> evalAnalytic(const zgpu_analytic& a, V<D> x
     return r;
 }
 
+// DenseGrid<float, 1, D>::operator() (utils/dense_grid.h:264-355) over a zgpu_grid: local
+// coordinates t = (x - min) / (max - min); nearest: cell floor(t * shape) clamped to the
+// grid; interpolated: between the cell centres around t * shape - 1/2, indices clamped to
+// the grid and blend fractions to [0, 1].  Row-major, last axis fastest.
+template <int D>
+ZG_D float gridValue(const zgpu_grid& g, V<D> x, bool aligned) {
+    const float* __restrict__ v = (aligned && g.values_aligned) ? g.values_aligned : g.values;
+    int lo[D], hi[D];
+    float w[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const int n = g.shape[i];
+        const float t = (x[i] - g.grid_min[i]) / (g.grid_max[i] - g.grid_min[i]);
+        if (g.enable_interpolation) {
+            const float u = n == 1 ? 0.0f : t * (float)n - 0.5f;
+            const int i0 = min(max((int)floorf(u), 0), n - 1);
+            lo[i] = i0;
+            hi[i] = min(i0 + 1, n - 1);
+            w[i] = fminf(fmaxf(u - (float)i0, 0.0f), 1.0f);
+        } else {
+            lo[i] = hi[i] = min(max((int)floorf(t * (float)n), 0), n - 1);
+            w[i] = 0.0f;
+        }
+    }
+    if (!g.enable_interpolation) {
+        long long k = lo[0];
+#pragma unroll
+        for (int i = 1; i < D; i++) k = k * g.shape[i] + lo[i];
+        return __ldg(v + k);
+    }
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < (1 << D); c++) {
+        long long k = 0;
+        float wt = 1.0f;
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            const bool up = (c >> (D - 1 - i)) & 1;
+            k = k * g.shape[i] + (up ? hi[i] : lo[i]);
+            wt *= up ? w[i] : 1.0f - w[i];
+        }
+        acc += wt * __ldg(v + k);
+    }
+    return acc;
+}
+
 template <int D>
 struct DevicePde {
     const zgpu_pde* p;   // in constant or global memory
-    ZG_D float robinCoeff(bool aligned) const {
+    // the Robin coefficient; grids depend on the position only (getDenseGridCallback3/4
+    // ignore the normal)
+    ZG_D float robinCoeff(V<D> x, bool aligned) const {
         if (p->robin_coeff_kind == ZGPU_FIELD_ZERO) return 0.0f;
+        if (p->robin_coeff_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->robin_coeff_grid, x, aligned);
         return aligned ? p->robin_coeff_value_aligned : p->robin_coeff_value;
     }
     ZG_D float source(V<D> x) const {
@@ -401,11 +496,13 @@ struct DevicePde {
             FieldEval<D> e = evalAnalytic<D>(p->solution, x);
             return -e.lap + p->absorption_coeff * e.u;
         }
+        if (p->source_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->source_grid, x, false);
         return 0.0f;
     }
     ZG_D float dirichlet(V<D> x, bool aligned) const {
         if (p->dirichlet_kind == ZGPU_FIELD_CONSTANT) return aligned ? p->dirichlet_value_aligned : p->dirichlet_value;
         if (p->dirichlet_kind == ZGPU_FIELD_ANALYTIC) return evalAnalytic<D>(p->solution, x).u;
+        if (p->dirichlet_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->dirichlet_grid, x, aligned);
         return 0.0f;
     }
     // Robin data h = du/dn + kappa u, n outward (the aligned side sees -n)
@@ -414,14 +511,15 @@ struct DevicePde {
         if (p->robin_kind == ZGPU_FIELD_ANALYTIC) {
             FieldEval<D> e = evalAnalytic<D>(p->solution, x);
             float s = aligned ? -1.0f : 1.0f;
-            return s * dot(e.grad, n) + robinCoeff(aligned) * e.u;
+            return s * dot(e.grad, n) + robinCoeff(x, aligned) * e.u;
         }
+        if (p->robin_kind == ZGPU_FIELD_GRID) return gridValue<D>(p->robin_grid, x, aligned);
         return 0.0f;
     }
     // PDE::hasNonZeroRobinCoeff (core/pde.h:62-78)
-    ZG_D bool hasNonZeroRobinCoeff() const {
+    ZG_D bool hasNonZeroRobinCoeff(V<D> x) const {
         if (p->are_robin_conditions_pure_neumann) return false;
-        return fabsf(robinCoeff(true)) > 0.0f || fabsf(robinCoeff(false)) > 0.0f;
+        return fabsf(robinCoeff(x, true)) > 0.0f || fabsf(robinCoeff(x, false)) > 0.0f;
     }
 };
 

@@ -61,8 +61,6 @@ struct Carver {
     }
 };
 
-bool fieldOk(int kind) { return kind == ZGPU_FIELD_ZERO || kind == ZGPU_FIELD_CONSTANT || kind == ZGPU_FIELD_ANALYTIC; }
-
 }  // namespace
 
 extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
@@ -89,10 +87,10 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
         return fail(ZGPU_ERR_INVALID_ARG, "zgpu_solve_static does not split walks: splitting_threshold must be FLT_MAX");
     if (ws->max_walk_length <= 0 || !(ws->epsilon_shell_for_absorbing_boundary >= 0.0f) || !(pde->absorption_coeff >= 0.0f))
         return fail(ZGPU_ERR_INVALID_ARG, "invalid walk settings or absorption coefficient");
-    if (!fieldOk(pde->source_kind) || !fieldOk(pde->dirichlet_kind) || !fieldOk(pde->robin_kind) ||
-        (pde->robin_coeff_kind != ZGPU_FIELD_ZERO && pde->robin_coeff_kind != ZGPU_FIELD_CONSTANT) ||
-        pde->solution.n_terms < 0 || pde->solution.n_terms > ZGPU_MAX_TERMS)
-        return fail(ZGPU_ERR_UNSUPPORTED, "PDE fields must be ZERO, CONSTANT or ANALYTIC (robin_coeff ZERO/CONSTANT)");
+    // grids must already be on the device: this entry point copies nothing
+    if (int st = checkPdeFields(pde, D, false)) return st;
+    if (pde->solution.n_terms < 0 || pde->solution.n_terms > ZGPU_MAX_TERMS)
+        return fail(ZGPU_ERR_INVALID_ARG, "analytic solution has %d terms (max %d)", pde->solution.n_terms, ZGPU_MAX_TERMS);
 
     SolveParams P;
     std::memset(&P, 0, sizeof(P));

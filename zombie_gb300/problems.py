@@ -247,6 +247,56 @@ def make_pde(solution, sigma=0.0, dirichlet=True, robin=False, robin_coeff=0.0, 
     return p
 
 
+def with_grid_fields(pr, fields=("dirichlet",), shape=None, interpolate=True, robin_coeff=None):
+    """Replaces analytic PDE fields of pr by dense grids sampled at the cell centres of the
+    domain box (DenseGrid<float, 1, DIM>): "dirichlet" (g = u) and "source" (f = -Lap u +
+    sigma u).  robin_coeff: a callable kappa(x) sampled onto a "robin_coeff" grid (the Robin
+    data stays analytic, h = du/dn + kappa(x) u, so u remains the exact solution); the
+    boundary's per-primitive coefficient bounds become the grid's range.  The grid arrays are
+    kept on pr.grids (the descriptor points at them)."""
+    D = pr.dim
+    shape = tuple(shape or ((1024, 1024) if D == 2 else (96, 96, 96)))
+    lo = np.asarray(pr.domain_min[:D], np.float64)
+    hi = np.asarray(pr.domain_max[:D], np.float64)
+    axes = [lo[i] + (np.arange(shape[i]) + 0.5) * (hi[i] - lo[i]) / shape[i] for i in range(D)]
+    centres = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, D)
+    u, _, lap = eval_analytic(pr.solution, centres)
+    pr.grids = getattr(pr, "grids", [])
+
+    def grid(values):
+        v = np.ascontiguousarray(values, np.float32)
+        pr.grids.append(v)
+        g = A.Grid()
+        g.values = v.ctypes.data
+        for i in range(D):
+            g.shape[i] = shape[i]
+            g.grid_min[i] = lo[i]
+            g.grid_max[i] = hi[i]
+        g.enable_interpolation = int(interpolate)
+        return g
+    for f in fields:
+        if f == "dirichlet":
+            pr.pde.dirichlet_kind = A.ZGPU_FIELD_GRID
+            pr.pde.dirichlet_grid = grid(u)
+        elif f == "source":
+            pr.pde.source_kind = A.ZGPU_FIELD_GRID
+            pr.pde.is_source_constant = 0
+            pr.pde.source_grid = grid(-lap + pr.pde.absorption_coeff * u)
+        else:
+            raise ValueError(f"unknown grid field {f}")
+    if robin_coeff is not None:
+        k = np.asarray(robin_coeff(centres), np.float32)
+        pr.pde.robin_coeff_kind = A.ZGPU_FIELD_GRID
+        pr.pde.robin_coeff_grid = grid(k)
+        pr.pde.are_robin_conditions_pure_neumann = 0
+        pr.pde.are_robin_coeffs_nonnegative = int(k.min() >= 0.0)
+        n = len(pr.reflecting[1])
+        pr.robin_coeff_range = (np.full(n, k.min(), np.float32), np.full(n, k.max(), np.float32))
+    pr.pde.memory = A.ZGPU_MEM_HOST
+    pr.name += "_grid"
+    return pr
+
+
 def default_walk_settings(eps_abs=1e-3, eps_refl=1e-3, silhouette_precision=1e-3, rr=0.0,
                           splitting=A.FLT_MAX, max_len=1024, tikhonov=0, maximal=None, double_sided=False,
                           ignore_abs=False, ignore_refl=False, ignore_src=False):
@@ -292,6 +342,7 @@ class Problem:
         self.reflecting = None      # (positions, indices)
         self.reflecting_kind = A.ZGPU_BOUNDARY_NEUMANN
         self.robin_coeff = 0.0
+        self.robin_coeff_range = None   # per-primitive (min, max) coefficient bounds; None: robin_coeff
         # threshold of the silhouette-ignore rule (getIgnoreCandidateSilhouetteCallback,
         # utils/fcpw_geometric_queries.h:1029-1038): 0 keeps every non-convex vertex/edge.
         # The reference default 1e-3 drops nearly flat concave features of finely

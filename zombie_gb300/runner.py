@@ -27,8 +27,11 @@ class GpuProblem:
             if problem.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN:
                 h = GpuRobinBoundaryHandler(D, self.ctx)
                 n = len(problem.reflecting[1])
-                k = np.full(n, problem.robin_coeff, np.float32)
-                h.build_acceleration_structure(*problem.reflecting, ic, k, k)
+                if problem.robin_coeff_range is not None:
+                    kmin, kmax = problem.robin_coeff_range
+                else:
+                    kmin = kmax = np.full(n, problem.robin_coeff, np.float32)
+                h.build_acceleration_structure(*problem.reflecting, ic, kmin, kmax)
             else:
                 h = GpuNeumannBoundaryHandler(D, self.ctx)
                 h.build_acceleration_structure(*problem.reflecting, ic)
