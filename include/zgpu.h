@@ -297,15 +297,19 @@ int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, cons
                                float* out_normal, float* out_pdf, int memory);
 
 /*
- * FcpwDirichletBoundaryHandler::buildAccelerationStructure with the tree built on the GPU
- * (no counterpart in the reference, which builds on the CPU): a linear BVH over Morton codes
- * of the primitive centroids, collapsed to the same 4-wide node layout. Absorbing boundaries
- * only (reflecting boundaries need adjacency, cones and silhouette trees, built on the host).
- * positions / indices may live in host or device memory (`memory`).  Queries answer as on a
- * host-built tree; a tree deeper than the traversal stack returns ZGPU_ERR_UNSUPPORTED.
+ * zgpu_boundary_create with everything built on the GPU (no counterpart in the reference,
+ * which builds on the CPU): a linear BVH over Morton codes of the primitive centres,
+ * collapsed to the same 4-wide node layout; for reflecting boundaries also the face
+ * adjacency, silhouette flags, normal cones (merged bottom-up: possibly wider than the host
+ * builder's, never narrower), Robin coefficient ranges and the silhouette-candidate tree.
+ * positions / indices / min_robin / max_robin live in host or device memory (`memory`).
+ * Queries answer as on a host-built tree; a tree deeper than the traversal stack returns
+ * ZGPU_ERR_UNSUPPORTED.
  */
 int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
-                                   const int* indices, int n_prims, int memory, zgpu_boundary** out);
+                                   const int* indices, int n_prims, int kind, const float* min_robin,
+                                   const float* max_robin, int solve_double_sided, float silhouette_precision,
+                                   int memory, zgpu_boundary** out);
 
 /* ------------------------------- solve ----------------------------------- */
 /*

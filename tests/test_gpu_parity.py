@@ -686,6 +686,81 @@ def test_device_built_bvh_answers_like_the_host_built_one(zgpu, dim, level):
     assert np.array_equal(host.count_hits(x, d, tm), dev.count_hits(x, d, tm))
 
 
+@pytest.mark.parametrize("dim,kind,level", [(2, A.ZGPU_BOUNDARY_NEUMANN, None), (3, A.ZGPU_BOUNDARY_NEUMANN, 3),
+                                            (3, A.ZGPU_BOUNDARY_NEUMANN, 5), (2, A.ZGPU_BOUNDARY_ROBIN, None),
+                                            (3, A.ZGPU_BOUNDARY_ROBIN, 4)])
+def test_device_built_reflecting_boundary_answers_like_the_host_built_one(zgpu, oracle, dim, kind, level):
+    """Reflecting boundaries built on the GPU (adjacency, silhouette flags, normal cones,
+    Robin coefficient ranges and the silhouette-candidate tree all on the device): closest
+    points as on the host-built tree; Neumann star radii (closest silhouette points) identical;
+    Robin star radii against the oracle's brute force as for host-built trees, and refitted
+    by a coefficient update exactly like a fresh device build."""
+    from zombie_gb300 import api
+    if dim == 2:
+        pos, idx = P.star_polygon(4096)
+    else:
+        pos, idx, _ = P.displaced_icosphere(level, seed=5)
+    n = idx.shape[0]
+    ic = api.IgnoreCandidateSilhouette(False, 0.0)
+    robin = kind == A.ZGPU_BOUNDARY_ROBIN
+    kmin, kmax = _mixed_robin(n, 21) if robin else (None, None)
+    cls = api.GpuRobinBoundaryHandler if robin else api.GpuNeumannBoundaryHandler
+    host, dev = cls(dim), cls(dim)
+    args = (pos, idx, ic, kmin, kmax) if robin else (pos, idx, ic)
+    host.build_acceleration_structure(*args)
+    dev.build_acceleration_structure(*args, build_on_device=True)
+    assert dev.info()["depth"] <= 20
+    assert dev.signed_volume() == pytest.approx(host.signed_volume(), rel=1e-5)
+    rng = np.random.default_rng(31)
+    m = 8000
+    x = rng.uniform(-0.7, 0.7, (m, dim)).astype(np.float32)
+    assert np.array_equal(host.closest_point(x)[2], dev.closest_point(x)[2])
+    mn = np.full(m, 1e-3, np.float32)
+    mx = np.where(rng.random(m) < 0.3, A.FLT_MAX, rng.uniform(0.05, 2.0, m)).astype(np.float32)
+    for flip in (0, 1):
+        fl = np.full(m, flip, np.int32)
+        rh = host.star_radius(x, mn, mx, 1e-3, fl)
+        rd = dev.star_radius(x, mn, mx, 1e-3, fl)
+        if not robin:
+            assert np.array_equal(rh, rd)
+            continue
+        ob = oracle.Boundary(dim, pos, idx, kind=kind, kmin=kmin, kmax=kmax, silhouette_precision=0.0, use_bvh=False)
+        orr = ob.star_radius(x, mn, mx, 1e-3, fl)
+        for r in (rh, rd):
+            rel = np.abs(r - orr) / np.maximum(orr, 1e-30)
+            assert np.median(rel) <= 1e-6
+            assert np.quantile(rel, 0.99) <= 2e-3
+            assert np.mean(rel <= 1e-5) > 0.95
+    if robin:
+        k2min, k2max = _mixed_robin(n, 22)
+        dev.update_coefficient_values(k2min, k2max)
+        fresh = cls(dim)
+        fresh.build_acceleration_structure(pos, idx, ic, k2min, k2max, build_on_device=True)
+        fl = np.zeros(m, np.int32)
+        assert np.array_equal(dev.star_radius(x, mn, mx, 1e-3, fl), fresh.star_radius(x, mn, mx, 1e-3, fl))
+
+
+@pytest.mark.parametrize("make", [lambda: P.mixed_wost_2d(n_segments=4096, grid=32, spp=128),
+                                  lambda: P.robin_wost_3d(level=4, n_points=400, spp=128)])
+def test_solves_on_device_built_boundaries(zgpu, make):
+    """Walk on Stars over boundaries built entirely on the GPU: Neumann walks are the walks of
+    the host-built boundaries (identical queries); Robin estimates agree within their errors."""
+    from zombie_gb300.runner import GpuProblem, summarize
+    pr = make()
+    a, b = GpuProblem(pr), GpuProblem(pr, build_on_device=True)
+    xa, xb = a.host_arrays(), b.host_arrays()
+    ra, rb = a.solve(xa), b.solve(xb)
+    assert ra.error_word == 0 and rb.error_word == 0
+    if pr.reflecting_kind == A.ZGPU_BOUNDARY_NEUMANN:
+        assert ra.total_steps == rb.total_steps
+        assert np.array_equal(xa["total_walk_length"], xb["total_walk_length"])
+    ga, gb = summarize(xa, pr.exact()), summarize(xb, pr.exact())
+    z = (ga["mean"] - gb["mean"]) / np.maximum(np.sqrt(ga["se"] ** 2 + gb["se"] ** 2), 1e-12)
+    assert np.mean(np.abs(z) > 3.5) < 0.02
+    ez = gb["err"] / np.maximum(gb["se"], 1e-12)
+    assert abs(ez.mean()) < 0.5
+
+
 def test_step_budget_drops_walks_and_reports_it(zgpu):
     """zgpu_solve_options.step_budget caps the loop iterations of a walk state: a budget
     below the walks' lengths returns ZGPU_ERR_TIMEOUT_BUDGET, a generous one changes nothing."""

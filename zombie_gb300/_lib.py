@@ -38,7 +38,7 @@ def lib():
         L.zgpu_context_stream.restype = vp
         L.zgpu_boundary_create.argtypes = [vp, i32, vp, i32, vp, i32, i32, vp, vp, i32, f32, i32, pp]
         L.zgpu_boundary_destroy.argtypes = [vp]
-        L.zgpu_boundary_create_on_device.argtypes = [vp, i32, vp, i32, vp, i32, i32, pp]
+        L.zgpu_boundary_create_on_device.argtypes = [vp, i32, vp, i32, vp, i32, i32, vp, vp, i32, f32, i32, pp]
         L.zgpu_boundary_update_robin_coefficients.argtypes = [vp, vp, vp]
         L.zgpu_boundary_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64)]

@@ -561,18 +561,35 @@ class _BoundaryHandler:
         self.n_prims = 0
 
     def _build(self, positions, indices, kmin=None, kmax=None, solve_double_sided=False,
-               silhouette_precision=1e-3, bvh_width=4):
-        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, self.dim)
-        idx = np.ascontiguousarray(indices, np.int32).reshape(-1, self.dim)
-        kmn = None if kmin is None else np.ascontiguousarray(kmin, np.float32)
-        kmx = None if kmax is None else np.ascontiguousarray(kmax, np.float32)
+               silhouette_precision=1e-3, bvh_width=4, build_on_device=False):
+        """Builds on the host (binned SAH), or with build_on_device on the GPU
+        (zgpu_boundary_create_on_device: linear BVH, cones and silhouette trees built there);
+        the arrays may then be CUDA tensors."""
+        dev = build_on_device and hasattr(positions, "is_cuda") and positions.is_cuda
+        if dev:
+            import torch
+            pos = positions.contiguous().to(torch.float32).reshape(-1, self.dim)
+            idx = indices.contiguous().to(torch.int32).reshape(-1, self.dim)
+            kmn = None if kmin is None else torch.as_tensor(kmin, dtype=torch.float32, device=pos.device).contiguous()
+            kmx = None if kmax is None else torch.as_tensor(kmax, dtype=torch.float32, device=pos.device).contiguous()
+        else:
+            pos = np.ascontiguousarray(positions, np.float32).reshape(-1, self.dim)
+            idx = np.ascontiguousarray(indices, np.int32).reshape(-1, self.dim)
+            kmn = None if kmin is None else np.ascontiguousarray(kmin, np.float32)
+            kmx = None if kmax is None else np.ascontiguousarray(kmax, np.float32)
         self.close()
         h = C.c_void_p()
-        check(lib().zgpu_boundary_create(self.ctx.h, self.dim, A.ptr(pos), pos.shape[0], A.ptr(idx), idx.shape[0],
-                                         self.kind, A.ptr(kmn), A.ptr(kmx), int(solve_double_sided),
-                                         float(silhouette_precision), int(bvh_width), C.byref(h)))
+        if build_on_device:
+            check(lib().zgpu_boundary_create_on_device(self.ctx.h, self.dim, A.ptr(pos), int(pos.shape[0]), A.ptr(idx),
+                                                       int(idx.shape[0]), self.kind, A.ptr(kmn), A.ptr(kmx),
+                                                       int(solve_double_sided), float(silhouette_precision),
+                                                       A.ZGPU_MEM_DEVICE if dev else A.ZGPU_MEM_HOST, C.byref(h)))
+        else:
+            check(lib().zgpu_boundary_create(self.ctx.h, self.dim, A.ptr(pos), pos.shape[0], A.ptr(idx), idx.shape[0],
+                                             self.kind, A.ptr(kmn), A.ptr(kmx), int(solve_double_sided),
+                                             float(silhouette_precision), int(bvh_width), C.byref(h)))
         self.h = h
-        self.n_prims = idx.shape[0]
+        self.n_prims = int(idx.shape[0])
         self.positions, self.indices = pos, idx
 
     def info(self):
@@ -687,25 +704,7 @@ class GpuDirichletBoundaryHandler(_BoundaryHandler):
 
     def build_acceleration_structure(self, positions, indices, build_bvh=True, enable_bvh_vectorization=False,
                                      print_stats=False, build_on_device=False):
-        """build_on_device: the tree is built on the GPU (linear BVH over Morton codes,
-        zgpu_boundary_create_on_device); positions/indices may then be CUDA tensors."""
-        if not build_on_device:
-            self._build(positions, indices)
-            return
-        self.close()
-        dev = hasattr(positions, "is_cuda") and positions.is_cuda
-        if dev:
-            pos, idx = positions.contiguous(), indices.contiguous()
-            nv, npr = int(pos.shape[0]), int(idx.shape[0])
-        else:
-            pos = np.ascontiguousarray(positions, np.float32).reshape(-1, self.dim)
-            idx = np.ascontiguousarray(indices, np.int32).reshape(-1, self.dim)
-            nv, npr = pos.shape[0], idx.shape[0]
-        h = C.c_void_p()
-        check(lib().zgpu_boundary_create_on_device(self.ctx.h, self.dim, A.ptr(pos), nv, A.ptr(idx), npr,
-                                                   A.ZGPU_MEM_DEVICE if dev else A.ZGPU_MEM_HOST, C.byref(h)))
-        self.h = h
-        self.n_prims = npr
+        self._build(positions, indices, build_on_device=build_on_device)
 
 
 class GpuNeumannBoundaryHandler(_BoundaryHandler):
@@ -713,10 +712,10 @@ class GpuNeumannBoundaryHandler(_BoundaryHandler):
     kind = A.ZGPU_BOUNDARY_NEUMANN
 
     def build_acceleration_structure(self, positions, indices, ignore_candidate_silhouette=None, build_bvh=True,
-                                     enable_bvh_vectorization=False, print_stats=False):
+                                     enable_bvh_vectorization=False, print_stats=False, build_on_device=False):
         ic = ignore_candidate_silhouette or IgnoreCandidateSilhouette()
         self._build(positions, indices, solve_double_sided=ic.solve_double_sided,
-                    silhouette_precision=ic.silhouette_precision)
+                    silhouette_precision=ic.silhouette_precision, build_on_device=build_on_device)
 
 
 class GpuRobinBoundaryHandler(_BoundaryHandler):
@@ -725,13 +724,13 @@ class GpuRobinBoundaryHandler(_BoundaryHandler):
 
     def build_acceleration_structure(self, positions, indices, ignore_candidate_silhouette=None,
                                      min_robin_coeff_values=None, max_robin_coeff_values=None, build_bvh=True,
-                                     enable_bvh_vectorization=False, print_stats=False):
+                                     enable_bvh_vectorization=False, print_stats=False, build_on_device=False):
         ic = ignore_candidate_silhouette or IgnoreCandidateSilhouette()
-        n = np.asarray(indices).reshape(-1, self.dim).shape[0]
+        n = int(indices.shape[0]) if hasattr(indices, "is_cuda") else np.asarray(indices).reshape(-1, self.dim).shape[0]
         kmin = np.zeros(n, np.float32) if min_robin_coeff_values is None else min_robin_coeff_values
         kmax = np.zeros(n, np.float32) if max_robin_coeff_values is None else max_robin_coeff_values
         self._build(positions, indices, kmin, kmax, solve_double_sided=ic.solve_double_sided,
-                    silhouette_precision=ic.silhouette_precision)
+                    silhouette_precision=ic.silhouette_precision, build_on_device=build_on_device)
 
     def update_coefficient_values(self, min_robin_coeff_values, max_robin_coeff_values):
         kmin = np.ascontiguousarray(min_robin_coeff_values, np.float32)

@@ -293,16 +293,23 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
 }
 
 int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
-                                   const int* indices, int n_prims, int memory, zgpu_boundary** out) {
+                                   const int* indices, int n_prims, int kind, const float* min_robin,
+                                   const float* max_robin, int solve_double_sided, float silhouette_precision,
+                                   int memory, zgpu_boundary** out) {
     if (!ctx || !out) return fail(ZGPU_ERR_INVALID_ARG, "context/out is NULL");
     *out = nullptr;
     if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
+    if (kind < ZGPU_BOUNDARY_ABSORBING || kind > ZGPU_BOUNDARY_ROBIN) return fail(ZGPU_ERR_INVALID_ARG, "unknown boundary kind %d", kind);
     if (n_prims < 0 || n_vertices < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative sizes");
+    if (n_prims >= (1 << 27)) return fail(ZGPU_ERR_INVALID_ARG, "too many primitives");
     if (n_prims > 0 && (!positions || !indices)) return fail(ZGPU_ERR_INVALID_ARG, "positions/indices are NULL");
+    if (kind == ZGPU_BOUNDARY_ROBIN && n_prims > 0 && (!min_robin || !max_robin))
+        return fail(ZGPU_ERR_INVALID_ARG, "Robin boundary needs min/max Robin coefficients per primitive");
     if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
     ZG_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    // host copies: index validation and the signed volume
+    // host copies: index validation and the signed volume (computeSignedVolume,
+    // utils/fcpw_geometric_queries.h:431-458)
     std::vector<float> hp((size_t)n_vertices * dim);
     std::vector<int> hi((size_t)n_prims * dim);
     if (memory == ZGPU_MEM_HOST) {
@@ -326,36 +333,66 @@ int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* posi
                     ((double)a[0] * b[1] - (double)a[1] * b[0]) * c[2]) / 6.0;
         }
     }
+    // inputs on the device
+    const bool robin = kind == ZGPU_BOUNDARY_ROBIN;
     const float* dp = positions;
     const int* di = indices;
-    float* tp = nullptr;
-    int* ti = nullptr;
+    const float* dkn = robin ? min_robin : nullptr;
+    const float* dkx = robin ? max_robin : nullptr;
+    std::vector<void*> staged;
+    auto stage = [&](const void* src, size_t bytes, const void** dst) -> cudaError_t {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+        if (e != cudaSuccess) return e;
+        staged.push_back(p);
+        *dst = p;
+        return cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+    };
+    auto freeStaged = [&]() { for (void* p : staged) cudaFree(p); };
+    cudaError_t e = cudaSuccess;
     if (memory == ZGPU_MEM_HOST && n_prims > 0) {
-        ZG_CUDA(cudaMalloc(&tp, hp.size() * sizeof(float)));
-        if (cudaMalloc(&ti, hi.size() * sizeof(int)) != cudaSuccess) { cudaFree(tp); return fail(ZGPU_ERR_OUT_OF_MEMORY, "staging"); }
-        cudaMemcpy(tp, hp.data(), hp.size() * sizeof(float), cudaMemcpyHostToDevice);
-        cudaMemcpy(ti, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice);
-        dp = tp; di = ti;
+        e = stage(hp.data(), hp.size() * sizeof(float), (const void**)&dp);
+        if (e == cudaSuccess) e = stage(hi.data(), hi.size() * sizeof(int), (const void**)&di);
+        if (e == cudaSuccess && robin) e = stage(min_robin, (size_t)n_prims * sizeof(float), (const void**)&dkn);
+        if (e == cudaSuccess && robin) e = stage(max_robin, (size_t)n_prims * sizeof(float), (const void**)&dkx);
+        if (e != cudaSuccess) { freeStaged(); return fail(ZGPU_ERR_OUT_OF_MEMORY, "staging: %s", cudaGetErrorString(e)); }
     }
-    float4 *nodes = nullptr, *prims = nullptr;
-    int* primIndex = nullptr;
-    int nNodes = 0, depth = 0;
-    cudaError_t e = buildWideBvhOnDevice(dim, dp, di, n_prims, s, &nodes, &nNodes, &prims, &primIndex, &depth);
-    if (tp) cudaFree(tp);
-    if (ti) cudaFree(ti);
+    DeviceBuilt db;
+    e = buildBoundaryOnDevice(dim, dp, n_vertices, di, n_prims, kind, dkn, dkx, solve_double_sided != 0,
+                              silhouette_precision, s, db);
+    freeStaged();
+    auto release = [&]() {
+        cudaFree(db.nodes); cudaFree(db.cones); cudaFree(db.prims); cudaFree(db.sil); cudaFree(db.primIndex);
+        cudaFree(db.silTree); cudaFree(db.silCones); cudaFree(db.silFeat);
+    };
     if (e == cudaErrorNotSupported)
         return fail(ZGPU_ERR_UNSUPPORTED, "device-built BVH deeper than the traversal stack (%d levels); build on the host",
                     kMaxWideDepth);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        release();
         return fail(e == cudaErrorMemoryAllocation ? ZGPU_ERR_OUT_OF_MEMORY : ZGPU_ERR_CUDA, "device BVH build: %s",
                     cudaGetErrorString(e));
+    }
     zgpu_boundary* b = new zgpu_boundary();
-    b->ctx = ctx; b->dim = dim; b->kind = ZGPU_BOUNDARY_ABSORBING; b->nPrims = n_prims; b->nNodes = nNodes;
-    b->depth = depth; b->signedVolume = (float)vol;
-    b->nodes = nodes; b->prims = prims; b->primIndex = primIndex;
-    b->view.nodes = nodes; b->view.prims = prims; b->view.primIndex = primIndex;
-    b->view.nNodes = nNodes; b->view.nPrims = n_prims;
-    b->view.stackEntries = stackEntriesForDepth(std::max(depth, 1));
+    b->ctx = ctx; b->dim = dim; b->kind = kind; b->nPrims = n_prims; b->nNodes = db.nNodes;
+    b->depth = db.depth; b->signedVolume = (float)vol;
+    b->nodes = db.nodes; b->cones = db.cones; b->prims = db.prims; b->sil = db.sil; b->primIndex = db.primIndex;
+    b->silTree = db.silTree; b->silCones = db.silCones; b->silFeat = db.silFeat;
+    if (robin && n_prims > 0) {
+        // leaf slot -> caller index, for coefficient updates
+        b->primIndexHost.resize(n_prims);
+        if (cudaMemcpy(b->primIndexHost.data(), db.primIndex, sizeof(int) * n_prims, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            zgpu_boundary_destroy(b);
+            return fail(ZGPU_ERR_CUDA, "device BVH build: reading the primitive order");
+        }
+    }
+    b->view.nodes = b->nodes; b->view.cones = b->cones; b->view.prims = b->prims; b->view.sil = b->sil;
+    b->view.primIndex = b->primIndex;
+    b->view.nNodes = b->nNodes; b->view.nPrims = n_prims;
+    b->view.stackEntries = stackEntriesForDepth(std::max(std::max(db.depth, db.silDepth), 1));
+    b->view.silTree = b->silTree; b->view.silCones = b->silCones; b->view.silFeat = b->silFeat;
+    b->view.silNodes = db.silNodes;
+    b->view.robin = robin;
     *out = b;
     return ZGPU_OK;
 }

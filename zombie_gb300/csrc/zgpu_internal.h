@@ -117,8 +117,22 @@ int contextDevice(const zgpu_context* ctx);
 size_t scanScratchElems(int64_t n);
 
 // device-side LBVH build of an absorbing boundary's 4-wide tree (zgpu_devbuild.cu)
-cudaError_t buildWideBvhOnDevice(int D, const float* pos, const int* idx, int nP, cudaStream_t s, float4** outNodes,
-                                 int* outNodeCount, float4** outPrims, int** outPrimIndex, int* outDepth);
+// a boundary built on the device (zgpu_devbuild.cu): device arrays owned by the receiver
+struct DeviceBuilt {
+    float4* nodes = nullptr;
+    float4* cones = nullptr;       // reflecting boundaries
+    float4* prims = nullptr;
+    float4* sil = nullptr;         // reflecting boundaries
+    int* primIndex = nullptr;
+    float4* silTree = nullptr;     // reflecting boundaries with silhouette candidates
+    float4* silCones = nullptr;
+    float4* silFeat = nullptr;
+    int nNodes = 0, depth = 0, silNodes = 0, silDepth = 0, silFeatures = 0;
+};
+// pos [nV * D], idx [nP * D], kmin / kmax [nP] (Robin) in device memory; kind 0 absorbing,
+// 1 Neumann, 2 Robin.  cudaErrorNotSupported: a tree deeper than the traversal stack.
+cudaError_t buildBoundaryOnDevice(int D, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
+                                  const float* kmax, bool doubleSided, float prec, cudaStream_t s, DeviceBuilt& out);
 
 // accessors into the C ABI objects (zgpu_api.cu)
 void setLastError(const char* msg);

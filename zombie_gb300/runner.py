@@ -13,7 +13,7 @@ from .api import (GeometricQueries, GpuDirichletBoundaryHandler, GpuNeumannBound
 
 
 class GpuProblem:
-    def __init__(self, problem, context=None, seed_base=0x5eed, options=None):
+    def __init__(self, problem, context=None, seed_base=0x5eed, options=None, build_on_device=False):
         self.problem = problem
         self.ctx = context or default_context()
         D = problem.dim
@@ -21,7 +21,7 @@ class GpuProblem:
         ic = IgnoreCandidateSilhouette(bool(problem.settings.solve_double_sided), problem.ignore_silhouette_precision)
         if problem.absorbing is not None and len(problem.absorbing[1]) > 0:
             h = GpuDirichletBoundaryHandler(D, self.ctx)
-            h.build_acceleration_structure(*problem.absorbing)
+            h.build_acceleration_structure(*problem.absorbing, build_on_device=build_on_device)
             self.queries.absorbing = h
         if problem.reflecting is not None and len(problem.reflecting[1]) > 0:
             if problem.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN:
@@ -31,10 +31,10 @@ class GpuProblem:
                     kmin, kmax = problem.robin_coeff_range
                 else:
                     kmin = kmax = np.full(n, problem.robin_coeff, np.float32)
-                h.build_acceleration_structure(*problem.reflecting, ic, kmin, kmax)
+                h.build_acceleration_structure(*problem.reflecting, ic, kmin, kmax, build_on_device=build_on_device)
             else:
                 h = GpuNeumannBoundaryHandler(D, self.ctx)
-                h.build_acceleration_structure(*problem.reflecting, ic)
+                h.build_acceleration_structure(*problem.reflecting, ic, build_on_device=build_on_device)
             self.queries.reflecting = h
         self.pde = PDE.from_c(D, problem.pde)
         self.solver = (WalkOnSpheres if problem.solver == A.ZGPU_SOLVER_WALK_ON_SPHERES else WalkOnStars)(
