@@ -465,6 +465,11 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
+        if not args.skip_build_times and not dist:
+            try:
+                line["boundary_build"] = boundary_build_times(ctx)
+            except Exception as e:
+                line["boundary_build"] = {"error": f"{type(e).__name__}: {e}"}
         if args.ttr_points > 0 and not dist:
             try:
                 line["time_to_rmse"] = time_to_rmse(ctx, args.ttr_points, budget_s=args.ttr_budget)
@@ -475,6 +480,45 @@ def run_gpu(args):
         tdist.barrier()
         tdist.destroy_process_group()
     return line
+
+
+def boundary_build_times(ctx):
+    """Wall time of building boundaries on the host (binned SAH, cones and silhouette trees on
+    one CPU thread) and on the GPU (zgpu_boundary_create_on_device), after one warm-up build."""
+    from zombie_gb300 import api
+    from zombie_gb300 import problems as P
+    scenes = []
+    pos8, idx8, _ = P.displaced_icosphere(8, seed=0)
+    scenes.append(("absorbing icosphere L8", api.GpuDirichletBoundaryHandler, 3, pos8, idx8, None))
+    pos7, idx7, _ = P.displaced_icosphere(7, seed=0)
+    scenes.append(("Neumann icosphere L7", api.GpuNeumannBoundaryHandler, 3, pos7, idx7, None))
+    pos6, idx6, _ = P.displaced_icosphere(6, seed=0)
+    k6 = np.full(len(idx6), 2.0, np.float32)
+    scenes.append(("Robin icosphere L6", api.GpuRobinBoundaryHandler, 3, pos6, idx6, k6))
+    pos2, idx2 = P.star_polygon(1 << 16)
+    scenes.append(("Neumann star polygon 65536", api.GpuNeumannBoundaryHandler, 2, pos2, idx2, None))
+    ic = api.IgnoreCandidateSilhouette(False, 1e-3)
+    out = {}
+    for name, cls, dim, pos, idx, k in scenes:
+        def build(on_device):
+            h = cls(dim, ctx)
+            args = (pos, idx) if cls is api.GpuDirichletBoundaryHandler else (pos, idx, ic)
+            if k is not None:
+                args = args + (k, k)
+            t0 = time.perf_counter()
+            h.build_acceleration_structure(*args, build_on_device=on_device)
+            ctx.synchronize()
+            dt = time.perf_counter() - t0
+            info = h.info()
+            h.close()
+            return dt, info
+        build(True)
+        td, info_d = build(True)
+        th, info_h = build(False)
+        out[name] = {"primitives": int(len(idx)), "host_s": th, "device_s": td, "speedup": th / td,
+                     "depth_host": info_h["depth"], "depth_device": info_d["depth"]}
+        log("boundary build", name, out[name])
+    return out
 
 
 def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2), budget_s=150.0, level=8):
@@ -561,6 +605,8 @@ def main():
     ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-build-times", action="store_true",
+                    help="skip the host vs device boundary build timings")
     ap.add_argument("--ttr-points", type=int, default=1 << 19,
                     help="evaluation points of the neural-cache time-to-RMSE comparison (0 = skip)")
     ap.add_argument("--ttr-budget", type=float, default=300.0, help="seconds allowed for that comparison")
