@@ -324,8 +324,9 @@ int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* quer
                const zgpu_solve_options* options, zgpu_solve_report* report);
 
 /*
- * Batched many-solve: `n_scenes` independent problems in one launch.  points->scene_id
- * selects the row of queries/pdes/settings for every point.
+ * Batched many-solve: `n_scenes` independent problems of one dimension (2D or 3D) in one
+ * launch.  points->scene_id selects the row of queries/pdes/settings for every point; each
+ * point runs the walks it runs in a single-scene solve.
  */
 int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
                        const zgpu_geometric_queries* queries, const zgpu_pde* pdes,
@@ -335,7 +336,8 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
 
 /*
  * Autotuner (no counterpart in the reference): times launch configurations (block size
- * 32/64/128 x blocks per SM auto/2/4, and for Walk on Spheres the query mode) on a stride
+ * 32/64/128 x blocks per SM auto/2/4, and the query mode for Walk on Spheres and for Walk
+ * on Stars on a Robin boundary) on a stride
  * sample of `sample_points` points with `sample_walks` walks each, and writes the fastest
  * into `out_options`.  Results are cached in the context per scene signature (dimension,
  * solver, log2 primitive counts, reflecting kind, screening); a cached answer returns with
@@ -432,6 +434,70 @@ int zgpu_solve_cached(zgpu_context* ctx, int solver, const zgpu_geometric_querie
                       const zgpu_sample_points* points, zgpu_sample_statistics* stats,
                       const zgpu_solve_options* options, zgpu_cache* cache, float min_distance,
                       zgpu_solve_report* report);
+
+/* ------------------------------ PDE fields -------------------------------- */
+/*
+ * The PDE's fields at n points as the walks read them: source(x), dirichlet(x, aligned),
+ * robin(x, n, aligned), robinCoeff(x, n, aligned) (core/pde.h:29-41).  normal and aligned may
+ * be NULL (zero normal, not aligned); any output may be NULL.  All arrays in `memory`.
+ */
+int zgpu_pde_evaluate(zgpu_context* ctx, int dim, const zgpu_pde* pde, int64_t n, const float* x,
+                      const float* normal, const int32_t* aligned, int memory, float* out_source,
+                      float* out_dirichlet, float* out_robin, float* out_robin_coeff);
+
+/* ------------------------- boundary value caching -------------------------- */
+/*
+ * Boundary Value Caching (variance_reduction/boundary_value_caching.h).  A cache is a set of
+ * SamplePoints with the members the splat reads: position, normal, pdf, type
+ * (ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY / ON_REFLECTING_BOUNDARY: boundary samples;
+ * ZGPU_SAMPLE_IN_DOMAIN: source samples), estimate_normal_aligned, and the estimated
+ * solution, normalDerivative, contribution (Robin data or source value) and robinCoeff.
+ */
+typedef struct zgpu_bvc_samples {
+    int64_t n;
+    const float* pt;                  /* [n*dim] */
+    const float* normal;              /* [n*dim] */
+    const float* pdf;
+    const int32_t* type;
+    const int32_t* estimate_normal_aligned;   /* NULL -> 0 */
+    const float* solution;
+    const float* normal_derivative;
+    const float* contribution;
+    const float* robin_coeff;         /* NULL -> 0 */
+} zgpu_bvc_samples;
+
+/* ZGPU_BVC_* : the five statistics of an EvaluationPoint (boundary_value_caching.h:19-56) */
+enum { ZGPU_BVC_ABSORBING = 0, ZGPU_BVC_ABSORBING_ALIGNED = 1, ZGPU_BVC_REFLECTING = 2,
+       ZGPU_BVC_REFLECTING_ALIGNED = 3, ZGPU_BVC_SOURCE = 4, ZGPU_BVC_GROUPS = 5 };
+
+/*
+ * EvaluationPoints as structure of arrays; each holds five SampleStatistics (solution and
+ * gradient moments, FP64), indexed [point][group] and [point][group][dim].  The estimated
+ * solution of a point is the sum of its five means (EvaluationPoint::getEstimatedSolution).
+ */
+typedef struct zgpu_bvc_eval_points {
+    int64_t n;
+    const float* pt;                  /* [n*dim] */
+    const int32_t* type;              /* NULL -> IN_DOMAIN */
+    const float* dist_to_absorbing;
+    const float* dist_to_reflecting;  /* NULL -> +inf */
+    double* mean;                     /* [n*5] */
+    double* m2;                       /* [n*5] */
+    int32_t* count;                   /* [n*5] */
+    double* gradient_mean;            /* [n*5*dim] */
+    double* gradient_m2;              /* [n*5*dim], may be NULL */
+} zgpu_bvc_eval_points;
+
+/*
+ * BoundaryValueCaching::splat (boundary_value_caching.h:408-425, :652-811): every sample of
+ * the cache splats its free-space Green's function estimate (harmonic, or Yukawa when the
+ * PDE's absorption coefficient is > 0) onto every evaluation point at least the cutoff
+ * distances from the boundaries; statistics merge with what the points already hold.
+ */
+int zgpu_bvc_splat(zgpu_context* ctx, int dim, const zgpu_pde* pde, const zgpu_bvc_samples* samples,
+                   float radius_clamp, float kernel_regularization, float robin_coeff_cutoff_for_normal_derivative,
+                   float cutoff_dist_to_absorbing_boundary, float cutoff_dist_to_reflecting_boundary,
+                   zgpu_bvc_eval_points* eval_points, int memory);
 
 #ifdef __cplusplus
 }

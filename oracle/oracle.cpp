@@ -6,6 +6,7 @@
 #include <cstdio>
 #include "oracle_walk.h"
 #include "oracle_cache.h"
+#include "oracle_bvc.h"
 
 using namespace orc;
 
@@ -81,7 +82,7 @@ void solveImpl(int solver, const zgpu_geometric_queries* gq, const zgpu_pde* pde
                 float fsr = pts->first_sphere_radius ? pts->first_sphere_radius[i] : 0.0f;
                 PointStats ps;
                 GradStats gs;
-                const bool gradient = eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT && type == ZGPU_SAMPLE_IN_DOMAIN &&
+                const bool gradient = eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT &&
                                       st->gradient_mean && st->n_gradient_estimates;
                 if (gradient) {
                     float dB = pts->dist_to_absorbing[i];
@@ -436,4 +437,53 @@ extern "C" double orc_cache_grads(int dim, int levels, int log2T, const float* r
     std::copy(g.w3.begin(), g.w3.end(), gw3);
     *gb3 = g.b3;
     return loss;
+}
+
+// BoundaryValueCaching::splat over all evaluation points (boundary_value_caching.h:427-459 with
+// :380-425 per point): the cache's statistics merged into the points' (common.h:268-310)
+extern "C" int orc_bvc_splat(int dim, float absorption, const zgpu_bvc_samples* s, float radiusClamp, float reg,
+                             float robinCutoff, float cutoffA, float cutoffR, zgpu_bvc_eval_points* ev, int nThreads) {
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const int64_t i = next.fetch_add(1);
+            if (i >= ev->n) break;
+            const float dA = ev->dist_to_absorbing[i];
+            const float dR = ev->dist_to_reflecting ? ev->dist_to_reflecting[i] : std::numeric_limits<float>::max();
+            if (dA < cutoffA || dR < cutoffR) continue;
+            const int type = ev->type ? ev->type[i] : ZGPU_SAMPLE_IN_DOMAIN;
+            SplatStat st[ZGPU_BVC_GROUPS];
+            if (dim == 2) bvcSplatPoint<2>(*s, absorption, radiusClamp, reg, robinCutoff, load<2>(ev->pt + i * 2), type, st);
+            else bvcSplatPoint<3>(*s, absorption, radiusClamp, reg, robinCutoff, load<3>(ev->pt + i * 3), type, st);
+            for (int g = 0; g < ZGPU_BVC_GROUPS; g++) {
+                if (st[g].n == 0) continue;
+                const size_t k = (size_t)i * ZGPU_BVC_GROUPS + g;
+                const int n1 = ev->count[k], n2 = st[g].n, nt = n1 + n2;
+                const double d = st[g].mean - ev->mean[k];
+                if (n1 == 0) { ev->mean[k] = st[g].mean; ev->m2[k] = st[g].m2; }
+                else {
+                    ev->mean[k] += d * ((double)n2 / nt);
+                    ev->m2[k] += st[g].m2 + d * d * ((double)n1 * n2 / nt);
+                }
+                for (int c = 0; c < dim; c++) {
+                    double* gm = ev->gradient_mean + k * dim + c;
+                    double* gv = ev->gradient_m2 ? ev->gradient_m2 + k * dim + c : nullptr;
+                    if (n1 == 0) { *gm = st[g].gmean[c]; if (gv) *gv = st[g].gm2[c]; }
+                    else {
+                        const double e = st[g].gmean[c] - *gm;
+                        *gm += e * ((double)n2 / nt);
+                        if (gv) *gv += st[g].gm2[c] + e * e * ((double)n1 * n2 / nt);
+                    }
+                }
+                ev->count[k] = nt;
+            }
+        }
+    };
+    if (nThreads <= 1) work();
+    else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nThreads; t++) th.emplace_back(work);
+        for (auto& t : th) t.join();
+    }
+    return 0;
 }

@@ -67,6 +67,7 @@ def lib():
         L.orc_offset_point.argtypes = [i32, vp, vp, vp]
         L.orc_eval_pde.argtypes = [i32, vp, i64, vp, vp, i32, vp, vp, vp, vp]
         L.orc_solve.argtypes = [i32, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_uint64)]
+        L.orc_bvc_splat.argtypes = [i32, C.c_float, vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, vp, i32]
         L.orc_hardware_threads.restype = i32
         L.orc_counters.argtypes = [vp]
         L.orc_cache_forward.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, f32, i64, vp, vp, vp]
@@ -275,3 +276,24 @@ class CacheModel:
         loss = lib().orc_cache_grads(*self._args(), x.shape[0], A.ptr(x), A.ptr(t), A.ptr(g["table"]), A.ptr(g["W1"]),
                                      A.ptr(g["b1"]), A.ptr(g["W2"]), A.ptr(g["b2"]), A.ptr(g["w3"]), A.ptr(g["b3"]))
         return loss, g
+
+
+def bvc_splat(dim, absorption, samples, evals, radius_clamp=1e-3, kernel_regularization=0.0,
+              robin_coeff_cutoff=float("inf"), cutoff_absorbing=0.0, cutoff_reflecting=0.0, n_threads=None):
+    """BoundaryValueCaching::splat on the CPU: samples / evals are dicts of numpy arrays with the
+    zgpu_bvc_samples / zgpu_bvc_eval_points fields; the evaluation statistics are updated in place."""
+    s = A.BvcSamplesC()
+    s.n = samples["pt"].shape[0]
+    for name in ("pt", "normal", "pdf", "type", "estimate_normal_aligned", "solution", "normal_derivative",
+                 "contribution", "robin_coeff"):
+        setattr(s, name, A.ptr(samples.get(name)))
+    e = A.BvcEvalPointsC()
+    e.n = evals["pt"].shape[0]
+    for name in ("pt", "type", "dist_to_absorbing", "dist_to_reflecting", "mean", "m2", "count", "gradient_mean",
+                 "gradient_m2"):
+        setattr(e, name, A.ptr(evals.get(name)))
+    if n_threads is None:
+        n_threads = max(1, lib().orc_hardware_threads())
+    lib().orc_bvc_splat(dim, float(absorption), C.byref(s), float(radius_clamp), float(kernel_regularization),
+                        float(robin_coeff_cutoff), float(cutoff_absorbing), float(cutoff_reflecting), C.byref(e),
+                        int(n_threads))

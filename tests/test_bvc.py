@@ -1,0 +1,239 @@
+"""Boundary Value Caching: samplers (CPU), the all-pairs splat kernel against the oracle's
+restatement of BoundaryValueCaching::splat, device PDE evaluation against the oracle, and
+end-to-end solves against manufactured solutions."""
+import numpy as np
+import pytest
+
+from zombie_gb300 import _abi as A
+from zombie_gb300 import problems as P
+from zombie_gb300.api import SampleType
+
+
+class _BoxQueries:
+    """Distances for sampler tests on the CPU: to a circle of radius 1 (absorbing), none reflecting."""
+    dim = 2
+
+    def compute_dist_to_absorbing_boundary(self, x, compute_signed_distance=False):
+        return np.abs(1.0 - np.linalg.norm(np.asarray(x, np.float64), axis=1)).astype(np.float32)
+
+    def compute_dist_to_reflecting_boundary(self, x, compute_signed_distance=False):
+        return np.full(np.asarray(x).shape[0], np.finfo(np.float32).max, np.float32)
+
+
+def _circle(n):
+    t = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    pos = np.stack([np.cos(t), np.sin(t)], axis=1).astype(np.float32)
+    idx = np.stack([np.arange(n), (np.arange(n) + 1) % n], axis=1).astype(np.int32)
+    return pos, idx
+
+
+def test_boundary_sampler_pdf_and_offset():
+    """Uniform boundary samples on the inward-displaced polygon: the pdf integrates to one over
+    the displaced boundary (E[1/pdf] = its length), the samples sit at the offset inside, and
+    the double-sided split follows the two sampling masses."""
+    from zombie_gb300 import bvc
+    pos, idx = _circle(512)
+    inside = lambda x: np.linalg.norm(x, axis=1) < 1.5
+    s = bvc.UniformLineSegmentBoundarySampler(pos, idx, inside, seed=1)
+    off = 0.01
+    s.initialize(off, True)
+    q = _BoxQueries()
+    c = s.generate_samples(s.get_sample_count(20000, False), int(SampleType.OnAbsorbingBoundary), off, q, False)
+    r = np.linalg.norm(c.pt, axis=1)
+    assert np.allclose(r, 1.0 - off, atol=2e-4)                   # displaced along the inward vertex normals
+    length = 2 * np.pi * (1.0 - off)
+    assert np.mean(1.0 / c.pdf) == pytest.approx(length, rel=2e-3)
+    assert np.all(c.estimate_normal_aligned == 0)
+    assert np.allclose(np.sum(c.normal * c.pt, axis=1) / r, 1.0, atol=1e-3)   # outward normals
+    ca = s.generate_samples(s.get_sample_count(20000, True), int(SampleType.OnAbsorbingBoundary), off, q, True)
+    assert np.allclose(np.linalg.norm(ca.pt, axis=1), 1.0 + off, atol=2e-4)
+    assert np.all(ca.estimate_normal_aligned == 1)
+    n0, n1 = s.get_sample_count(20000, False), s.get_sample_count(20000, True)
+    assert abs(n0 / (n0 + n1) - (1 - off) / 2) < 2e-3
+
+
+def test_boundary_sampler_weights_and_solve_region():
+    from zombie_gb300 import bvc
+    pos, idx = _circle(256)
+    w = np.where(np.arange(256) < 128, 1.0, 0.0)             # upper half only
+    s = bvc.UniformLineSegmentBoundarySampler(pos, idx, lambda x: np.ones(len(x), bool), primitive_weights=w, seed=2)
+    s.initialize(0.0, False)
+    c = s.generate_samples(5000, int(SampleType.OnAbsorbingBoundary), 0.0, _BoxQueries(), False)
+    assert np.all(c.pt[:, 1] >= -1e-6)
+    # a solve region excluding the left half drops those faces
+    s2 = bvc.UniformLineSegmentBoundarySampler(pos, idx, lambda x: x[:, 0] > 0.0, seed=3)
+    s2.initialize(0.0, False)
+    c2 = s2.generate_samples(5000, int(SampleType.OnAbsorbingBoundary), 0.0, _BoxQueries(), False)
+    assert np.all(c2.pt[:, 0] > -0.03)
+    with pytest.raises(ValueError):
+        bvc.UniformLineSegmentBoundarySampler(pos, idx, lambda x: True, primitive_weights=-w)
+
+
+def test_triangle_sampler_and_domain_sampler():
+    from zombie_gb300 import bvc
+    pos, idx = P.icosphere(3)
+    s = bvc.UniformTriangleBoundarySampler(pos, idx, lambda x: np.ones(len(x), bool), seed=4)
+    s.initialize(0.0, False)
+
+    class Q3(_BoxQueries):
+        dim = 3
+    c = s.generate_samples(20000, int(SampleType.OnAbsorbingBoundary), 0.0, Q3(), False)
+    area = s.mass
+    assert np.mean(1.0 / c.pdf) == pytest.approx(area, rel=1e-6)
+    assert area == pytest.approx(4 * np.pi, rel=2e-2)
+    d = bvc.UniformDomainSampler(lambda x: np.linalg.norm(x, axis=1) < 1.0, [-1, -1], [1, 1], np.pi, seed=5)
+    dc = d.generate_samples(10000, _BoxQueries())
+    assert len(dc) == pytest.approx(10000, rel=0.03)
+    assert np.all(np.linalg.norm(dc.pt, axis=1) < 1.0)
+    assert np.allclose(dc.pdf, 1.0 / np.pi)
+    assert np.all(dc.type == int(SampleType.InDomain))
+
+
+# ------------------------------------------------------------------------------ GPU
+def _random_cache(dim, n, rng, kinds):
+    pt = rng.uniform(-1, 1, (n, dim)).astype(np.float32)
+    nrm = rng.normal(size=(n, dim)).astype(np.float32)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    types = rng.choice(kinds, n).astype(np.int32)
+    return dict(pt=pt, normal=nrm, pdf=rng.uniform(0.2, 2.0, n).astype(np.float32), type=types,
+                estimate_normal_aligned=(rng.random(n) < 0.3).astype(np.int32),
+                solution=rng.normal(size=n).astype(np.float32), normal_derivative=rng.normal(size=n).astype(np.float32),
+                contribution=rng.normal(size=n).astype(np.float32),
+                robin_coeff=np.where(rng.random(n) < 0.4, rng.uniform(0.5, 4.0, n), 0.0).astype(np.float32))
+
+
+def _evals(dim, m, rng):
+    return dict(pt=rng.uniform(-1.2, 1.2, (m, dim)).astype(np.float32),
+                type=rng.choice([0, 0, 0, 1, 2], m).astype(np.int32),
+                dist_to_absorbing=rng.uniform(0.0, 0.5, m).astype(np.float32),
+                dist_to_reflecting=rng.uniform(0.0, 0.5, m).astype(np.float32),
+                mean=np.zeros((m, 5)), m2=np.zeros((m, 5)), count=np.zeros((m, 5), np.int32),
+                gradient_mean=np.zeros((m, 5, dim)), gradient_m2=np.zeros((m, 5, dim)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,sigma,reg", [(2, 0.0, 0.0), (2, 1.5, 0.05), (3, 0.0, 0.02), (3, 2.0, 0.0)])
+def test_splat_matches_oracle(zgpu, oracle, dim, sigma, reg):
+    """zgpu_bvc_splat against the oracle's BoundaryValueCaching::splat on a synthetic cache of
+    absorbing, reflecting (Robin, pure Neumann, normal-aligned) and source samples: the same
+    counts, means within FP32 rounding, merged into statistics the points already held."""
+    import ctypes as C
+    from zombie_gb300 import api, bvc
+    from zombie_gb300._lib import check, lib
+    rng = np.random.default_rng(dim * 10 + int(sigma))
+    cache = _random_cache(dim, 3000, rng, [1, 2, 0])
+    ev = _evals(dim, 700, rng)
+    pde = P.make_pde(P.solution_expcos(0.0), sigma=sigma)
+    kw = dict(radius_clamp=1e-3, kernel_regularization=reg, robin_coeff_cutoff=2.0, cutoff_absorbing=0.05,
+              cutoff_reflecting=0.02)
+    # two splats (a first cache, then a second one merged in)
+    halves = [{k: np.ascontiguousarray(v[:1200]) for k, v in cache.items()},
+              {k: np.ascontiguousarray(v[1200:]) for k, v in cache.items()}]
+    og = {k: v.copy() for k, v in ev.items()}
+    for h in halves:
+        oracle.bvc_splat(dim, sigma, h, og, **kw)
+    gg = {k: v.copy() for k, v in ev.items()}
+    ctx = api.default_context()
+    for h in halves:
+        s = A.BvcSamplesC()
+        s.n = h["pt"].shape[0]
+        for k, v in h.items():
+            setattr(s, k, A.ptr(v))
+        e = A.BvcEvalPointsC()
+        e.n = gg["pt"].shape[0]
+        for k, v in gg.items():
+            setattr(e, k, A.ptr(v))
+        check(lib().zgpu_bvc_splat(ctx.h, dim, C.byref(pde), C.byref(s), kw["radius_clamp"], reg,
+                                   kw["robin_coeff_cutoff"], kw["cutoff_absorbing"], kw["cutoff_reflecting"],
+                                   C.byref(e), A.ZGPU_MEM_HOST))
+    assert np.array_equal(gg["count"], og["count"])
+    assert np.any(og["count"] > 0) and np.any(og["count"] == 0)
+    scale = np.abs(og["mean"]).max()
+    assert np.max(np.abs(gg["mean"] - og["mean"])) <= 2e-5 * scale
+    sd = np.sqrt(np.maximum(og["m2"], 0))
+    assert np.max(np.abs(np.sqrt(np.maximum(gg["m2"], 0)) - sd)) <= 1e-3 * sd.max()
+    gs = np.abs(og["gradient_mean"]).max()
+    assert np.max(np.abs(gg["gradient_mean"] - og["gradient_mean"])) <= 2e-5 * gs
+    # points on the boundary (alpha = 2) splat no gradient
+    on = (ev["type"] != 0)
+    assert np.all(gg["gradient_mean"][on] == 0.0)
+
+
+@pytest.mark.gpu
+def test_pde_evaluate_matches_oracle(zgpu, oracle):
+    from zombie_gb300 import api
+    pr = P.mixed_wost_2d(n_segments=256, grid=8, spp=4, sigma=1.0)
+    P.with_grid_fields(pr, ("dirichlet",), shape=(64, 64))
+    pr.pde.robin_coeff_kind = A.ZGPU_FIELD_CONSTANT
+    pr.pde.robin_coeff_value, pr.pde.robin_coeff_value_aligned = 1.5, 0.5
+    pr.pde.are_robin_conditions_pure_neumann = 0
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, (2000, 2)).astype(np.float32)
+    n = rng.normal(size=(2000, 2)).astype(np.float32)
+    for aligned in (0, 1):
+        g = api.pde_evaluate(pr.pde, x, n, aligned, dim=2)
+        o = oracle.eval_pde(2, pr.pde, x, n, aligned=bool(aligned), with_robin_coeff=True)
+        for a, b in zip(g, o):
+            assert np.allclose(a, b, rtol=2e-5, atol=2e-5)
+
+
+def _laplace_bvc(spp_grad, cache, fd=False, seed=7):
+    from zombie_gb300 import api, bvc
+    from zombie_gb300.runner import GpuProblem
+    pr = P.laplace_wos_2d(n_segments=1024, grid=24, spp=4)
+    gp = GpuProblem(pr)
+    pos, idx = pr.absorbing
+    inside = lambda x: gp.queries.inside_domain(x)
+    s = bvc.UniformLineSegmentBoundarySampler(pos, idx, inside, seed=seed)
+    s.initialize(1e-3, False)
+    solver = bvc.BoundaryValueCachingSolver(gp.queries, s, None, None)
+    solver.generate_samples(cache, 0, 0, 1e-3, 1e-3, False)
+    settings = api.WalkSettings(1e-3, 1e-3, 1024, False)
+    solver.compute_sample_estimates(gp.pde, settings, spp_grad, spp_grad, float("inf"), use_finite_differences=fd)
+    ev = bvc.EvaluationPoints(pr.points, dist_to_absorbing=gp.dist, dim=2)
+    solver.splat(gp.pde, 1e-3, 0.0, float("inf"), 0.05, 0.0, ev)
+    return pr, gp, solver, ev
+
+
+@pytest.mark.gpu
+def test_bvc_laplace_2d_matches_the_exact_solution(zgpu):
+    """2D Laplace on the star polygon: boundary samples estimate u and du/dn with Walk on Stars
+    (gradient estimator along the normal), splats recover u inside; the cached normal
+    derivatives agree with grad u . n."""
+    pr, gp, solver, ev = _laplace_bvc(256, 8192)
+    c = solver.get_absorbing_boundary_cache()
+    _, grad, _ = P.eval_analytic(pr.solution, c.pt)
+    dn_exact = np.sum(grad * c.normal, axis=1)
+    err = c.normal_derivative - dn_exact
+    u_exact = pr.exact(c.pt)
+    far = gp.dist >= 0.05
+    est = ev.get_estimated_solution()
+    ex = pr.exact()
+    rmse = np.sqrt(np.mean((est[far] - ex[far]) ** 2))
+    info = dict(dn_bias=err.mean(), dn_bias_se=err.std() / np.sqrt(len(err)), dn_rms=np.sqrt(np.mean(err ** 2)),
+                u_rms=np.sqrt(np.mean((c.solution - u_exact) ** 2)), splat_rmse=rmse, u_std=np.std(ex[far]),
+                corr=np.corrcoef(est[far], ex[far])[0, 1], n=len(c))
+    # the per-sample normal derivatives are noisy (first ball ~ the 1e-3 offset) but unbiased
+    assert abs(info["dn_bias"]) < 4 * info["dn_bias_se"] + 1e-3, info
+    assert info["u_rms"] < 0.05, info
+    assert np.all(ev.count[~far] == 0)
+    assert rmse < 0.1 * info["u_std"] + 0.02, info
+    assert info["corr"] > 0.99, info
+
+
+@pytest.mark.gpu
+def test_bvc_finite_differences_and_near_boundary_estimates(zgpu):
+    from zombie_gb300 import api
+    pr, gp, solver, ev = _laplace_bvc(128, 4096, fd=True)
+    c = solver.get_absorbing_boundary_cache()
+    assert np.all(c.type == int(SampleType.OnAbsorbingBoundary))
+    far = gp.dist >= 0.05
+    est, ex = ev.get_estimated_solution(), pr.exact()
+    corr = np.corrcoef(est[far], ex[far])[0, 1]
+    assert corr > 0.98, (corr, np.sqrt(np.mean((est[far] - ex[far]) ** 2)))
+    # points inside the cutoff get a plain walk estimate in their source statistic
+    settings = api.WalkSettings(1e-3, 1e-3, 1024, False)
+    solver.estimate_solution_near_boundary(gp.pde, settings, 0.05, 0.0, 256, ev)
+    near = ~far
+    assert np.all(ev.count[near, A.ZGPU_BVC_SOURCE] == 1)
+    assert np.sqrt(np.mean((ev.get_estimated_solution()[near] - ex[near]) ** 2)) < 0.1

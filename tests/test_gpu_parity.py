@@ -446,6 +446,30 @@ def test_batched_solve_equals_individual_solves(zgpu):
     assert np.mean(np.abs(err) <= 4 * se + 1e-6) > 0.99
 
 
+def test_batched_3d_solve_equals_individual_solves(zgpu):
+    """3D problems of one solver batched (different meshes, absorption and sources): each
+    point runs the walks of its problem solved alone."""
+    from zombie_gb300.runner import GpuBatch
+    scenes = [P.screened_wos_3d(level=3, n_points=150, spp=64, sigma=4.0, seed=1),
+              P.screened_wos_3d(level=4, n_points=200, spp=32, sigma=1.0, seed=2),
+              P.laplace_wos_2d(n_segments=64, grid=4, spp=4)]
+    with pytest.raises(ValueError):
+        GpuBatch(scenes)                                  # one dimension per batch
+    scenes = scenes[:2] + [P.screened_wos_3d(level=3, n_points=100, spp=16, sigma=0.0, seed=3)]
+    batch = GpuBatch(scenes)
+    arr = batch.device_arrays()
+    rep = batch.solve(arr)
+    assert rep.error_word == 0
+    for k, g in enumerate(batch.problems):
+        d = g.device_arrays()
+        g.solve(d)
+        lo, hi = batch.offsets[k], batch.offsets[k + 1]
+        for key in ("n_solution_estimates", "total_walk_length"):
+            assert np.array_equal(d[key].cpu().numpy(), arr[key][lo:hi].cpu().numpy()), (k, key)
+        for key in ("solution_mean", "solution_m2"):
+            assert np.allclose(d[key].cpu().numpy(), arr[key][lo:hi].cpu().numpy(), rtol=1e-9, atol=1e-12), (k, key)
+
+
 def test_batched_solve_rejects_scene_ids_outside_the_table(zgpu):
     import ctypes as C
     from zombie_gb300 import _lib

@@ -210,3 +210,37 @@ class CacheConfig(C.Structure):
         ("epsilon", C.c_float),
         ("seed", C.c_uint64),
     ]
+
+
+ZGPU_BVC_ABSORBING, ZGPU_BVC_ABSORBING_ALIGNED, ZGPU_BVC_REFLECTING, ZGPU_BVC_REFLECTING_ALIGNED, ZGPU_BVC_SOURCE = range(5)
+ZGPU_BVC_GROUPS = 5
+
+
+class BvcSamplesC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("pt", C.c_void_p),
+        ("normal", C.c_void_p),
+        ("pdf", C.c_void_p),
+        ("type", C.c_void_p),
+        ("estimate_normal_aligned", C.c_void_p),
+        ("solution", C.c_void_p),
+        ("normal_derivative", C.c_void_p),
+        ("contribution", C.c_void_p),
+        ("robin_coeff", C.c_void_p),
+    ]
+
+
+class BvcEvalPointsC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("pt", C.c_void_p),
+        ("type", C.c_void_p),
+        ("dist_to_absorbing", C.c_void_p),
+        ("dist_to_reflecting", C.c_void_p),
+        ("mean", C.c_void_p),
+        ("m2", C.c_void_p),
+        ("count", C.c_void_p),
+        ("gradient_mean", C.c_void_p),
+        ("gradient_m2", C.c_void_p),
+    ]

@@ -363,6 +363,24 @@ class PDE:
         return pde
 
 
+def pde_evaluate(pde, x, normals=None, aligned=None, dim=None, context=None):
+    """The PDE's fields at points x as the walk kernels read them (zgpu_pde_evaluate):
+    returns (source, dirichlet, robin, robin_coeff) as float32 arrays."""
+    ctx = context or default_context()
+    p = pde.to_c() if isinstance(pde, PDE) else pde
+    dim = dim or (pde.dim if isinstance(pde, PDE) else None)
+    x = np.ascontiguousarray(x, np.float32)
+    dim = dim or x.shape[-1]
+    x = x.reshape(-1, dim)
+    n = x.shape[0]
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, dim)
+    al = None if aligned is None else np.ascontiguousarray(np.broadcast_to(np.asarray(aligned, np.int32), (n,)))
+    out = [np.zeros(n, np.float32) for _ in range(4)]
+    check(lib().zgpu_pde_evaluate(ctx.h, dim, C.byref(p), n, A.ptr(x), A.ptr(nrm), A.ptr(al), A.ZGPU_MEM_HOST,
+                                  *[A.ptr(o) for o in out]))
+    return tuple(out)
+
+
 # ---------------------------------------------------------------------- settings
 class WalkSettings:
     """WalkSettings (point_estimation/common.h:19-91): both constructors, same defaults."""

@@ -68,7 +68,8 @@ struct zgpu_context {
            kWalkStart, kFlags, kNPrev, kAccSum, kAccSq, kAccN, kAccLen, kAccSplits, kBlockSums, kCounters,
            kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId,
            kDistRefl, kGMean, kGM2, kGN, kAccGrad, kAccGradSq, kAccGradN, kDirDeriv, kFirstSrc, kDeriv, kAccFirstSrc,
-           kAccDeriv, kNumBufs };
+           kAccDeriv, kB0, kB1, kB2, kB3, kB4, kB5, kB6, kB7, kB8, kB9, kB10, kB11, kB12, kB13, kB14, kB15, kB16, kB17,
+           kB18, kB19, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
     // use_graph: the captured prepare/scan/walk/finalize sequence, replayed while the solve's
@@ -697,7 +698,6 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3, got %d", D);
     if (nScenes < 1) return fail(ZGPU_ERR_INVALID_ARG, "n_scenes must be >= 1");
     const bool batched = nScenes > 1 || (pts->scene_id != nullptr);
-    if (batched && D != 2) return fail(ZGPU_ERR_UNSUPPORTED, "batched many-solve is built for 2D scenes");
     if (batched && cache) return fail(ZGPU_ERR_UNSUPPORTED, "the neural cache serves single-scene solves");
     if (batched && pts->n > 0 && !pts->scene_id) return fail(ZGPU_ERR_INVALID_ARG, "scene_id is required with n_scenes > 1");
     for (int k = 0; k < nScenes; k++) ZG_TRY(checkScene(q + k, pde + k, ws + k, D));
@@ -1041,3 +1041,118 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes, const zgpu_g
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ PDE fields, BVC
+int zgpu_pde_evaluate(zgpu_context* ctx, int dim, const zgpu_pde* pde, int64_t n, const float* x, const float* normal,
+                      const int32_t* aligned, int memory, float* out_source, float* out_dirichlet, float* out_robin,
+                      float* out_robin_coeff) {
+    if (!ctx || !pde) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
+    if (n < 0 || (n > 0 && !x)) return fail(ZGPU_ERR_INVALID_ARG, "points");
+    if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    ZG_TRY(zg::checkPdeFields(pde, dim, true));
+    if (n == 0) return ZGPU_OK;
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    using C = zgpu_context;
+    zgpu_pde dp = *pde;
+    ZG_TRY(stageGrids(ctx, dp, dim, 0));
+    const float *dx, *dn;
+    const int* da;
+    ZG_TRY(stageIn<float>(ctx, C::kB0, x, (size_t)n * dim, memory, &dx));
+    ZG_TRY(stageIn<float>(ctx, C::kB1, normal, (size_t)n * dim, memory, &dn));
+    ZG_TRY(stageIn<int>(ctx, C::kB2, aligned, (size_t)n, memory, &da));
+    float* outs[4] = {out_source, out_dirichlet, out_robin, out_robin_coeff};
+    float* dOut[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 4; k++) {
+        if (!outs[k]) continue;
+        if (memory == ZGPU_MEM_DEVICE) dOut[k] = outs[k];
+        else ZG_TRY(scratch<float>(ctx, C::kB3 + k, (size_t)n, &dOut[k]));
+    }
+    ZG_CUDA(launchPdeEvaluate(dim, dp, n, dx, dn, da, dOut[0], dOut[1], dOut[2], dOut[3], ctx->stream));
+    for (int k = 0; k < 4; k++)
+        if (outs[k] && memory == ZGPU_MEM_HOST)
+            ZG_CUDA(cudaMemcpyAsync(outs[k], dOut[k], sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    ZG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ZGPU_OK;
+}
+
+int zgpu_bvc_splat(zgpu_context* ctx, int dim, const zgpu_pde* pde, const zgpu_bvc_samples* samples, float radius_clamp,
+                   float kernel_regularization, float robin_coeff_cutoff_for_normal_derivative,
+                   float cutoff_dist_to_absorbing_boundary, float cutoff_dist_to_reflecting_boundary,
+                   zgpu_bvc_eval_points* ev, int memory) {
+    if (!ctx || !pde || !samples || !ev) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
+    if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    if (samples->n < 0 || ev->n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative sizes");
+    if (samples->n > 0 && (!samples->pt || !samples->normal || !samples->pdf || !samples->type || !samples->solution ||
+                           !samples->normal_derivative || !samples->contribution))
+        return fail(ZGPU_ERR_INVALID_ARG, "sample arrays pt, normal, pdf, type, solution, normal_derivative and "
+                                          "contribution are required");
+    if (ev->n > 0 && (!ev->pt || !ev->dist_to_absorbing || !ev->mean || !ev->m2 || !ev->count || !ev->gradient_mean))
+        return fail(ZGPU_ERR_INVALID_ARG, "evaluation arrays pt, dist_to_absorbing, mean, m2, count and gradient_mean "
+                                          "are required");
+    if (!(pde->absorption_coeff >= 0.0f)) return fail(ZGPU_ERR_INVALID_ARG, "absorption coefficient must be >= 0");
+    if (samples->n == 0 || ev->n == 0) return ZGPU_OK;
+    if (samples->n >= ((int64_t)1 << 40) || ev->n >= ((int64_t)1 << 40)) return fail(ZGPU_ERR_INVALID_ARG, "too many points");
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    using C = zgpu_context;
+    const int64_t ns = samples->n, ne = ev->n;
+    BvcSplatParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.nSamples = ns;
+    ZG_TRY(stageIn<float>(ctx, C::kB0, samples->pt, (size_t)ns * dim, memory, &p.pt));
+    ZG_TRY(stageIn<float>(ctx, C::kB1, samples->normal, (size_t)ns * dim, memory, &p.normal));
+    ZG_TRY(stageIn<float>(ctx, C::kB2, samples->pdf, (size_t)ns, memory, &p.pdf));
+    ZG_TRY(stageIn<int>(ctx, C::kB3, samples->type, (size_t)ns, memory, &p.type));
+    ZG_TRY(stageIn<int>(ctx, C::kB4, samples->estimate_normal_aligned, (size_t)ns, memory, &p.aligned));
+    ZG_TRY(stageIn<float>(ctx, C::kB5, samples->solution, (size_t)ns, memory, &p.solution));
+    ZG_TRY(stageIn<float>(ctx, C::kB6, samples->normal_derivative, (size_t)ns, memory, &p.normalDerivative));
+    ZG_TRY(stageIn<float>(ctx, C::kB7, samples->contribution, (size_t)ns, memory, &p.contribution));
+    ZG_TRY(stageIn<float>(ctx, C::kB8, samples->robin_coeff, (size_t)ns, memory, &p.robinCoeff));
+    p.nEval = ne;
+    ZG_TRY(stageIn<float>(ctx, C::kB9, ev->pt, (size_t)ne * dim, memory, &p.evalPt));
+    ZG_TRY(stageIn<int>(ctx, C::kB10, ev->type, (size_t)ne, memory, &p.evalType));
+    ZG_TRY(stageIn<float>(ctx, C::kB11, ev->dist_to_absorbing, (size_t)ne, memory, &p.evalDistA));
+    ZG_TRY(stageIn<float>(ctx, C::kB12, ev->dist_to_reflecting, (size_t)ne, memory, &p.evalDistR));
+    const size_t ng = (size_t)ne * ZGPU_BVC_GROUPS;
+    ZG_TRY(stageInOut<double>(ctx, C::kB13, ev->mean, ng, memory, &p.mean));
+    ZG_TRY(stageInOut<double>(ctx, C::kB14, ev->m2, ng, memory, &p.m2));
+    ZG_TRY(stageInOut<int>(ctx, C::kB15, ev->count, ng, memory, &p.count));
+    ZG_TRY(stageInOut<double>(ctx, C::kB16, ev->gradient_mean, ng * dim, memory, &p.gradMean));
+    if (ev->gradient_m2) ZG_TRY(stageInOut<double>(ctx, C::kB17, ev->gradient_m2, ng * dim, memory, &p.gradM2));
+    p.sqrtLambda = std::sqrt(pde->absorption_coeff);
+    p.radiusClamp = radius_clamp;
+    p.regularization = kernel_regularization;
+    p.robinCutoff = robin_coeff_cutoff_for_normal_derivative;
+    p.cutoffA = cutoff_dist_to_absorbing_boundary;
+    p.cutoffR = cutoff_dist_to_reflecting_boundary;
+    // the statistic groups present in the cache: one launch each
+    std::vector<int32_t> ht((size_t)ns), ha;
+    if (memory == ZGPU_MEM_HOST) std::memcpy(ht.data(), samples->type, sizeof(int32_t) * ns);
+    else ZG_CUDA(cudaMemcpy(ht.data(), samples->type, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost));
+    if (samples->estimate_normal_aligned) {
+        ha.resize((size_t)ns);
+        if (memory == ZGPU_MEM_HOST) std::memcpy(ha.data(), samples->estimate_normal_aligned, sizeof(int32_t) * ns);
+        else ZG_CUDA(cudaMemcpy(ha.data(), samples->estimate_normal_aligned, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost));
+    }
+    bool present[ZGPU_BVC_GROUPS] = {false, false, false, false, false};
+    for (int64_t j = 0; j < ns; j++) {
+        const int t = ht[j], al = ha.empty() ? 0 : ha[j];
+        const int g = t == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY ? (al ? ZGPU_BVC_ABSORBING_ALIGNED : ZGPU_BVC_ABSORBING)
+                    : t == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY ? (al ? ZGPU_BVC_REFLECTING_ALIGNED : ZGPU_BVC_REFLECTING)
+                    : ZGPU_BVC_SOURCE;
+        present[g] = true;
+    }
+    for (int g = 0; g < ZGPU_BVC_GROUPS; g++) {
+        if (!present[g]) continue;
+        p.group = g;
+        ZG_CUDA(launchBvcSplat(dim, pde->absorption_coeff > 0.0f, p, ctx->stream));
+    }
+    ZG_TRY(stageOut<double>(ctx, p.mean, ev->mean, ng, memory));
+    ZG_TRY(stageOut<double>(ctx, p.m2, ev->m2, ng, memory));
+    ZG_TRY(stageOut<int>(ctx, p.count, ev->count, ng, memory));
+    ZG_TRY(stageOut<double>(ctx, p.gradMean, ev->gradient_mean, ng * dim, memory));
+    if (ev->gradient_m2) ZG_TRY(stageOut<double>(ctx, p.gradM2, ev->gradient_m2, ng * dim, memory));
+    ZG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ZGPU_OK;
+}

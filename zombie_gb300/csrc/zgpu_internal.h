@@ -134,6 +134,36 @@ struct DeviceBuilt {
 cudaError_t buildBoundaryOnDevice(int D, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
                                   const float* kmax, bool doubleSided, float prec, cudaStream_t s, DeviceBuilt& out);
 
+// Boundary Value Caching splat (zgpu_bvc.cu): device arrays of one cache and of the
+// evaluation points, one statistic group per launch
+struct BvcSplatParams {
+    int64_t nSamples;
+    const float* pt;
+    const float* normal;
+    const float* pdf;
+    const int* type;
+    const int* aligned;
+    const float* solution;
+    const float* normalDerivative;
+    const float* contribution;
+    const float* robinCoeff;
+    int64_t nEval;
+    const float* evalPt;
+    const int* evalType;
+    const float* evalDistA;
+    const float* evalDistR;
+    double* mean;
+    double* m2;
+    int* count;
+    double* gradMean;
+    double* gradM2;
+    float sqrtLambda, radiusClamp, regularization, robinCutoff, cutoffA, cutoffR;
+    int group;
+};
+cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, cudaStream_t s);
+cudaError_t launchPdeEvaluate(int D, const zgpu_pde& pde, int64_t n, const float* x, const float* nrm, const int* aligned,
+                              float* src, float* dir, float* rob, float* kap, cudaStream_t s);
+
 // accessors into the C ABI objects (zgpu_api.cu)
 void setLastError(const char* msg);
 bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind);

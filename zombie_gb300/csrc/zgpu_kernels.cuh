@@ -732,9 +732,11 @@ __global__ void __launch_bounds__(kQueryThreads) prepareKernel(const __grid_cons
     if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && ws.solve_double_sided && type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && aligned)
         flags |= kPointFlip;
     if (badScene) atomicOr(P.errorWord, kErrBadInput);
-    if (eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT && type == ZGPU_SAMPLE_IN_DOMAIN && !badScene && P.accGrad) {
-        // estimateSolutionAndGradient (walk_on_spheres.h:422-430, walk_on_stars.h:670-684):
-        // first ball 0.99 x the distance to the boundary; antithetic pairs halve the draws
+    if (eq == ZGPU_ESTIMATE_SOLUTION_AND_GRADIENT && !badScene && P.accGrad) {
+        // estimateSolutionAndGradient (walk_on_spheres.h:422-430, walk_on_stars.h:670-684),
+        // whatever the point's type (boundary value caching estimates normal derivatives at
+        // boundary samples offset into the domain): first ball 0.99 x the distance to the
+        // boundary; antithetic pairs halve the draws
         float dB = dAbs;
         if (P.solver == ZGPU_SOLVER_WALK_ON_STARS && sc.hasRefl) {
             float dR;
@@ -980,17 +982,13 @@ inline size_t walkSmemBytes(const SolveParams& p, int threads) {
 // walk kernel launchers, explicitly instantiated per (dimension, solver) in zgpu_walk_<D>d_<solver>.cu
 template <int D, int SOLVER>
 struct WalkLaunch {
-    // the walk kernel for a solve: screened or not, batched (2D scene tables) or one scene,
+    // the walk kernel for a solve: screened or not, batched (a scene table) or one scene,
     // warp-cooperative queries or one lane per query; nullptr for a combination not built
     static const void* kernel(bool screened, bool batched, bool coop) {
         if (batched) {
-            if constexpr (D == 2) {
-                if (coop) return nullptr;
-                return screened ? (const void*)detail::walkKernel<D, SOLVER, true, true, false>
-                                : (const void*)detail::walkKernel<D, SOLVER, false, true, false>;
-            } else {
-                return nullptr;
-            }
+            if (coop) return nullptr;
+            return screened ? (const void*)detail::walkKernel<D, SOLVER, true, true, false>
+                            : (const void*)detail::walkKernel<D, SOLVER, false, true, false>;
         }
         if (coop) return screened ? (const void*)detail::walkKernel<D, SOLVER, true, false, true>
                                   : (const void*)detail::walkKernel<D, SOLVER, false, false, true>;

@@ -89,8 +89,8 @@ class GpuBatch:
         self.ctx = context or default_context()
         self.problems = [GpuProblem(p, context=self.ctx, seed_base=seed_base) for p in problems]
         self.solver_id = problems[0].solver
-        if any(p.solver != self.solver_id for p in problems) or any(p.dim != 2 for p in problems):
-            raise ValueError("a batch holds 2D problems of one solver")
+        if any(p.solver != self.solver_id for p in problems) or any(p.dim != problems[0].dim for p in problems):
+            raise ValueError("a batch holds problems of one dimension and one solver")
         self.options = options
         n = len(self.problems)
         self.q = (A.GeometricQueriesC * n)(*[g.queries.to_c() for g in self.problems])
