@@ -50,6 +50,9 @@ WORKLOADS = {
     "cache_kernels": dict(fn=None, kw={}, desc="neural cache kernels: fused training step (encode + 32-64-64-1 "
                           "MLP forward/backward + table scatter + Adam) on 2^18-point batches and inference on "
                           "2^20 points, 3D, 16 levels x 2^19 entries"),
+    "bvc_laplace_2d": dict(fn=None, kw={}, desc="boundary value caching, 2D Laplace on a 4096-segment star "
+                           "polygon: 65,536 boundary samples x 256 gradient walks, splat onto a 256x256 grid "
+                           "(points at least 0.05 from the boundary)"),
     "screened_wos_3d_small": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=16384, spp=4),
                                   desc="profiling case: 3D screened WoS sigma=4, icosphere L8, 16384 points, 4 spp"),
 }
@@ -316,6 +319,83 @@ def run_cache_kernels(args):
                                  "scatter bound these kernels, not the tensor pipe"},
             "clocks": clk.summary(), "gpu_launches": 2 * args.steps + args.steps}
     print(json.dumps(line), flush=True)
+
+
+def run_bvc(args):
+    """Boundary value caching end to end: boundary estimates (Walk on Stars with the gradient
+    estimator) and the all-pairs splat, on the GPU; the splat throughput against the oracle's
+    CPU splat on a bounded sample of the evaluation points."""
+    import torch
+    from zombie_gb300 import api, bvc
+    from zombie_gb300.runner import GpuProblem
+    pr = P_mod().laplace_wos_2d(n_segments=4096, grid=256, spp=4)
+    gp = GpuProblem(pr)
+    ctx = gp.ctx
+    pos, idx = pr.absorbing
+    cache_size, walks = 65536, 256
+    settings = api.WalkSettings(1e-3, 1e-3, 1024, False)
+    ev_far = gp.dist >= 0.05
+
+    def one(seed):
+        s = bvc.UniformLineSegmentBoundarySampler(pos, idx, gp.queries.inside_domain, seed=seed)
+        s.initialize(1e-3, False)
+        solver = bvc.BoundaryValueCachingSolver(gp.queries, s, None, None, context=ctx)
+        solver.generate_samples(cache_size, 0, 0, 1e-3, 1e-3, False)
+        ev = bvc.EvaluationPoints(pr.points, dist_to_absorbing=gp.dist, dim=2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.compute_sample_estimates(gp.pde, settings, walks, walks, float("inf"))
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        solver.splat(gp.pde, 1e-3, 0.0, float("inf"), 0.05, 0.0, ev)
+        ctx.synchronize()
+        t2 = time.perf_counter()
+        return solver, ev, t1 - t0, t2 - t1
+    for w in range(max(args.warmup, 1)):
+        one(100 + w)
+    est_s, splat_s, errs = [], [], []
+    with ClockSampler(0) as clk:
+        for k in range(args.steps):
+            solver, ev, te, ts = one(200 + k)
+            est_s.append(te)
+            splat_s.append(ts)
+            e = ev.get_estimated_solution()[ev_far] - pr.exact()[ev_far]
+            errs.append(float(np.sqrt(np.mean(e ** 2))))
+    n_cache = len(solver.get_absorbing_boundary_cache())
+    n_eval = int(ev_far.sum())
+    pairs = n_cache * n_eval
+    splat_ms = 1e3 * float(np.median(splat_s))
+    line = {"metric": "splat pairs/s", "value": pairs / (splat_ms / 1e3), "unit": "pairs/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(np.add(est_s, splat_s))),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 moments)",
+            "data": "synthetic",
+            "config": {"workload": "bvc_laplace_2d", "cache_samples": n_cache, "evaluation_points": n_eval,
+                       "walks_per_sample": walks, "description": WORKLOADS["bvc_laplace_2d"]["desc"]},
+            "boundary_estimates_ms": 1e3 * float(np.median(est_s)), "splat_ms": splat_ms,
+            "rmse_vs_exact": float(np.median(errs)), "u_std": float(np.std(pr.exact()[ev_far])),
+            "clocks": clk.summary(), "gpu_launches": "1 splat launch + 4 walk launches per step"}
+    if not args.skip_cpu:
+        from oracle import oracle as O
+        c = solver.get_absorbing_boundary_cache()
+        cache = {k: getattr(c, k) for k in ("pt", "normal", "pdf", "type", "estimate_normal_aligned", "solution",
+                                            "normal_derivative", "contribution", "robin_coeff")}
+        m = 2048
+        pts = np.ascontiguousarray(pr.points[ev_far][:m])
+        e = dict(pt=pts, type=np.zeros(m, np.int32), dist_to_absorbing=np.ones(m, np.float32),
+                 dist_to_reflecting=np.ones(m, np.float32), mean=np.zeros((m, 5)), m2=np.zeros((m, 5)),
+                 count=np.zeros((m, 5), np.int32), gradient_mean=np.zeros((m, 5, 2)), gradient_m2=np.zeros((m, 5, 2)))
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.bvc_splat(2, 0.0, cache, e, radius_clamp=1e-3, n_threads=threads)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_cache * m / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                "sample": f"{m} of {n_eval} evaluation points x {n_cache} samples in {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
+def P_mod():
+    from zombie_gb300 import problems
+    return problems
 
 
 def run_reference(args):
@@ -617,6 +697,8 @@ def main():
         run_batched(args)
     elif args.workload == "cache_kernels":
         run_cache_kernels(args)
+    elif args.workload == "bvc_laplace_2d":
+        run_bvc(args)
     else:
         run_gpu(args)
 

@@ -126,9 +126,10 @@ def test_splat_matches_oracle(zgpu, oracle, dim, sigma, reg):
     pde = P.make_pde(P.solution_expcos(0.0), sigma=sigma)
     kw = dict(radius_clamp=1e-3, kernel_regularization=reg, robin_coeff_cutoff=2.0, cutoff_absorbing=0.05,
               cutoff_reflecting=0.02)
-    # two splats (a first cache, then a second one merged in)
-    halves = [{k: np.ascontiguousarray(v[:1200]) for k, v in cache.items()},
-              {k: np.ascontiguousarray(v[1200:]) for k, v in cache.items()}]
+    # three splats merged into the same points: a small cache (one block row) and two larger
+    # ones whose samples the kernel splits across blocks and merges
+    cuts = [0, 300, 1500, 3000]
+    halves = [{k: np.ascontiguousarray(v[a:b]) for k, v in cache.items()} for a, b in zip(cuts[:-1], cuts[1:])]
     og = {k: v.copy() for k, v in ev.items()}
     for h in halves:
         oracle.bvc_splat(dim, sigma, h, og, **kw)

@@ -1143,10 +1143,12 @@ int zgpu_bvc_splat(zgpu_context* ctx, int dim, const zgpu_pde* pde, const zgpu_b
                     : ZGPU_BVC_SOURCE;
         present[g] = true;
     }
+    const int splits = bvcSplitCount(ne, ns, ctx->numSMs);
+    if (splits > 1) ZG_TRY(scratch<double>(ctx, C::kB18, (size_t)splits * ne * (3 + 2 * dim), &p.partial));
     for (int g = 0; g < ZGPU_BVC_GROUPS; g++) {
         if (!present[g]) continue;
         p.group = g;
-        ZG_CUDA(launchBvcSplat(dim, pde->absorption_coeff > 0.0f, p, ctx->stream));
+        ZG_CUDA(launchBvcSplat(dim, pde->absorption_coeff > 0.0f, p, splits, ctx->stream));
     }
     ZG_TRY(stageOut<double>(ctx, p.mean, ev->mean, ng, memory));
     ZG_TRY(stageOut<double>(ctx, p.m2, ev->m2, ng, memory));

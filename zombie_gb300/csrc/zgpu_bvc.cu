@@ -102,11 +102,15 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
 #pragma unroll
     for (int d = 0; d < D; d++) { kG[d] = 0.0f; accG[d] = 0.0; accGQ[d] = 0.0; }
     long long count = 0;
-    for (int64_t base = 0; base < P.nSamples; base += kTile) {
+    // this block's share of the cache (split along grid.y when the evaluation points alone
+    // cannot fill the GPU)
+    const int64_t begin = (int64_t)blockIdx.y * P.splitChunk;
+    const int64_t end = min(P.nSamples, begin + P.splitChunk);
+    for (int64_t base = begin; base < end; base += kTile) {
         const int64_t j = base + threadIdx.x;
         if (threadIdx.x < kTile) {
             int grp = -1;
-            if (j < P.nSamples) {
+            if (j < end) {
                 const int al = P.aligned ? P.aligned[j] : 0;
                 grp = groupOf(P.type[j], al);
                 const float sgn = (grp != ZGPU_BVC_SOURCE && al) ? -1.0f : 1.0f;
@@ -125,7 +129,7 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
         }
         __syncthreads();
         if (active) {
-            const int m = P.nSamples - base < kTile ? (int)(P.nSamples - base) : kTile;
+            const int m = end - base < kTile ? (int)(end - base) : kTile;
             float s = 0.0f, q = 0.0f, gs[D], gq[D];
 #pragma unroll
             for (int d = 0; d < D; d++) { gs[d] = 0.0f; gq[d] = 0.0f; }
@@ -193,12 +197,24 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
         }
         __syncthreads();
     }
+    if (i >= P.nEval) return;
+    const double n2 = (double)count;
+    const double mean2 = count ? kS + accS / n2 : 0.0;
+    const double m22 = count ? fmax(0.0, accQ - accS * accS / n2) : 0.0;
+    if (P.partial) {
+        // split cache: this block's moments for the merge kernel (count 0 included)
+        double* out = P.partial + ((size_t)blockIdx.y * P.nEval + i) * (3 + 2 * D);
+        out[0] = n2; out[1] = mean2; out[2] = m22;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            out[3 + d] = count ? kG[d] + accG[d] / n2 : 0.0;
+            out[3 + D + d] = count ? fmax(0.0, accGQ[d] - accG[d] * accG[d] / n2) : 0.0;
+        }
+        return;
+    }
     if (!active || count == 0) return;
     // moments of this launch, merged with the point's (SampleStatistics::merge, common.h:268-310)
     const size_t slot = (size_t)i * ZGPU_BVC_GROUPS + P.group;
-    const double n2 = (double)count;
-    const double mean2 = kS + accS / n2;
-    const double m22 = fmax(0.0, accQ - accS * accS / n2);
     const int n1 = P.count[slot];
     const double nt = (double)n1 + n2;
     if (n1 == 0) {
@@ -226,6 +242,56 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
     P.count[slot] = (int)(n1 + count);
 }
 
+// merges the split moments of every evaluation point, then into its statistics
+template <int D>
+__global__ void splatMergeKernel(const __grid_constant__ BvcSplatParams P, int splits) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nEval) return;
+    double n = 0.0, mean = 0.0, m2 = 0.0, gm[D], gv[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) { gm[d] = 0.0; gv[d] = 0.0; }
+    for (int sp = 0; sp < splits; sp++) {
+        const double* in = P.partial + ((size_t)sp * P.nEval + i) * (3 + 2 * D);
+        const double nb = in[0];
+        if (nb == 0.0) continue;
+        const double nt = n + nb, delta = in[1] - mean;
+        mean += delta * (nb / nt);
+        m2 += in[2] + delta * delta * (n * nb / nt);
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const double e = in[3 + d] - gm[d];
+            gm[d] += e * (nb / nt);
+            gv[d] += in[3 + D + d] + e * e * (n * nb / nt);
+        }
+        n = nt;
+    }
+    if (n == 0.0) return;
+    const size_t slot = (size_t)i * ZGPU_BVC_GROUPS + P.group;
+    const int n1 = P.count[slot];
+    const double nt = (double)n1 + n;
+    const double delta = mean - P.mean[slot];
+    if (n1 == 0) {
+        P.mean[slot] = mean;
+        P.m2[slot] = m2;
+    } else {
+        P.mean[slot] += delta * (n / nt);
+        P.m2[slot] += m2 + delta * delta * ((double)n1 * n / nt);
+    }
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const size_t gslot = slot * D + d;
+        if (n1 == 0) {
+            P.gradMean[gslot] = gm[d];
+            if (P.gradM2) P.gradM2[gslot] = gv[d];
+        } else {
+            const double e = gm[d] - P.gradMean[gslot];
+            P.gradMean[gslot] += e * (n / nt);
+            if (P.gradM2) P.gradM2[gslot] += gv[d] + e * e * ((double)n1 * n / nt);
+        }
+    }
+    P.count[slot] = n1 + (int)n;
+}
+
 // PDE fields at points (zgpu_pde_evaluate)
 template <int D>
 __global__ void pdeKernel(const zgpu_pde pde, int64_t n, const float* __restrict__ x, const float* __restrict__ nrm,
@@ -245,9 +311,23 @@ __global__ void pdeKernel(const zgpu_pde pde, int64_t n, const float* __restrict
 
 }  // namespace
 
-cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, cudaStream_t s) {
-    if (p.nEval == 0 || p.nSamples == 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((p.nEval + kSplatThreads - 1) / kSplatThreads);
+int bvcSplitCount(int64_t nEval, int64_t nSamples, int numSMs) {
+    // enough blocks for ~8 resident per SM, each split at least 8 tiles of the cache
+    const int64_t evalBlocks = (nEval + kSplatThreads - 1) / kSplatThreads;
+    const int64_t want = ((int64_t)numSMs * 8 + evalBlocks - 1) / evalBlocks;
+    const int64_t maxSplits = (nSamples + 8 * kTile - 1) / (8 * kTile);
+    int64_t s = want < maxSplits ? want : maxSplits;
+    if (s > 64) s = 64;
+    return s < 1 ? 1 : (int)s;
+}
+
+cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p0, int splits, cudaStream_t s) {
+    if (p0.nEval == 0 || p0.nSamples == 0) return cudaSuccess;
+    BvcSplatParams p = p0;
+    if (splits <= 1) { p.partial = nullptr; splits = 1; }
+    const int64_t tiles = (p.nSamples + kTile - 1) / kTile;
+    p.splitChunk = ((tiles + splits - 1) / splits) * kTile;
+    const dim3 grid((unsigned)((p.nEval + kSplatThreads - 1) / kSplatThreads), (unsigned)splits);
     if (D == 2) {
         if (screened) splatKernel<2, true><<<grid, kSplatThreads, 0, s>>>(p);
         else splatKernel<2, false><<<grid, kSplatThreads, 0, s>>>(p);
@@ -255,6 +335,11 @@ cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, cudaSt
         if (screened) splatKernel<3, true><<<grid, kSplatThreads, 0, s>>>(p);
         else splatKernel<3, false><<<grid, kSplatThreads, 0, s>>>(p);
     }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !p.partial) return e;
+    const unsigned mg = (unsigned)((p.nEval + 127) / 128);
+    if (D == 2) splatMergeKernel<2><<<mg, 128, 0, s>>>(p, splits);
+    else splatMergeKernel<3><<<mg, 128, 0, s>>>(p, splits);
     return cudaGetLastError();
 }
 

@@ -159,8 +159,15 @@ struct BvcSplatParams {
     double* gradM2;
     float sqrtLambda, radiusClamp, regularization, robinCutoff, cutoffA, cutoffR;
     int group;
+    // cache split across grid.y: splitChunk samples per block row; partial moments
+    // [split][eval][3 + 2 dim] merged by a second kernel (NULL: one split, merged in place)
+    int64_t splitChunk;
+    double* partial;
 };
-cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, cudaStream_t s);
+// splits of the cache for nEval points on numSMs SMs; the partial buffer needs
+// splits * nEval * (3 + 2 dim) doubles when splits > 1
+int bvcSplitCount(int64_t nEval, int64_t nSamples, int numSMs);
+cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, int splits, cudaStream_t s);
 cudaError_t launchPdeEvaluate(int D, const zgpu_pde& pde, int64_t n, const float* x, const float* nrm, const int* aligned,
                               float* src, float* dir, float* rob, float* kap, cudaStream_t s);
 
