@@ -17,8 +17,10 @@ from .api import (BranchTraversalWeight, Context, DenseGrid, EstimationQuantity,
                   populate_geometric_queries_for_dirichlet_boundary,
                   populate_geometric_queries_for_neumann_boundary, populate_geometric_queries_for_robin_boundary)
 from ._lib import ZgpuError
+from . import bvc as _bvc
+from . import io as _io
 
-__all__ = ["Core", "Solvers", "Utils", "ZgpuError", "Context", "default_context"]
+__all__ = ["Core", "Solvers", "Samplers", "Utils", "ZgpuError", "Context", "default_context"]
 
 
 def _dim_factory(cls):
@@ -62,10 +64,30 @@ Solvers = _types.SimpleNamespace(
     WalkOnSpheres=_solver_factory(WalkOnSpheres),
     WalkOnStars=_solver_factory(WalkOnStars),
     NeuralCache=NeuralCache,
+    BVCEvaluationPoint=_bvc.EvaluationPoint,
+    BVCEvaluationPoints=_bvc.EvaluationPoints,
+    BoundaryValueCaching=_bvc.BoundaryValueCachingSolver,
+)
+
+Samplers = _types.SimpleNamespace(
+    BoundarySampler=_bvc._MeshBoundarySampler,
+    DomainSampler=_bvc.UniformDomainSampler,
+    create_uniform_line_segment_boundary_sampler=_bvc.create_uniform_line_segment_boundary_sampler,
+    create_uniform_triangle_boundary_sampler=_bvc.create_uniform_triangle_boundary_sampler,
+    create_uniform_domain_sampler=_bvc.create_uniform_domain_sampler,
 )
 
 Utils = _types.SimpleNamespace(
     DenseGrid=_dim_factory(DenseGrid),
+    load_boundary_mesh=_io.load_boundary_mesh,
+    write_boundary_mesh=_io.write_boundary_mesh,
+    normalize=_io.normalize,
+    apply_shift=_io.apply_shift,
+    flip_orientation=_io.flip_orientation,
+    compute_bounding_box=_io.compute_bounding_box,
+    read_pfm=_io.read_pfm,
+    write_pfm=_io.write_pfm,
+    image_to_grid=_io.image_to_grid,
     get_dense_grid_source_callback=get_dense_grid_source_callback,
     get_dense_grid_dirichlet_callback=get_dense_grid_dirichlet_callback,
     get_dense_grid_robin_callback=get_dense_grid_robin_callback,

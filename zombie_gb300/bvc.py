@@ -321,15 +321,27 @@ class UniformDomainSampler:
                            seeds=_seeds(self.rng, pt.shape[0]))
 
 
-def create_uniform_line_segment_boundary_sampler(positions, indices, inside_solve_region, *weights,
-                                                 compute_weighted_normals=False, seed=None):
-    return UniformLineSegmentBoundarySampler(positions, indices, inside_solve_region, *weights,
+def _sampler_args(args):
+    # (inside), (weights, inside) or (weights, weights_normal_aligned, inside), as the
+    # reference's create_uniform_*_boundary_sampler overloads (python/zombie_bindings.h)
+    if len(args) == 1:
+        return args[0], None, None
+    if len(args) == 2:
+        return args[1], args[0], None
+    if len(args) == 3:
+        return args[2], args[0], args[1]
+    raise TypeError("expected inside_solve_region, optionally preceded by one or two weight arrays")
+
+
+def create_uniform_line_segment_boundary_sampler(positions, indices, *args, compute_weighted_normals=False, seed=None):
+    inside, w, wa = _sampler_args(args)
+    return UniformLineSegmentBoundarySampler(positions, indices, inside, w, wa,
                                              compute_weighted_normals=compute_weighted_normals, seed=seed)
 
 
-def create_uniform_triangle_boundary_sampler(positions, indices, inside_solve_region, *weights,
-                                             compute_weighted_normals=False, seed=None):
-    return UniformTriangleBoundarySampler(positions, indices, inside_solve_region, *weights,
+def create_uniform_triangle_boundary_sampler(positions, indices, *args, compute_weighted_normals=False, seed=None):
+    inside, w, wa = _sampler_args(args)
+    return UniformTriangleBoundarySampler(positions, indices, inside, w, wa,
                                           compute_weighted_normals=compute_weighted_normals, seed=seed)
 
 
