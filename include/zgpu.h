@@ -499,6 +499,50 @@ int zgpu_bvc_splat(zgpu_context* ctx, int dim, const zgpu_pde* pde, const zgpu_b
                    float cutoff_dist_to_absorbing_boundary, float cutoff_dist_to_reflecting_boundary,
                    zgpu_bvc_eval_points* eval_points, int memory);
 
+/* ------------------------- reverse walk on stars --------------------------- */
+/*
+ * Reverse Walk on Stars (point_estimation/reverse_walk_on_stars.h, variance_reduction/
+ * reverse_walk_solver.h): one walk per sample point, started at the sample, that splats the
+ * sample's contribution (source value, Dirichlet value of an absorbing sample offset into the
+ * domain, or Robin data) onto every evaluation point inside each step's star-shaped ball
+ * and visible from the walk position, weighted by the ball's Green's function.
+ */
+typedef struct zgpu_rws_samples {
+    int64_t n;
+    const float* pt;                  /* [n*dim] */
+    const float* normal;              /* [n*dim] */
+    const int32_t* type;              /* ZGPU_SAMPLE_* */
+    const int32_t* estimate_normal_aligned;   /* NULL -> 0 */
+    const float* pdf;
+    const float* contribution;        /* SamplePoint::contribution set by the caller */
+    const float* dist_to_absorbing;
+    const uint64_t* seed;             /* walk of sample i: pcg32(seed[i], stream) */
+} zgpu_rws_samples;
+
+/* ZGPU_RWS_* : the running sums of an rws::EvaluationPoint (reverse_walk_solver.h:19-45) */
+enum { ZGPU_RWS_ABSORBING = 0, ZGPU_RWS_ABSORBING_ALIGNED = 1, ZGPU_RWS_REFLECTING = 2,
+       ZGPU_RWS_REFLECTING_ALIGNED = 3, ZGPU_RWS_SOURCE = 4, ZGPU_RWS_POISSON_KERNEL = 5, ZGPU_RWS_TOTALS = 6 };
+
+typedef struct zgpu_rws_eval_points {
+    int64_t n;
+    const float* pt;                  /* [n*dim] */
+    const float* normal;              /* [n*dim], NULL -> 0 */
+    const int32_t* type;              /* NULL -> IN_DOMAIN; absorbing points are not splatted */
+    double* totals;                   /* [n*6], added to */
+} zgpu_rws_eval_points;
+
+/*
+ * One call of ReverseWalkOnStars::solve over all samples (one walk each, pcg32 stream
+ * `stream`), splatting into eval_points->totals.  Absorbing samples' splats are divided by
+ * normal_offset_for_absorbing_boundary; the Poisson-kernel total (self-normalisation) is kept
+ * when the domain is watertight, the PDE unscreened and the reflecting boundary (if any) pure
+ * Neumann.  report->total_steps counts walk steps, report->total_walks the walks.
+ */
+int zgpu_rws_solve(zgpu_context* ctx, const zgpu_geometric_queries* queries, const zgpu_pde* pde,
+                   const zgpu_walk_settings* settings, const zgpu_rws_samples* samples,
+                   float normal_offset_for_absorbing_boundary, float radius_clamp, float kernel_regularization,
+                   uint64_t stream, zgpu_rws_eval_points* eval_points, int memory, zgpu_solve_report* report);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@
 #include "oracle_walk.h"
 #include "oracle_cache.h"
 #include "oracle_bvc.h"
+#include "oracle_rws.h"
 
 using namespace orc;
 
@@ -486,4 +487,50 @@ extern "C" int orc_bvc_splat(int dim, float absorption, const zgpu_bvc_samples* 
         for (auto& t : th) t.join();
     }
     return 0;
+}
+
+// ReverseWalkOnStarsSolver::solve's walks for all samples (reverse_walk_solver.h:304-338):
+// totals [n_eval][6] added to; returns the number of walk steps
+template <int D>
+uint64_t rwsImpl(const zgpu_geometric_queries* gq, const zgpu_pde* pde, const zgpu_walk_settings* ws,
+                 const zgpu_rws_samples* s, float normalOffset, float radiusClamp, float reg, uint64_t stream,
+                 zgpu_rws_eval_points* ev, int nThreads) {
+    Queries<D> q;
+    q.absorbing = gq->absorbing ? (const Boundary<D>*)((Handle*)gq->absorbing)->b : nullptr;
+    q.reflecting = gq->reflecting ? (const Boundary<D>*)((Handle*)gq->reflecting)->b : nullptr;
+    for (int i = 0; i < D; i++) { q.domainMin[i] = gq->domain_min[i]; q.domainMax[i] = gq->domain_max[i]; }
+    const bool selfNorm = gq->domain_is_watertight && pde->absorption_coeff == 0.0f &&
+                          (!q.hasNonEmptyReflectingBoundary() || pde->are_robin_conditions_pure_neumann);
+    RwsEval<D> e{ev->n, ev->pt, ev->normal, ev->type};
+    nThreads = std::max(1, nThreads);
+    std::vector<std::vector<double>> local(nThreads, std::vector<double>((size_t)ev->n * ZGPU_RWS_TOTALS, 0.0));
+    std::vector<uint64_t> steps(nThreads, 0);
+    std::atomic<int64_t> next{0};
+    auto work = [&](int t) {
+        Solver<D> sv{q, Pde<D>{pde}, *ws};
+        for (;;) {
+            const int64_t i = next.fetch_add(1);
+            if (i >= s->n) break;
+            const bool aligned = s->estimate_normal_aligned ? s->estimate_normal_aligned[i] != 0 : false;
+            reverseWalkSample<D>(sv, load<D>(s->pt + i * D), load<D>(s->normal + i * D), s->type[i], aligned, s->pdf[i],
+                                 s->contribution[i], s->dist_to_absorbing[i], s->seed[i], stream, e, normalOffset,
+                                 radiusClamp, reg, selfNorm, local[t].data(), steps[t]);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nThreads; t++) th.emplace_back(work, t);
+    for (auto& t : th) t.join();
+    uint64_t total = 0;
+    for (int t = 0; t < nThreads; t++) {
+        total += steps[t];
+        for (size_t k = 0; k < local[t].size(); k++) ev->totals[k] += local[t][k];
+    }
+    return total;
+}
+
+extern "C" uint64_t orc_rws_solve(const zgpu_geometric_queries* gq, const zgpu_pde* pde, const zgpu_walk_settings* ws,
+                                  const zgpu_rws_samples* s, float normalOffset, float radiusClamp, float reg,
+                                  uint64_t stream, zgpu_rws_eval_points* ev, int nThreads) {
+    return gq->dim == 2 ? rwsImpl<2>(gq, pde, ws, s, normalOffset, radiusClamp, reg, stream, ev, nThreads)
+                        : rwsImpl<3>(gq, pde, ws, s, normalOffset, radiusClamp, reg, stream, ev, nThreads);
 }

@@ -68,6 +68,8 @@ def lib():
         L.orc_eval_pde.argtypes = [i32, vp, i64, vp, vp, i32, vp, vp, vp, vp]
         L.orc_solve.argtypes = [i32, vp, vp, vp, vp, vp, i32, C.POINTER(C.c_uint64)]
         L.orc_bvc_splat.argtypes = [i32, C.c_float, vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, vp, i32]
+        L.orc_rws_solve.argtypes = [vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_uint64, vp, i32]
+        L.orc_rws_solve.restype = C.c_uint64
         L.orc_hardware_threads.restype = i32
         L.orc_counters.argtypes = [vp]
         L.orc_cache_forward.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, f32, i64, vp, vp, vp]
@@ -297,3 +299,30 @@ def bvc_splat(dim, absorption, samples, evals, radius_clamp=1e-3, kernel_regular
     lib().orc_bvc_splat(dim, float(absorption), C.byref(s), float(radius_clamp), float(kernel_regularization),
                         float(robin_coeff_cutoff), float(cutoff_absorbing), float(cutoff_reflecting), C.byref(e),
                         int(n_threads))
+
+
+def rws_solve(dim, absorbing, reflecting, domain_min, domain_max, pde, settings, samples, evals, normal_offset,
+              radius_clamp=1e-3, kernel_regularization=0.0, stream=0, n_threads=None, watertight=True):
+    """The reverse walks of ReverseWalkOnStarsSolver::solve on the CPU: samples / evals are dicts
+    of numpy arrays with the zgpu_rws_samples / zgpu_rws_eval_points fields; evals["totals"] is
+    added to.  Returns the number of walk steps."""
+    q = A.GeometricQueriesC()
+    q.dim = dim
+    q.domain_is_watertight = int(watertight)
+    for i in range(dim):
+        q.domain_min[i] = float(domain_min[i]); q.domain_max[i] = float(domain_max[i])
+    q.absorbing = absorbing.h if absorbing is not None else None
+    q.reflecting = reflecting.h if reflecting is not None else None
+    s = A.RwsSamplesC()
+    s.n = samples["pt"].shape[0]
+    for name in ("pt", "normal", "type", "estimate_normal_aligned", "pdf", "contribution", "dist_to_absorbing", "seed"):
+        setattr(s, name, A.ptr(samples.get(name)))
+    e = A.RwsEvalPointsC()
+    e.n = evals["pt"].shape[0]
+    for name in ("pt", "normal", "type", "totals"):
+        setattr(e, name, A.ptr(evals.get(name)))
+    if n_threads is None:
+        n_threads = max(1, lib().orc_hardware_threads())
+    return int(lib().orc_rws_solve(C.byref(q), C.byref(pde), C.byref(settings), C.byref(s), float(normal_offset),
+                                   float(radius_clamp), float(kernel_regularization), int(stream), C.byref(e),
+                                   int(n_threads)))

@@ -1,0 +1,127 @@
+"""Reverse Walk on Stars: the GPU's walks and splats against the oracle's restatement of
+ReverseWalkOnStars / ReverseWalkOnStarsSolver (same samples, seeds and streams), and
+end-to-end estimates against manufactured solutions."""
+import numpy as np
+import pytest
+
+from zombie_gb300 import _abi as A
+from zombie_gb300 import problems as P
+from zombie_gb300.api import SampleType
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(pr, n_abs, n_refl, n_dom, offset, seed=3, grid_pts=None):
+    from zombie_gb300 import bvc, rws
+    from zombie_gb300.runner import GpuProblem
+    gp = GpuProblem(pr)
+    inside = gp.queries.inside_domain
+    sa = bvc.UniformLineSegmentBoundarySampler(*pr.absorbing, inside, seed=seed) if pr.absorbing is not None else None
+    if sa is not None:
+        sa.initialize(offset, False)
+    sr = None
+    if pr.reflecting is not None:
+        # reflecting samples sit on the boundary itself: a point-in-domain test of the faces'
+        # midpoints would be a coin flip there, so the solve region keeps every face
+        sr = bvc.UniformLineSegmentBoundarySampler(*pr.reflecting, lambda x: np.ones(len(x), bool), seed=seed + 1)
+        sr.initialize(0.0, False)
+    lo, hi = np.asarray(pr.domain_min[:2]), np.asarray(pr.domain_max[:2])
+    area = float(np.prod(hi - lo)) * float(np.mean(inside(np.random.default_rng(9).uniform(lo, hi, (200000, 2))
+                                                            .astype(np.float32))))
+    sd = bvc.UniformDomainSampler(inside, lo, hi, area, seed=seed + 2) if n_dom > 0 else None
+    solver = rws.ReverseWalkOnStarsSolver(gp.queries, sa, sr, sd)
+    solver.generate_samples(n_abs, n_refl, n_dom, offset, False)
+    pts = pr.points if grid_pts is None else grid_pts
+    ev = rws.EvaluationPoints(pts, dim=2)
+    return gp, solver, ev
+
+
+def test_reverse_walks_match_the_oracle(zgpu, oracle):
+    """Mixed Dirichlet / Neumann problem with a source: absorbing, reflecting and domain samples
+    walk on the GPU and on the oracle with the same seeds and stream; the splatted sums agree."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    pr = P.mixed_wost_2d(n_segments=512, grid=14, spp=4)
+    offset = 0.01
+    gp, solver, ev = _setup(pr, 1500, 800, 800, offset)
+    ws = pr.settings
+    og = ev.totals.copy()
+    ab = oracle.Boundary(2, *pr.absorbing)
+    rf = oracle.Boundary(2, *pr.reflecting, kind=pr.reflecting_kind, silhouette_precision=pr.ignore_silhouette_precision)
+    caches = [solver.absorbing, solver.reflecting, solver.domain]
+    for c in caches:
+        mask = solver._contributions(gp.pde, ws, c)
+        idx = np.nonzero(mask)[0]
+        smp = {k: np.ascontiguousarray(getattr(c, k)[idx]) for k in
+               ("pt", "normal", "type", "estimate_normal_aligned", "pdf", "contribution", "dist_to_absorbing", "seed")}
+        evd = dict(pt=ev.pt, normal=ev.normal, type=ev.type, totals=og)
+        oracle.rws_solve(2, ab, rf, pr.domain_min, pr.domain_max, pr.pde, ws, smp, evd, offset, stream=0)
+    solver.solve(gp.pde, ws, offset, 1e-3, 0.0, ev)
+    gg = ev.totals
+    assert all(r.error_word == 0 for r in solver.last_reports)
+    # walks from the absorbing samples are short and follow the oracle's step for step; the
+    # long walks of reflecting and domain samples along the Neumann boundary part ways with
+    # the oracle's after FP32 differences in star radii, so only their sums are compared
+    for g in (A.ZGPU_RWS_ABSORBING, A.ZGPU_RWS_POISSON_KERNEL):
+        a, b = gg[:, g], og[:, g]
+        assert np.any(b != 0), g
+        assert abs(a.sum() - b.sum()) <= 2e-3 * np.abs(b).sum(), (g, a.sum(), b.sum())
+        close = np.abs(a - b) <= 1e-3 * np.abs(b).max()
+        assert close.mean() > 0.9, (g, close.mean())
+    for g in (A.ZGPU_RWS_REFLECTING, A.ZGPU_RWS_SOURCE):
+        a, b = gg[:, g], og[:, g]
+        assert np.any(b != 0), g
+        assert abs(a.sum() - b.sum()) <= 2e-2 * np.abs(b).sum(), (g, a.sum(), b.sum())
+
+
+def test_reverse_walks_solve_laplace(zgpu):
+    """Dirichlet samples offset into the domain (self-normalised by the Poisson-kernel sums)
+    recover the harmonic solution at interior points."""
+    pr = P.laplace_wos_2d(n_segments=1024, grid=24, spp=4)
+    offset = 5e-3
+    gp, solver, ev = _setup(pr, 40000, 0, 0, offset)
+    for _ in range(2):
+        solver.solve(gp.pde, pr.settings, offset, 1e-3, 0.0, ev)
+    est = solver.get_estimated_solution(ev)
+    ex = pr.exact()
+    far = gp.dist > 0.05
+    err = est[far] - ex[far]
+    info = dict(rmse=float(np.sqrt(np.mean(err ** 2))), bias=float(err.mean()), std=float(np.std(ex[far])),
+                steps=sum(r.total_steps for r in solver.last_reports))
+    assert info["rmse"] < 0.15 * info["std"] + 0.02, info
+    assert np.corrcoef(est[far], ex[far])[0, 1] > 0.97, info
+
+
+def test_reverse_walks_with_a_source(zgpu):
+    """Poisson with f = -1 on the star polygon: domain samples splat the source, Dirichlet
+    samples the boundary values; the sum matches u = e^x cos y + (x^2 + y^2) / 4."""
+    pr = P.mixed_wost_2d(n_segments=1024, grid=20, spp=4)
+    # all-Dirichlet version of the mixed problem (same solution, f = -1)
+    pr.absorbing = (np.concatenate([pr.absorbing[0], pr.reflecting[0]]),
+                    np.concatenate([pr.absorbing[1], pr.reflecting[1] + len(pr.absorbing[0])]))
+    pr.reflecting = None
+    offset = 5e-3
+    gp, solver, ev = _setup(pr, 30000, 0, 60000, offset)
+    solver.solve(gp.pde, pr.settings, offset, 1e-3, 0.0, ev)
+    est = solver.get_estimated_solution(ev)
+    ex = pr.exact()
+    far = gp.dist > 0.05
+    err = est[far] - ex[far]
+    rmse = float(np.sqrt(np.mean(err ** 2)))
+    assert rmse < 0.15 * float(np.std(ex[far])) + 0.03, (rmse, float(err.mean()))
+
+
+def test_reverse_walks_mixed_boundary(zgpu):
+    """Mixed Dirichlet / Neumann with f = -1: absorbing, reflecting (Neumann data) and domain
+    samples together recover the manufactured solution away from the boundary."""
+    pr = P.mixed_wost_2d(n_segments=1024, grid=20, spp=4)
+    gp, solver, ev = _setup(pr, 30000, 40000, 60000, 5e-3)
+    solver.solve(gp.pde, pr.settings, 5e-3, 1e-3, 0.0, ev)
+    est = solver.get_estimated_solution(ev)
+    ex = pr.exact()
+    far = (gp.dist > 0.05) & (gp.queries.compute_dist_to_reflecting_boundary(pr.points) > 0.05)
+    err = est[far] - ex[far]
+    info = dict(rmse=float(np.sqrt(np.mean(err ** 2))), bias=float(err.mean()), std=float(np.std(ex[far])))
+    assert abs(info["bias"]) < 0.05, info
+    assert info["rmse"] < 0.25 * info["std"] + 0.03, info

@@ -244,3 +244,32 @@ class BvcEvalPointsC(C.Structure):
         ("gradient_mean", C.c_void_p),
         ("gradient_m2", C.c_void_p),
     ]
+
+
+ZGPU_RWS_ABSORBING, ZGPU_RWS_ABSORBING_ALIGNED, ZGPU_RWS_REFLECTING, ZGPU_RWS_REFLECTING_ALIGNED, ZGPU_RWS_SOURCE, \
+    ZGPU_RWS_POISSON_KERNEL = range(6)
+ZGPU_RWS_TOTALS = 6
+
+
+class RwsSamplesC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("pt", C.c_void_p),
+        ("normal", C.c_void_p),
+        ("type", C.c_void_p),
+        ("estimate_normal_aligned", C.c_void_p),
+        ("pdf", C.c_void_p),
+        ("contribution", C.c_void_p),
+        ("dist_to_absorbing", C.c_void_p),
+        ("seed", C.c_void_p),
+    ]
+
+
+class RwsEvalPointsC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("pt", C.c_void_p),
+        ("normal", C.c_void_p),
+        ("type", C.c_void_p),
+        ("totals", C.c_void_p),
+    ]

@@ -42,6 +42,7 @@ def lib():
         L.zgpu_boundary_update_robin_coefficients.argtypes = [vp, vp, vp]
         L.zgpu_pde_evaluate.argtypes = [vp, i32, vp, i64, vp, vp, vp, i32, vp, vp, vp, vp]
         L.zgpu_bvc_splat.argtypes = [vp, i32, vp, vp, f32, f32, f32, f32, f32, vp, i32]
+        L.zgpu_rws_solve.argtypes = [vp, vp, vp, vp, vp, f32, f32, f32, C.c_uint64, vp, i32, vp]
         L.zgpu_boundary_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64)]
         L.zgpu_boundary_signed_volume.argtypes = [vp, C.POINTER(C.c_float)]

@@ -1158,3 +1158,98 @@ int zgpu_bvc_splat(zgpu_context* ctx, int dim, const zgpu_pde* pde, const zgpu_b
     ZG_CUDA(cudaStreamSynchronize(ctx->stream));
     return ZGPU_OK;
 }
+
+// ------------------------------------------------------------------ reverse walk on stars
+int zgpu_rws_solve(zgpu_context* ctx, const zgpu_geometric_queries* q, const zgpu_pde* pde, const zgpu_walk_settings* ws,
+                   const zgpu_rws_samples* samples, float normal_offset_for_absorbing_boundary, float radius_clamp,
+                   float kernel_regularization, uint64_t stream, zgpu_rws_eval_points* ev, int memory,
+                   zgpu_solve_report* report) {
+    if (!ctx || !q || !pde || !ws || !samples || !ev) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    const int D = q->dim;
+    if (D != 2 && D != 3) return fail(ZGPU_ERR_INVALID_ARG, "queries dim must be 2 or 3, got %d", D);
+    ZG_TRY(checkScene(q, pde, ws, D));
+    if (memory != ZGPU_MEM_HOST && memory != ZGPU_MEM_DEVICE) return fail(ZGPU_ERR_INVALID_ARG, "unknown memory space");
+    if (samples->n < 0 || ev->n < 0) return fail(ZGPU_ERR_INVALID_ARG, "negative sizes");
+    if (samples->n > 0 && (!samples->pt || !samples->normal || !samples->type || !samples->pdf || !samples->contribution ||
+                           !samples->dist_to_absorbing || !samples->seed))
+        return fail(ZGPU_ERR_INVALID_ARG, "sample arrays pt, normal, type, pdf, contribution, dist_to_absorbing and "
+                                          "seed are required");
+    if (ev->n > 0 && (!ev->pt || !ev->totals)) return fail(ZGPU_ERR_INVALID_ARG, "evaluation arrays pt and totals are required");
+    if (!(normal_offset_for_absorbing_boundary > 0.0f))
+        return fail(ZGPU_ERR_INVALID_ARG, "normal_offset_for_absorbing_boundary must be > 0");
+    if (samples->n >= ((int64_t)1 << 40) || ev->n >= ((int64_t)1 << 30)) return fail(ZGPU_ERR_INVALID_ARG, "too many points");
+    if (report) std::memset(report, 0, sizeof(*report));
+    if (samples->n == 0 || ev->n == 0) return ZGPU_OK;
+    ZG_CUDA(cudaSetDevice(ctx->device));
+    using C = zgpu_context;
+    cudaStream_t s = ctx->stream;
+    const int64_t ns = samples->n, ne = ev->n;
+    RwsParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.sc = sceneOf(q, pde, ws);
+    ZG_TRY(stageGrids(ctx, P.sc.pde, D, 0));
+    P.nSamples = ns;
+    ZG_TRY(stageIn<float>(ctx, C::kB0, samples->pt, (size_t)ns * D, memory, &P.pt));
+    ZG_TRY(stageIn<float>(ctx, C::kB1, samples->normal, (size_t)ns * D, memory, &P.normal));
+    ZG_TRY(stageIn<int>(ctx, C::kB2, samples->type, (size_t)ns, memory, &P.type));
+    ZG_TRY(stageIn<int>(ctx, C::kB3, samples->estimate_normal_aligned, (size_t)ns, memory, &P.aligned));
+    ZG_TRY(stageIn<float>(ctx, C::kB4, samples->pdf, (size_t)ns, memory, &P.pdf));
+    ZG_TRY(stageIn<float>(ctx, C::kB5, samples->contribution, (size_t)ns, memory, &P.contribution));
+    ZG_TRY(stageIn<float>(ctx, C::kB6, samples->dist_to_absorbing, (size_t)ns, memory, &P.distAbs));
+    ZG_TRY(stageIn<uint64_t>(ctx, C::kB7, samples->seed, (size_t)ns, memory, &P.seed));
+    P.stream = stream;
+    P.nEval = ne;
+    ZG_TRY(stageIn<float>(ctx, C::kB9, ev->pt, (size_t)ne * D, memory, &P.evalPt));
+    ZG_TRY(stageIn<float>(ctx, C::kB10, ev->normal, (size_t)ne * D, memory, &P.evalNormal));
+    ZG_TRY(stageIn<int>(ctx, C::kB11, ev->type, (size_t)ne, memory, &P.evalType));
+    ZG_TRY(stageInOut<double>(ctx, C::kB13, ev->totals, (size_t)ne * ZGPU_RWS_TOTALS, memory, &P.totals));
+    // the evaluation points' tree for the per-step radius searches
+    float4* evalNodes = nullptr;
+    int* evalOrder = nullptr;
+    int nEvalNodes = 0, evalDepth = 0;
+    cudaError_t e = buildPointBvhOnDevice(D, P.evalPt, (int)ne, s, &evalNodes, &nEvalNodes, &evalDepth, &evalOrder);
+    auto freeTree = [&]() { cudaFree(evalNodes); cudaFree(evalOrder); };
+    if (e != cudaSuccess) {
+        freeTree();
+        if (e == cudaErrorNotSupported) return fail(ZGPU_ERR_UNSUPPORTED, "evaluation-point tree too deep");
+        return fail(ZGPU_ERR_CUDA, "evaluation-point tree: %s", cudaGetErrorString(e));
+    }
+    P.evalNodes = evalNodes;
+    P.evalOrder = evalOrder;
+    P.evalDepth = evalDepth;
+    P.normalOffset = normal_offset_for_absorbing_boundary;
+    P.radiusClamp = radius_clamp;
+    P.regularization = kernel_regularization;
+    P.selfNormalize = q->domain_is_watertight && pde->absorption_coeff == 0.0f &&
+                      (!P.sc.hasRefl || pde->are_robin_conditions_pure_neumann);
+    P.stackEntries = 8;
+    if (P.sc.hasAbs) P.stackEntries = std::max(P.stackEntries, P.sc.absorbing.stackEntries);
+    if (P.sc.hasRefl) P.stackEntries = std::max(P.stackEntries, P.sc.reflecting.stackEntries);
+    unsigned long long* counters = nullptr;
+    if (int st = scratch<unsigned long long>(ctx, C::kCounters, 16, &counters)) { freeTree(); return st; }
+    P.counters = counters;
+    P.errorWord = (unsigned int*)(counters + 8);
+    e = cudaMemsetAsync(counters, 0, 16 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[1], s);
+    if (e == cudaSuccess) e = launchReverseWalks(D, pde->absorption_coeff > 0.0f, P, ctx->numSMs * 4, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[2], s);
+    if (e != cudaSuccess) { freeTree(); return fail(ZGPU_ERR_CUDA, "reverse walks: %s", cudaGetErrorString(e)); }
+    int st = stageOut<double>(ctx, P.totals, ev->totals, (size_t)ne * ZGPU_RWS_TOTALS, memory);
+    if (st == ZGPU_OK) {
+        e = cudaMemcpyAsync(ctx->hostCounters, counters, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = fail(ZGPU_ERR_CUDA, "reverse walks: %s", cudaGetErrorString(e));
+    }
+    freeTree();
+    if (st != ZGPU_OK) return st;
+    const unsigned int errWord = (unsigned int)(ctx->hostCounters[8] & 0xffffffffu);
+    if (report) {
+        report->total_steps = ctx->hostCounters[0];
+        report->total_walks = ctx->hostCounters[1];
+        report->error_word = errWord;
+        cudaEventElapsedTime(&report->kernel_ms, ctx->ev[1], ctx->ev[2]);
+        report->total_ms = report->kernel_ms;
+    }
+    if (errWord) return fail(ZGPU_ERR_DEVICE_STATE, "reverse walks: device error word 0x%x", errWord);
+    return ZGPU_OK;
+}

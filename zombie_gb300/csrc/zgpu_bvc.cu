@@ -58,12 +58,6 @@ struct FreeSpace {
     }
 };
 
-// KernelRegularization (core/distributions.h:13-56)
-template <int D> ZG_D float regularizeG(float r) { return D == 2 ? 1.0f : erff(r); }
-template <int D> ZG_D float regularizeP(float r) {
-    if (D == 2) return 1.0f - expf(-r * r);
-    return erff(r) - 2.0f * r * expf(-r * r) * 0.56418958354775628f;   // 1 / sqrt(pi)
-}
 
 // the statistic group a sample feeds (splat / splatBoundaryData / splatSourceData)
 ZG_HD int groupOf(int type, int aligned) {
@@ -149,7 +143,7 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
                 if (source) {
                     // splatSourceData (boundary_value_caching.h:775-811)
                     if (!finiteF(G) || !finiteF(len(dG))) continue;
-                    if (P.regularization > 0.0f) G *= regularizeG<D>(r / P.regularization);
+                    if (P.regularization > 0.0f) G *= kernelRegularizationG<D>(r / P.regularization);
                     const float f = scon[k];
                     est = alpha * G * f / pdf;
                     const float a = alpha > 1.0f ? 0.0f : alpha;     // no gradient on the boundary
@@ -161,8 +155,8 @@ __global__ void __launch_bounds__(kSplatThreads) splatKernel(const __grid_consta
                     if (!finiteF(G) || !finiteF(Pk) || !finiteF(len(dG)) || !finiteF(len(dP))) continue;
                     if (P.regularization > 0.0f) {
                         const float rr = r / P.regularization;
-                        G *= regularizeG<D>(rr);
-                        Pk *= regularizeP<D>(rr);
+                        G *= kernelRegularizationG<D>(rr);
+                        Pk *= kernelRegularizationP<D>(rr);
                     }
                     const float u = ssol[k], dn = sdn[k], h = scon[k], kap = skap[k];
                     const float a = alpha > 1.0f ? 0.0f : alpha;

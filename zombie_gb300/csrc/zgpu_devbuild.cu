@@ -760,6 +760,19 @@ cudaError_t wideCones(const BinaryTree& t, ConeArrays item, const int* wideKids,
     return cudaSuccess;
 }
 
+// points as zero-extent boxes (unit weight), with their bounds
+template <int D>
+__global__ void pointBoxKernel(const float* __restrict__ pts, int n, float4* __restrict__ lo, float4* __restrict__ hi,
+                               float* __restrict__ weight, int* __restrict__ sceneKey) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float p[3] = {0.0f, 0.0f, 0.0f};
+    for (int j = 0; j < D; j++) p[j] = pts[(size_t)i * D + j];
+    lo[i] = hi[i] = make_float4(p[0], p[1], p[2], 0.0f);
+    weight[i] = 1.0f;
+    centreBounds(D, p, p, sceneKey);
+}
+
 cudaError_t initSceneKey(int* key, cudaStream_t s) {
     static const int init[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000, (int)0x80000000};
     ZB(cudaMemcpyAsync(key, init, sizeof(init), cudaMemcpyHostToDevice, s));
@@ -767,6 +780,28 @@ cudaError_t initSceneKey(int* key, cudaStream_t s) {
 }
 
 }  // namespace
+
+// A 4-wide BVH over n device-resident points for radius searches; order maps leaf slots to
+// point indices.
+cudaError_t buildPointBvhOnDevice(int D, const float* pts, int n, cudaStream_t s, float4** outNodes, int* outCount,
+                                  int* outDepth, int** outOrder) {
+    *outNodes = nullptr; *outCount = 0; *outDepth = 0; *outOrder = nullptr;
+    if (n <= 0) return cudaSuccess;
+    const int T = 256, G = (n + T - 1) / T;
+    DevBuf<float4> lo, hi;
+    DevBuf<float> w;
+    DevBuf<int> sceneKey;
+    ZB(lo.alloc(n)); ZB(hi.alloc(n)); ZB(w.alloc(n)); ZB(sceneKey.alloc(6));
+    ZB(initSceneKey(sceneKey.p, s));
+    if (D == 2) pointBoxKernel<2><<<G, T, 0, s>>>(pts, n, lo.p, hi.p, w.p, sceneKey.p);
+    else pointBoxKernel<3><<<G, T, 0, s>>>(pts, n, lo.p, hi.p, w.p, sceneKey.p);
+    ZB(cudaGetLastError());
+    BinaryTree tree;
+    ZB(buildBinary(D, lo.p, hi.p, w.p, sceneKey.p, n, s, tree));
+    ZB(collapseWide(D, tree, lo.p, hi.p, w.p, s, outNodes, outCount, outDepth, nullptr));
+    *outOrder = tree.ids.release();
+    return cudaSuccess;
+}
 
 // Builds on the device from device-resident positions / indices.  Absorbing boundaries fill
 // nodes, prims and primIndex; reflecting boundaries (kind 1 Neumann, 2 Robin with kmin/kmax

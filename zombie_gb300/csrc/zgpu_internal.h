@@ -171,6 +171,40 @@ cudaError_t launchBvcSplat(int D, bool screened, const BvcSplatParams& p, int sp
 cudaError_t launchPdeEvaluate(int D, const zgpu_pde& pde, int64_t n, const float* x, const float* nrm, const int* aligned,
                               float* src, float* dir, float* rob, float* kap, cudaStream_t s);
 
+// a 4-wide BVH over points (reverse walks' radius searches, zgpu_devbuild.cu): nodes as the
+// boundary trees', order[sorted slot] = point index; device arrays owned by the receiver
+cudaError_t buildPointBvhOnDevice(int D, const float* pts, int n, cudaStream_t s, float4** nodes, int* nNodes,
+                                  int* depth, int** order);
+
+// reverse Walk on Stars (zgpu_rws.cu)
+struct RwsParams {
+    SceneDesc sc;
+    int64_t nSamples;
+    const float* pt;
+    const float* normal;
+    const int* type;
+    const int* aligned;
+    const float* pdf;
+    const float* contribution;
+    const float* distAbs;
+    const uint64_t* seed;
+    uint64_t stream;
+    int64_t nEval;
+    const float* evalPt;
+    const float* evalNormal;
+    const int* evalType;
+    double* totals;
+    const float4* evalNodes;       // point BVH over the evaluation points
+    const int* evalOrder;
+    int evalDepth;
+    float normalOffset, radiusClamp, regularization;
+    int selfNormalize;
+    int stackEntries;
+    unsigned long long* counters;  // [0] steps, [1] walks
+    unsigned int* errorWord;
+};
+cudaError_t launchReverseWalks(int D, bool screened, const RwsParams& p, int blocks, cudaStream_t s);
+
 // accessors into the C ABI objects (zgpu_api.cu)
 void setLastError(const char* msg);
 bool boundaryView(const zgpu_boundary* b, BoundaryView* view, int* dim, int* kind);

@@ -147,6 +147,14 @@ ZG_D V<3> toFrame(const V<3>& n, const V<3>& d) {
     return r;
 }
 
+// KernelRegularization (core/distributions.h:13-56): factors that smooth the singularity of
+// the Green's function and the Poisson kernel at r (in units of the regularisation radius)
+template <int D> ZG_D float kernelRegularizationG(float r) { return D == 2 ? 1.0f : erff(r); }
+template <int D> ZG_D float kernelRegularizationP(float r) {
+    if (D == 2) return 1.0f - expf(-r * r);
+    return erff(r) - 2.0f * r * expf(-r * r) * 0.56418958354775628f;   // 1 / sqrt(pi)
+}
+
 // Latin-hypercube stratum of sample k among m for dimension j of point `key`: an affine
 // permutation k -> (a k + b) mod m with a coprime to m, a and b hashed from (key, j)
 ZG_D uint32_t lhsStratum(uint64_t key, int j, uint32_t k, uint32_t m) {

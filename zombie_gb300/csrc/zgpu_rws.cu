@@ -1,0 +1,265 @@
+// zgpu_rws.cu -- reverse Walk on Stars (point_estimation/reverse_walk_on_stars.h) with the
+// splat of variance_reduction/reverse_walk_solver.h.
+//
+// One thread runs the walk of one sample (grid-stride over the samples).  At every step the
+// walk's star-shaped ball is searched for evaluation points: a 4-wide BVH over the points,
+// built on the device for the call, traversed with a local stack; a point inside the ball,
+// not on the absorbing boundary and visible from the walk position (line of sight against the
+// reflecting boundary) receives alpha * throughput * G(r) / pdf times the sample's
+// contribution by FP64 atomic add into its running sums.  Split states of the weight window
+// wait in a per-thread FIFO, processed in the reference's queue order, all on the sample's
+// one pcg32 stream.
+#include <cfloat>
+
+#include "zgpu_internal.h"
+
+namespace zg {
+namespace {
+
+constexpr int kRwsThreads = 128;
+constexpr int kRwsQueue = 8;
+constexpr int kPointStack = 64;
+
+// outsideBoundingDomain (core/geometric_queries.h:373-379)
+template <int D>
+ZG_D bool outsideDomainBox(const SceneDesc& sc, const V<D>& x) {
+#pragma unroll
+    for (int i = 0; i < D; i++)
+        if (x[i] < sc.domainMin[i] || x[i] > sc.domainMax[i]) return true;
+    return false;
+}
+
+template <int D>
+struct RevState {
+    V<D> pt, nrm, prevDir;
+    float prevDist, thr;
+    int wlen;
+    bool onRefl;
+};
+
+// splatContribution (reverse_walk_solver.h:236-302)
+template <int D, bool SCREENED>
+ZG_D void splatBall(const RwsParams& P, const RevState<D>& s, const Greens<D, SCREENED>& g, float R, float pdf,
+                    float contrib, int group, bool toPoissonTotal, TravStack& S, uint32_t& err) {
+    BoundaryView t;
+    t.nodes = P.evalNodes;
+    const float R2 = R * R;
+    int stack[kPointStack];
+    int sp = 0;
+    int node = 0;
+    const float alpha = s.onRefl ? 2.0f : 1.0f;
+    for (int guard = 0; guard < (1 << 26); guard++) {
+        WideNode<D> w;
+        loadNode<D>(t, node, w);
+#pragma unroll 1
+        for (int k = 0; k < 4; k++) {
+            const int c = w.child[k];
+            if (c == kEmptyChild || !(boxDist2<D>(w, k, s.pt) < R2)) continue;
+            if (!isLeaf(c)) {
+                if (sp < kPointStack) stack[sp++] = c;
+                else err |= kErrStackOverflow;
+                continue;
+            }
+            const int first = leafFirst(c), count = leafCount(c);
+#pragma unroll 1
+            for (int j = 0; j < count; j++) {
+                const int e = __ldg(P.evalOrder + first + j);
+                const V<D> xe = vload<D>(P.evalPt + (size_t)e * D);
+                const float d2 = len2(xe - s.pt);
+                if (!(d2 < R2)) continue;
+                const int te = P.evalType ? P.evalType[e] : ZGPU_SAMPLE_IN_DOMAIN;
+                if (te == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) continue;     // not splatted
+                if (P.sc.hasRefl) {
+                    // intersectsWithReflectingBoundary: the segment between the points, each
+                    // offset off the reflecting boundary when it lies on it
+                    const V<D> p1 = s.onRefl ? offsetPoint<D>(s.pt, -s.nrm) : s.pt;
+                    V<D> p2 = xe;
+                    if (te == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && P.evalNormal)
+                        p2 = offsetPoint<D>(xe, -vload<D>(P.evalNormal + (size_t)e * D));
+                    const V<D> seg = p2 - p1;
+                    const float sl = len(seg);
+                    if (sl > 0.0f && intersectRay<D>(P.sc.reflecting, p1, (1.0f / sl) * seg, sl, true, S, err).slot >= 0)
+                        continue;
+                }
+                float r = fmaxf(P.radiusClamp, sqrtf(d2));
+                float G = g.evaluate(r);
+                if (P.regularization > 0.0f) G *= kernelRegularizationG<D>(r / P.regularization);
+                float weight = alpha * s.thr * G / pdf;
+                if (group <= ZGPU_RWS_ABSORBING_ALIGNED) weight /= P.normalOffset;
+                atomicAdd(P.totals + (size_t)e * ZGPU_RWS_TOTALS + group, (double)(weight * contrib));
+                if (toPoissonTotal) atomicAdd(P.totals + (size_t)e * ZGPU_RWS_TOTALS + ZGPU_RWS_POISSON_KERNEL, (double)weight);
+            }
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+}
+
+// applyWeightWindow (reverse_walk_on_stars.h:230-263): split states join the FIFO
+template <int D>
+ZG_D bool weightWindow(const zgpu_walk_settings& ws, Pcg32& rng, RevState<D>& s, RevState<D>* q, int qh, int& qn,
+                       uint32_t& err) {
+    if (s.thr > ws.splitting_threshold) {
+        float left = s.thr - ws.splitting_threshold;
+        s.thr = ws.splitting_threshold;
+        RevState<D> split = s;
+        split.wlen = 0;
+        while (left > ws.splitting_threshold) {
+            left -= ws.splitting_threshold;
+            if (qn < kRwsQueue) q[(qh + qn++) % kRwsQueue] = split;
+            else err |= kErrSplitOverflow;
+        }
+        if (rng.uniform() < left / ws.splitting_threshold) {
+            if (qn < kRwsQueue) q[(qh + qn++) % kRwsQueue] = split;
+            else err |= kErrSplitOverflow;
+        }
+    } else if (s.thr < ws.russian_roulette_threshold) {
+        const float survival = s.thr / ws.russian_roulette_threshold;
+        if (survival < rng.uniform()) { s.thr = 0.0f; return true; }
+        s.thr = ws.russian_roulette_threshold;
+    }
+    return false;
+}
+
+template <int D, bool SCREENED>
+__global__ void __launch_bounds__(kRwsThreads) reverseWalkKernel(const __grid_constant__ RwsParams P) {
+    extern __shared__ int dynStack[];
+    TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
+                (int)blockDim.x, P.stackEntries};
+    const zgpu_walk_settings& ws = P.sc.ws;
+    DevicePde<D> pde;
+    pde.p = &P.sc.pde;
+    const bool ds = ws.solve_double_sided != 0;
+    uint32_t err = 0;
+    unsigned long long steps = 0, walks = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.nSamples;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int type = P.type[i];
+        const bool aligned = P.aligned ? P.aligned[i] != 0 : false;
+        const float pdf = P.pdf[i], contrib = P.contribution[i];
+        int group;
+        if (type == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) group = aligned ? ZGPU_RWS_ABSORBING_ALIGNED : ZGPU_RWS_ABSORBING;
+        else if (type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY) group = aligned ? ZGPU_RWS_REFLECTING_ALIGNED : ZGPU_RWS_REFLECTING;
+        else group = ZGPU_RWS_SOURCE;
+        const bool toPoisson = P.selfNormalize && group == ZGPU_RWS_ABSORBING;
+        Pcg32 rng;
+        rng.seed(P.seed[i], P.stream);
+        walks++;
+        // the walk's initial state (reverse_walk_on_stars.h:121-138)
+        RevState<D> s;
+        s.pt = vload<D>(P.pt + (size_t)i * D);
+        s.nrm = vload<D>(P.normal + (size_t)i * D);
+        s.onRefl = type == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY;
+        s.prevDir = (ds && s.onRefl && aligned) ? -s.nrm : s.nrm;
+        s.prevDist = FLT_MAX;
+        s.thr = 1.0f;
+        s.wlen = 0;
+        RevState<D> q[kRwsQueue];
+        int qh = 0, qn = 0;
+        bool first = true;
+        for (int states = 0;; states++) {
+            if (states >= 64) { err |= kErrBudget; break; }      // bounds the splits of one sample
+            Greens<D, SCREENED> g;
+            g.sqrtLambda = sqrtf(fmaxf(P.sc.pde.absorption_coeff, 0.0f));
+            g.yukawa = P.sc.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == 0;
+            float dist = first ? P.distAbs[i] : (P.sc.hasAbs ? closestPoint<D>(P.sc.absorbing, s.pt, S, err).d : FLT_MAX);
+            first = false;
+            // walk (reverse_walk_on_stars.h:265-393)
+            while (dist > ws.epsilon_shell_for_absorbing_boundary) {
+                steps++;
+                bool flip = false;
+                if (ds && s.onRefl && s.prevDist > 0.0f && dot(s.prevDir, s.nrm) < 0.0f) {
+                    s.nrm = -s.nrm;
+                    flip = true;
+                }
+                float R;
+                if (ws.steps_before_using_maximal_spheres <= s.wlen) {
+                    R = dist;
+                } else if (s.onRefl && pde.hasNonZeroRobinCoeff(s.pt)) {
+                    R = ws.epsilon_shell_for_reflecting_boundary;
+                } else {
+                    R = P.sc.hasRefl ? starRadius<D>(P.sc.reflecting, s.pt, ws.epsilon_shell_for_reflecting_boundary,
+                                                     dist, ws.silhouette_precision, flip, S, err)
+                                     : dist;
+                    if (ws.epsilon_shell_for_reflecting_boundary <= dist)
+                        R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
+                }
+                g.update(s.pt, R);
+                splatBall<D, SCREENED>(P, s, g, R, pdf, contrib, group, toPoisson, S, err);
+                V<D> dir = sampleSphere<D>(rng);
+                if (s.onRefl && dot(s.nrm, dir) > 0.0f) dir = -dir;
+                const V<D> origin = s.onRefl ? offsetPoint<D>(s.pt, -s.nrm) : s.pt;
+                V<D> hitPt = origin + R * dir, hitN = vzero<D>();
+                float hitDist = R;
+                bool hit = false;
+                if (P.sc.hasRefl) {
+                    RayHit<D> h = intersectRay<D>(P.sc.reflecting, origin, dir, R, false, S, err);
+                    if (h.slot >= 0) {
+                        hit = true;
+                        hitDist = h.t;
+                        hitPt = origin + h.t * dir;
+                        hitN = primNormal<D>(loadPrim<D>(P.sc.reflecting, h.slot));
+                    }
+                }
+                s.prevDist = hitDist;
+                s.prevDir = dir;
+                s.pt = hitPt;
+                s.nrm = hitN;
+                s.onRefl = hit;
+                // computeWalkStepThroughput (reverse_walk_on_stars.h:199-228)
+                float stepThr;
+                if (s.onRefl && s.prevDist > kFltEps) {
+                    float kappa = 0.0f;
+                    V<D> n = s.nrm;
+                    if (!P.sc.pde.are_robin_conditions_pure_neumann) {
+                        bool f2 = false;
+                        if (ds) { f2 = dot(s.prevDir, s.nrm) < 0.0f; if (f2) n = -n; }
+                        kappa = pde.robinCoeff(s.pt, ds && f2);
+                    }
+                    const float refl = g.reflectance(s.prevDist, s.prevDir, n, kappa);
+                    stepThr = fminf(fmaxf(refl, 0.0f), P.sc.pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f);
+                } else {
+                    stepThr = g.directionSampledPoissonKernel(s.pt);
+                }
+                s.thr *= stepThr;
+                if (!s.onRefl && outsideDomainBox<D>(P.sc, s.pt)) break;                 // escaped
+                if (weightWindow<D>(ws, rng, s, q, qh, qn, err)) break;                // roulette
+                s.wlen++;
+                if (s.wlen >= ws.max_walk_length) break;
+                if (P.sc.pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == s.wlen) g.yukawa = true;
+                dist = P.sc.hasAbs ? closestPoint<D>(P.sc.absorbing, s.pt, S, err).d : FLT_MAX;
+            }
+            if (qn == 0) break;
+            s = q[qh];
+            qh = (qh + 1) % kRwsQueue;
+            qn--;
+        }
+    }
+    // warp-reduce the counters, one atomic per warp
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        steps += __shfl_xor_sync(0xffffffffu, steps, o);
+        walks += __shfl_xor_sync(0xffffffffu, walks, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+    }
+    if (lane == 0) {
+        if (steps) atomicAdd(P.counters + 0, steps);
+        if (walks) atomicAdd(P.counters + 1, walks);
+        if (err) atomicOr(P.errorWord, err);
+    }
+}
+
+}  // namespace
+
+cudaError_t launchReverseWalks(int D, bool screened, const RwsParams& p, int blocks, cudaStream_t s) {
+    if (p.nSamples == 0) return cudaSuccess;
+    const size_t smem = (size_t)p.stackEntries * kRwsThreads * 8;
+    const void* f = D == 2 ? (screened ? (const void*)reverseWalkKernel<2, true> : (const void*)reverseWalkKernel<2, false>)
+                           : (screened ? (const void*)reverseWalkKernel<3, true> : (const void*)reverseWalkKernel<3, false>);
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    void* args[] = {const_cast<RwsParams*>(&p)};
+    return cudaLaunchKernel(f, dim3(blocks), dim3(kRwsThreads), args, smem, s);
+}
+
+}  // namespace zg
