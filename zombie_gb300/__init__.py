@@ -19,6 +19,7 @@ from .api import (BranchTraversalWeight, Context, DenseGrid, EstimationQuantity,
 from ._lib import ZgpuError
 from . import bvc as _bvc
 from . import io as _io
+from . import rws as _rws
 
 __all__ = ["Core", "Solvers", "Samplers", "Utils", "ZgpuError", "Context", "default_context"]
 
@@ -67,6 +68,8 @@ Solvers = _types.SimpleNamespace(
     BVCEvaluationPoint=_bvc.EvaluationPoint,
     BVCEvaluationPoints=_bvc.EvaluationPoints,
     BoundaryValueCaching=_bvc.BoundaryValueCachingSolver,
+    RWSEvaluationPoints=_rws.EvaluationPoints,
+    ReverseWalkOnStars=_rws.ReverseWalkOnStarsSolver,
 )
 
 Samplers = _types.SimpleNamespace(
