@@ -53,6 +53,9 @@ WORKLOADS = {
     "bvc_laplace_2d": dict(fn=None, kw={}, desc="boundary value caching, 2D Laplace on a 4096-segment star "
                            "polygon: 65,536 boundary samples x 256 gradient walks, splat onto a 256x256 grid "
                            "(points at least 0.05 from the boundary)"),
+    "rws_mixed_2d": dict(fn=None, kw={}, desc="reverse Walk on Stars, 2D mixed Dirichlet/Neumann (4096-segment "
+                         "star polygon, f=-1): 32,768 absorbing + 32,768 reflecting + 65,536 domain samples, one "
+                         "walk each, splatting onto the 256x256 grid's interior points"),
     "screened_wos_3d_small": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=16384, spp=4),
                                   desc="profiling case: 3D screened WoS sigma=4, icosphere L8, 16384 points, 4 spp"),
 }
@@ -393,6 +396,72 @@ def run_bvc(args):
     print(json.dumps(line), flush=True)
 
 
+def run_rws(args):
+    """Reverse Walk on Stars: walk steps/s of the reverse-walk kernel (walks + per-step radius
+    searches + splats), and the oracle's walks on a bounded sample of the samples."""
+    from zombie_gb300 import bvc, rws
+    from zombie_gb300.runner import GpuProblem
+    Pm = P_mod()
+    pr = Pm.mixed_wost_2d(n_segments=4096, grid=256, spp=4)
+    gp = GpuProblem(pr)
+    inside = gp.queries.inside_domain
+    offset = 5e-3
+    sa = bvc.UniformLineSegmentBoundarySampler(*pr.absorbing, inside, seed=1)
+    sa.initialize(offset, False)
+    sr = bvc.UniformLineSegmentBoundarySampler(*pr.reflecting, lambda x: np.ones(len(x), bool), seed=2)
+    sr.initialize(0.0, False)
+    lo, hi = np.asarray(pr.domain_min[:2]), np.asarray(pr.domain_max[:2])
+    u = np.random.default_rng(9).uniform(lo, hi, (400000, 2)).astype(np.float32)
+    area = float(np.prod(hi - lo)) * float(np.mean(inside(u)))
+    sd = bvc.UniformDomainSampler(inside, lo, hi, area, seed=3)
+    solver = rws.ReverseWalkOnStarsSolver(gp.queries, sa, sr, sd)
+    solver.generate_samples(32768, 32768, 65536, offset, False)
+    ev = rws.EvaluationPoints(pr.points, dim=2)
+    for _ in range(max(args.warmup, 1)):
+        solver.solve(gp.pde, pr.settings, offset, 1e-3, 0.0, ev)
+    ev.reset()
+    solver.calls = 0
+    ms, steps = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            solver.solve(gp.pde, pr.settings, offset, 1e-3, 0.0, ev)
+            ms.append(sum(r.kernel_ms for r in solver.last_reports))
+            steps.append(sum(r.total_steps for r in solver.last_reports))
+    est = solver.get_estimated_solution(ev)
+    far = (gp.dist > 0.05) & (gp.queries.compute_dist_to_reflecting_boundary(pr.points) > 0.05)
+    err = est[far] - pr.exact()[far]
+    kernel_ms = float(np.median(ms))
+    value = float(np.median(steps)) / (kernel_ms / 1e3)
+    line = {"metric": "reverse walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 sums)", "data": "synthetic",
+            "config": {"workload": "rws_mixed_2d", "samples": len(solver.absorbing) + len(solver.reflecting) +
+                       len(solver.domain), "evaluation_points": int(len(ev)),
+                       "description": WORKLOADS["rws_mixed_2d"]["desc"]},
+            "walk_steps_per_call": float(np.median(steps)), "rmse_vs_exact": float(np.sqrt(np.mean(err ** 2))),
+            "u_std": float(np.std(pr.exact()[far])), "clocks": clk.summary(),
+            "gpu_launches": "3 reverse-walk launches + 3 point-tree builds per step"}
+    if not args.skip_cpu:
+        from oracle import oracle as O
+        m = 2048
+        c = solver.domain
+        mask = solver._contributions(gp.pde, pr.settings, c)
+        idx = np.nonzero(mask)[0][:m]
+        smp = {k: np.ascontiguousarray(getattr(c, k)[idx]) for k in
+               ("pt", "normal", "type", "estimate_normal_aligned", "pdf", "contribution", "dist_to_absorbing", "seed")}
+        ab = O.Boundary(2, *pr.absorbing)
+        rf = O.Boundary(2, *pr.reflecting, kind=pr.reflecting_kind, silhouette_precision=pr.ignore_silhouette_precision)
+        evd = dict(pt=ev.pt, normal=ev.normal, type=ev.type, totals=np.zeros_like(ev.totals))
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        st = O.rws_solve(2, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, smp, evd, offset, n_threads=threads)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": st / dt, "unit": "walk-steps/s", "cores": threads, "kind": "port",
+                                "sample": f"{len(idx)} domain samples' reverse walks ({st} steps, brute-force radius "
+                                          f"search over {len(ev)} points) in {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
 def P_mod():
     from zombie_gb300 import problems
     return problems
@@ -699,6 +768,8 @@ def main():
         run_cache_kernels(args)
     elif args.workload == "bvc_laplace_2d":
         run_bvc(args)
+    elif args.workload == "rws_mixed_2d":
+        run_rws(args)
     else:
         run_gpu(args)
 

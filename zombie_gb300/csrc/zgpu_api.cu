@@ -1206,9 +1206,11 @@ int zgpu_rws_solve(zgpu_context* ctx, const zgpu_geometric_queries* q, const zgp
     // the evaluation points' tree for the per-step radius searches
     float4* evalNodes = nullptr;
     int* evalOrder = nullptr;
+    int2* evalRanges = nullptr;
     int nEvalNodes = 0, evalDepth = 0;
-    cudaError_t e = buildPointBvhOnDevice(D, P.evalPt, (int)ne, s, &evalNodes, &nEvalNodes, &evalDepth, &evalOrder);
-    auto freeTree = [&]() { cudaFree(evalNodes); cudaFree(evalOrder); };
+    cudaError_t e = buildPointBvhOnDevice(D, P.evalPt, (int)ne, s, &evalNodes, &nEvalNodes, &evalDepth, &evalOrder,
+                                          &evalRanges);
+    auto freeTree = [&]() { cudaFree(evalNodes); cudaFree(evalOrder); cudaFree(evalRanges); };
     if (e != cudaSuccess) {
         freeTree();
         if (e == cudaErrorNotSupported) return fail(ZGPU_ERR_UNSUPPORTED, "evaluation-point tree too deep");
@@ -1216,6 +1218,7 @@ int zgpu_rws_solve(zgpu_context* ctx, const zgpu_geometric_queries* q, const zgp
     }
     P.evalNodes = evalNodes;
     P.evalOrder = evalOrder;
+    P.evalRanges = evalRanges;
     P.evalDepth = evalDepth;
     P.normalOffset = normal_offset_for_absorbing_boundary;
     P.radiusClamp = radius_clamp;

@@ -760,6 +760,18 @@ cudaError_t wideCones(const BinaryTree& t, ConeArrays item, const int* wideKids,
     return cudaSuccess;
 }
 
+// the contiguous range of sorted points behind every wide child (first, count): internal
+// binary nodes give their range, single items their position
+__global__ void childRangeKernel(const int* __restrict__ wideKids, int nWide, const BinNode* __restrict__ bin,
+                                 int2* __restrict__ ranges) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 4 * nWide) return;
+    const int r = wideKids[k];
+    int2 v = make_int2(0, 0);
+    if (r != kEmpty) v = r >= 0 ? make_int2(bin[r].first, bin[r].count) : make_int2(-r - 1, 1);
+    ranges[k] = v;
+}
+
 // points as zero-extent boxes (unit weight), with their bounds
 template <int D>
 __global__ void pointBoxKernel(const float* __restrict__ pts, int n, float4* __restrict__ lo, float4* __restrict__ hi,
@@ -784,8 +796,8 @@ cudaError_t initSceneKey(int* key, cudaStream_t s) {
 // A 4-wide BVH over n device-resident points for radius searches; order maps leaf slots to
 // point indices.
 cudaError_t buildPointBvhOnDevice(int D, const float* pts, int n, cudaStream_t s, float4** outNodes, int* outCount,
-                                  int* outDepth, int** outOrder) {
-    *outNodes = nullptr; *outCount = 0; *outDepth = 0; *outOrder = nullptr;
+                                  int* outDepth, int** outOrder, int2** outRanges) {
+    *outNodes = nullptr; *outCount = 0; *outDepth = 0; *outOrder = nullptr; *outRanges = nullptr;
     if (n <= 0) return cudaSuccess;
     const int T = 256, G = (n + T - 1) / T;
     DevBuf<float4> lo, hi;
@@ -798,8 +810,15 @@ cudaError_t buildPointBvhOnDevice(int D, const float* pts, int n, cudaStream_t s
     ZB(cudaGetLastError());
     BinaryTree tree;
     ZB(buildBinary(D, lo.p, hi.p, w.p, sceneKey.p, n, s, tree));
-    ZB(collapseWide(D, tree, lo.p, hi.p, w.p, s, outNodes, outCount, outDepth, nullptr));
+    DevBuf<int> kids;
+    ZB(collapseWide(D, tree, lo.p, hi.p, w.p, s, outNodes, outCount, outDepth, &kids.p));
+    DevBuf<int2> ranges;
+    ZB(ranges.alloc((size_t)4 * *outCount));
+    childRangeKernel<<<(4 * *outCount + T - 1) / T, T, 0, s>>>(kids.p, *outCount, tree.bin.p, ranges.p);
+    ZB(cudaGetLastError());
+    ZB(cudaStreamSynchronize(s));
     *outOrder = tree.ids.release();
+    *outRanges = ranges.release();
     return cudaSuccess;
 }
 

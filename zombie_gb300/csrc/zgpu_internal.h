@@ -174,7 +174,7 @@ cudaError_t launchPdeEvaluate(int D, const zgpu_pde& pde, int64_t n, const float
 // a 4-wide BVH over points (reverse walks' radius searches, zgpu_devbuild.cu): nodes as the
 // boundary trees', order[sorted slot] = point index; device arrays owned by the receiver
 cudaError_t buildPointBvhOnDevice(int D, const float* pts, int n, cudaStream_t s, float4** nodes, int* nNodes,
-                                  int* depth, int** order);
+                                  int* depth, int** order, int2** childRanges);
 
 // reverse Walk on Stars (zgpu_rws.cu)
 struct RwsParams {
@@ -196,6 +196,7 @@ struct RwsParams {
     double* totals;
     const float4* evalNodes;       // point BVH over the evaluation points
     const int* evalOrder;
+    const int2* evalRanges;        // per wide child: (first sorted slot, count)
     int evalDepth;
     float normalOffset, radiusClamp, regularization;
     int selfNormalize;
