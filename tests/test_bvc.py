@@ -238,3 +238,57 @@ def test_bvc_finite_differences_and_near_boundary_estimates(zgpu):
     near = ~far
     assert np.all(ev.count[near, A.ZGPU_BVC_SOURCE] == 1)
     assert np.sqrt(np.mean((ev.get_estimated_solution()[near] - ex[near]) ** 2)) < 0.1
+
+
+def _np_splat(dim, sigma, c, x, eval_type, radius_clamp, reg, robin_cutoff):
+    """splatBoundaryData / splatSourceData (boundary_value_caching.h:652-811) for one point in
+    FP64 numpy with scipy's Bessel functions: per-group running means of the solution."""
+    from scipy.special import erf, kv
+    mu = np.sqrt(sigma)
+    xy = x[None, :] - c["pt"].astype(np.float64)
+    r = np.maximum(radius_clamp, np.linalg.norm(xy, axis=1))
+    if sigma == 0:
+        G = -np.log(r) / (2 * np.pi) if dim == 2 else 1 / (4 * np.pi * r)
+        q = 1 / (2 * np.pi * r ** 2) if dim == 2 else 1 / (4 * np.pi * r ** 3)
+    else:
+        G = kv(0, mu * r) / (2 * np.pi) if dim == 2 else np.exp(-mu * r) / (4 * np.pi * r)
+        q = mu * kv(1, mu * r) / (2 * np.pi * r) if dim == 2 else mu * np.exp(-mu * r) * (1 + 1 / (mu * r)) / (4 * np.pi * r ** 2)
+    al = c["estimate_normal_aligned"] != 0
+    n = c["normal"].astype(np.float64) * np.where(al, -1.0, 1.0)[:, None]
+    Pk = np.sum(n * xy, axis=1) * q
+    if reg > 0:
+        rr = r / reg
+        gG = 1.0 if dim == 2 else erf(rr)
+        gP = 1 - np.exp(-rr ** 2) if dim == 2 else erf(rr) - 2 * rr * np.exp(-rr ** 2) / np.sqrt(np.pi)
+        G, Pk = G * gG, Pk * gP
+    alpha = 2.0 if eval_type in (1, 2) else 1.0
+    u, dn, h, k, pdf = (c[f].astype(np.float64) for f in ("solution", "normal_derivative", "contribution",
+                                                          "robin_coeff", "pdf"))
+    kk = np.where(k != 0, k, 1.0)
+    est = np.where(np.abs(k) > robin_cutoff, alpha * ((G + Pk / kk) * dn - Pk * h / kk) / pdf,
+                   np.where(np.abs(k) > 0, alpha * (G * h - (Pk + k * G) * u) / pdf, alpha * (G * dn - Pk * u) / pdf))
+    src = c["type"] == 0
+    est = np.where(src, alpha * G * h / pdf, est)
+    group = np.where(c["type"] == 1, np.where(al, 1, 0), np.where(c["type"] == 2, np.where(al, 3, 2), 4))
+    means = np.zeros(5)
+    for g in range(5):
+        if np.any(group == g):
+            means[g] = est[group == g].mean()
+    return means
+
+
+@pytest.mark.parametrize("dim,sigma,reg", [(2, 0.0, 0.0), (2, 1.5, 0.05), (3, 0.0, 0.02), (3, 2.0, 0.0)])
+def test_oracle_splat_matches_an_independent_restatement(oracle, dim, sigma, reg):
+    """The oracle's splat (the GPU kernel's checker) against a numpy restatement in FP64 with
+    scipy Bessel functions: every sample kind, normal-aligned samples, the three Robin cases,
+    boundary evaluation points (alpha = 2) and kernel regularisation."""
+    rng = np.random.default_rng(40 + dim + int(sigma))
+    c = _random_cache(dim, 400, rng, [1, 2, 0])
+    ev = _evals(dim, 60, rng)
+    ev["dist_to_absorbing"][:] = 1.0
+    ev["dist_to_reflecting"][:] = 1.0
+    oracle.bvc_splat(dim, sigma, c, ev, radius_clamp=1e-3, kernel_regularization=reg, robin_coeff_cutoff=2.0)
+    for i in range(60):
+        ref = _np_splat(dim, sigma, c, ev["pt"][i].astype(np.float64), ev["type"][i], 1e-3, reg, 2.0)
+        got = ev["mean"][i]
+        assert np.allclose(got, ref, rtol=2e-4, atol=2e-4 * np.abs(ref).max()), (i, got, ref)
