@@ -47,6 +47,7 @@ struct RevState {
 // alpha * throughput * G / pdf * contribution by FP64 atomic add.
 struct Ball {
     float R, thr, pdf, contrib;
+    float visible2;        // squared distance within which no reflecting point lies (no test needed)
     int group;
     bool onRefl, toPoisson, needTest, yukawa;
 };
@@ -88,9 +89,10 @@ ZG_D void coopSplat(const RwsParams& P, const V<D>& x, const V<D>& nrm, const Ba
                 if (!(d2 < R2)) continue;
                 const int te = P.evalType ? P.evalType[e] : ZGPU_SAMPLE_IN_DOMAIN;
                 if (te == ZGPU_SAMPLE_ON_ABSORBING_BOUNDARY) continue;      // not splatted
-                if (b.needTest) {
+                if (b.needTest && !(d2 < b.visible2)) {
                     // intersectsWithReflectingBoundary: the segment between the points, each
-                    // offset off the reflecting boundary when it lies on it
+                    // offset off the reflecting boundary when it lies on it (a segment shorter
+                    // than the distance to the reflecting boundary cannot cross it)
                     const V<D> p1 = b.onRefl ? offsetPoint<D>(x, -nrm) : x;
                     V<D> p2 = xe;
                     if (te == ZGPU_SAMPLE_ON_REFLECTING_BOUNDARY && P.evalNormal)
@@ -221,6 +223,7 @@ __global__ void __launch_bounds__(kRwsThreads) reverseWalkKernel(const __grid_co
         Ball b;
         b.R = 0.0f; b.thr = s.thr; b.pdf = pdf; b.contrib = contrib; b.group = group;
         b.onRefl = s.onRefl; b.toPoisson = toPoisson; b.needTest = false; b.yukawa = g.yukawa;
+        b.visible2 = 0.0f;
         if (haveState) {
             if (!(dist > ws.epsilon_shell_for_absorbing_boundary)) {
                 haveState = false;                                              // reached the boundary
@@ -248,8 +251,13 @@ __global__ void __launch_bounds__(kRwsThreads) reverseWalkKernel(const __grid_co
                 b.onRefl = s.onRefl;
                 b.yukawa = g.yukawa;
                 // line of sight needs testing only when the reflecting boundary reaches into the
-                // ball (segments inside a ball no reflecting point enters cannot cross it)
-                b.needTest = P.sc.hasRefl && (s.onRefl || closestPoint<D>(P.sc.reflecting, s.pt, S, err).d < R);
+                // ball (segments inside a ball no reflecting point enters cannot cross it), and
+                // then only for points farther than the closest reflecting point (0.1% margin)
+                if (P.sc.hasRefl) {
+                    const float dRefl = s.onRefl ? 0.0f : closestPoint<D>(P.sc.reflecting, s.pt, S, err).d;
+                    b.needTest = s.onRefl || dRefl < R;
+                    b.visible2 = b.needTest ? (0.999f * dRefl) * (0.999f * dRefl) : 0.0f;
+                }
                 pending = true;
             }
         }
@@ -269,6 +277,7 @@ __global__ void __launch_bounds__(kRwsThreads) reverseWalkKernel(const __grid_co
             bb.thr = __shfl_sync(0xffffffffu, b.thr, src);
             bb.pdf = __shfl_sync(0xffffffffu, b.pdf, src);
             bb.contrib = __shfl_sync(0xffffffffu, b.contrib, src);
+            bb.visible2 = __shfl_sync(0xffffffffu, b.visible2, src);
             bb.group = __shfl_sync(0xffffffffu, b.group, src);
             const int flags = __shfl_sync(0xffffffffu, (int)b.onRefl | ((int)b.toPoisson << 1) | ((int)b.needTest << 2) |
                                                            ((int)b.yukawa << 3), src);
