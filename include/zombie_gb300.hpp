@@ -224,6 +224,7 @@ struct SamplePoint {
 };
 
 template <typename T, size_t DIM> class WalkSolverBase;
+namespace detail { struct StatsAccess; }   // marshals moments for the variance reduction layer
 
 // SampleStatistics (point_estimation/common.h:199-390): the same running moments and getters.
 // The device accumulates in FP64; the getters return T.
@@ -292,6 +293,7 @@ public:
 
 protected:
     friend class WalkSolverBase<T, DIM>;
+    friend struct detail::StatsAccess;
     static void update(double estimate, double& mean, double& M2, int N) {
         double delta = estimate - mean;
         mean += delta / N;

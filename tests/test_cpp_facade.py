@@ -1,5 +1,7 @@
-"""The C++ host interface (include/zombie_gb300.hpp): compiles for 2D and 3D instantiations of
-the reference's class names on any machine, and on the GPU runs the facade driver
+"""The C++ host interfaces (include/zombie_gb300.hpp, include/zombie_gb300_variance_reduction.hpp):
+compile for 2D and 3D instantiations of the reference's class names on any machine; on the GPU
+the variance reduction driver (tests/cpp/facade_vr_2d.cpp: samplers, boundary value caching,
+reverse Walk on Stars with and without a source) runs, and so does the facade driver
 (tests/cpp/facade_solve_2d.cpp: WoS and WoSt solves, progressive solves, gradients, dense
 grids, callback rejection, host queries) and replays its mixed Dirichlet / Neumann solve
 through the Python interface with the same seeds: both host sides reach the same estimates."""
@@ -17,10 +19,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 DRIVER = os.path.join(HERE, "cpp", "facade_solve_2d.cpp")
+DRIVER_VR = os.path.join(HERE, "cpp", "facade_vr_2d.cpp")
 
 INSTANTIATIONS_3D = r"""
-#include "zombie_gb300.hpp"
+#include "zombie_gb300_variance_reduction.hpp"
 namespace zg = zombie_gb300;
+template class zg::UniformTriangleBoundarySampler<float>;
+template class zg::UniformDomainSampler<float, 3>;
+template class zg::bvc::BoundaryValueCaching<float, 3>;
+template class zg::bvc::BoundaryValueCachingSolver<float, 3>;
+template struct zg::bvc::EvaluationPoint<float, 3>;
+template class zg::rws::ReverseWalkOnStarsSolver<float, 3>;
+template struct zg::rws::EvaluationPoint<float, 3>;
 template class zg::WalkOnSpheres<float, 3>;
 template class zg::WalkOnStars<float, 3>;
 template struct zg::GeometricQueries<3>;
@@ -56,7 +66,7 @@ def test_facade_compiles_for_2d_and_3d(tmp_path):
     gxx = _gxx()
     src = tmp_path / "inst3d.cpp"
     src.write_text(INSTANTIATIONS_3D)
-    for f in (DRIVER, str(src)):
+    for f in (DRIVER, DRIVER_VR, str(src)):
         r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-I", INCLUDE, f],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
@@ -128,3 +138,15 @@ def test_facade_driver_and_python_replay(zgpu, tmp_path):
     assert np.array_equal(count_py, count_cpp)
     # the C++ getters return float; the walks themselves are the same
     assert np.allclose(mean_py, mean_cpp, rtol=1e-6, atol=1e-6), np.abs(mean_py - mean_cpp).max()
+
+
+@pytest.mark.gpu
+def test_variance_reduction_facade_driver(zgpu, tmp_path):
+    from zombie_gb300.build import LIBDIR
+    gxx = _gxx()
+    exe = str(tmp_path / "facade_vr_2d")
+    _compile(gxx, DRIVER_VR, exe, LIBDIR)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=900)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "variance reduction facade ok" in r.stdout
