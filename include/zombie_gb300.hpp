@@ -79,7 +79,11 @@ inline void check(int status) {
 // One CUDA device context (stream, scratch buffers); shared by handlers and solvers.
 class Context {
 public:
-    explicit Context(int device = 0) { check(zgpu_context_create(device, &h_)); }
+    explicit Context(int device = 0) {
+        if (zgpu_abi_version() != ZGPU_ABI_VERSION)
+            throw Error(ZGPU_ERR_UNSUPPORTED, "libzgpu was built for another zgpu.h (ABI version mismatch)");
+        check(zgpu_context_create(device, &h_));
+    }
     ~Context() { if (h_) zgpu_context_destroy(h_); }
     Context(const Context&) = delete;
     Context& operator=(const Context&) = delete;

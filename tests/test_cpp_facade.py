@@ -47,9 +47,43 @@ int main() {
     zg::PDE<float, 3> pde;
     pde.source = zg::getDenseGridCallback0(g);
     zg::WalkSettings ws(1e-3f, 1e-3f, 1024, false);
-    return (a.getSolutionEstimateCount() == 3 && a.getEstimatedSolution() == 3.0f &&
-            a.getEstimatedSolutionVariance() == 4.0f && pde.toC().source_kind == ZGPU_FIELD_GRID &&
-            ws.toC().max_walk_length == 1024) ? 0 : 1;
+    int bad = !(a.getSolutionEstimateCount() == 3 && a.getEstimatedSolution() == 3.0f &&
+                a.getEstimatedSolutionVariance() == 4.0f && pde.toC().source_kind == ZGPU_FIELD_GRID &&
+                ws.toC().max_walk_length == 1024 && ws.toC().steps_before_using_maximal_spheres == 1024);
+    // a unit cube's 12 triangles: sample counts split by side, validation of the inputs
+    std::vector<zg::Vector3> v;
+    for (int i = 0; i < 8; i++) v.push_back(zg::Vector3(i & 1, (i >> 1) & 1, (i >> 2) & 1));
+    const int f[12][3] = {{0,2,1},{1,2,3},{4,5,6},{5,7,6},{0,1,4},{1,5,4},{2,6,3},{3,6,7},{0,4,2},{2,4,6},{1,3,5},{3,7,5}};
+    std::vector<zg::Vectori<3>> t;
+    for (auto& q : f) t.push_back(zg::Vectori<3>(q[0], q[1], q[2]));
+    auto all = [](const zg::Vector3&) { return true; };
+    zg::UniformTriangleBoundarySampler<float> s(v, t, {}, {}, all, false, 5);
+    s.initialize(0.0f, false);
+    bad += !(s.getSampleCount(100) == 100 && s.getSampleCount(100, true) == 0);
+    s.initialize(0.0f, true);
+    bad += !(s.getSampleCount(100) == 50 && s.getSampleCount(100, true) == 50);
+    auto none = [](const zg::Vector3&) { return false; };
+    zg::UniformTriangleBoundarySampler<float> empty(v, t, {}, {}, none, false, 5);
+    empty.initialize(0.0f, false);
+    bad += empty.getSampleCount(100) != 0;
+    auto throwsInvalid = [](auto fn) {
+        try { fn(); } catch (const zg::Error& e) { return e.status() == ZGPU_ERR_INVALID_ARG; }
+        return false;
+    };
+    bad += !throwsInvalid([&] { zg::UniformTriangleBoundarySampler<float>(v, t, std::vector<float>(12, -1.0f), {}, all); });
+    bad += !throwsInvalid([&] { zg::UniformTriangleBoundarySampler<float>(v, t, std::vector<float>(3, 1.0f), {}, all); });
+    bad += !throwsInvalid([&] { zg::DenseGrid<3>(std::vector<float>(7), zg::Vectori<3>(2, 2, 2), zg::Vector3(), zg::Vector3(1, 1, 1)); });
+    // reverse-walk evaluation point: self-normalised absorbing part + per-count other parts
+    zg::rws::EvaluationPoint<float, 3> e(zg::Vector3(), zg::Vector3(), zg::SampleType::InDomain, 1.0f, 1.0f);
+    e.totalAbsorbingBoundaryContribution = 6.0; e.totalPoissonKernelContribution = 3.0; e.totalSourceContribution = 4.0;
+    bad += e.getEstimatedSolution(10, 0, 0, 0, 8) != 2.5f;
+    e.totalPoissonKernelContribution = 0.0;
+    bad += e.getEstimatedSolution(10, 0, 0, 0, 8) != 1.1f;
+    zg::bvc::EvaluationPoint<float, 3> ep(zg::Vector3(), zg::Vector3(), zg::SampleType::InDomain, 1.0f, 1.0f);
+    std::vector<float> grad;
+    ep.getEstimatedGradient(grad);
+    bad += !(ep.getEstimatedSolution() == 0.0f && grad.size() == 3 && grad[2] == 0.0f);
+    return bad ? 1 : 0;
 }
 """
 
@@ -81,7 +115,10 @@ def _compile(gxx, src, out, lib_dir):
 def test_facade_host_classes_run_without_a_gpu(tmp_path):
     """Linked against the library, the 3D instantiations run their host-only parts (no
     context is created): SampleStatistics::merge (Chan et al.) gives the pooled mean 3 and
-    variance 4 of {1, 3, 5}; a DenseGrid becomes a grid field; settings carry over."""
+    variance 4 of {1, 3, 5}; a DenseGrid becomes a grid field; settings carry over; a cube's
+    triangle sampler splits sample counts by side and keeps none outside the solve region;
+    negative or missing primitive weights and mis-sized grids throw INVALID_ARG; the
+    reverse-walk evaluation point self-normalises its absorbing part."""
     from zombie_gb300 import build
     build.build()
     LIBDIR = build.LIBDIR
