@@ -135,8 +135,9 @@ def test_reverse_walks_3d_match_the_oracle_and_the_solution(zgpu, oracle):
 
     With absorption (sigma > 0) ReverseWalkOnStarsSolver does not self-normalise, and the plain
     estimate of the absorbing part reads walks absorbed in the epsilon shell as reaching the
-    boundary: for g = 1 it gives about 0.88 at an offset of 5e-3 (0.93 at 1e-2), on the GPU and
-    in the oracle alike, so the end-to-end check uses sigma = 0."""
+    boundary (for g = 1 without the normalisation the oracle reads about 0.88 at an offset of
+    5e-3 with a 1e-3 shell); the screened solve's bias (-0.09) is the same on the GPU and in
+    the oracle, so the end-to-end check uses sigma = 0."""
     from zombie_gb300 import bvc, rws
     from zombie_gb300.runner import GpuProblem
     pr = P.screened_wos_3d(level=4, n_points=300, spp=4, sigma=0.0)
