@@ -18,6 +18,7 @@ from .api import (BranchTraversalWeight, Context, DenseGrid, EstimationQuantity,
                   populate_geometric_queries_for_neumann_boundary, populate_geometric_queries_for_robin_boundary)
 from ._lib import ZgpuError
 from . import bvc as _bvc
+from . import api as _api
 from . import io as _io
 from . import rws as _rws
 
@@ -42,6 +43,26 @@ def _solver_factory(cls):
     return factory
 
 
+def _list_factory(*args, dim=None, channels=1):
+    return list(*args)
+
+
+def _load_boundary_mesh(obj_file, positions=None, indices=None, dim=None):
+    """load_boundary_mesh(obj_file, positions, indices, dim=...) filling the two lists as the
+    reference does, or load_boundary_mesh(obj_file, dim) returning arrays."""
+    if isinstance(positions, int) and dim is None:
+        dim, positions = positions, None
+    p, i = _io.load_boundary_mesh(obj_file, dim)
+    return _io._fill(positions, p), _io._fill(indices, i)
+
+
+def _load_textured_boundary_mesh(obj_file, positions=None, texture_coordinates=None, indices=None,
+                                 texture_indices=None, dim=3):
+    if dim != 3:
+        raise ValueError("load_textured_boundary_mesh is only supported for dim=3")
+    return _io.load_textured_boundary_mesh(obj_file, positions, texture_coordinates, indices, texture_indices)
+
+
 Core = _types.SimpleNamespace(
     PDE=_dim_factory(PDE),
     GeometricQueries=_dim_factory(GeometricQueries),
@@ -51,6 +72,8 @@ Core = _types.SimpleNamespace(
     get_constant_robin_callback=lambda value, value_aligned=None, dim=None, channels=1: Field.constant(value, value_aligned),
     get_constant_robin_coefficient_callback=lambda value, value_aligned=None, dim=None: Field.constant(value, value_aligned),
     get_analytic_callback=lambda dim=None, channels=1: Field.analytic(),
+    get_constant_indicator_callback=_api.get_constant_indicator_callback,
+    IntersectionPoint=_dim_factory(_api.IntersectionPoint),
 )
 
 Solvers = _types.SimpleNamespace(
@@ -69,7 +92,16 @@ Solvers = _types.SimpleNamespace(
     BVCEvaluationPoints=_bvc.EvaluationPoints,
     BoundaryValueCaching=_bvc.BoundaryValueCachingSolver,
     RWSEvaluationPoints=_rws.EvaluationPoints,
+    RWSEvaluationPoint=_rws.EvaluationPoint,
     ReverseWalkOnStars=_rws.ReverseWalkOnStarsSolver,
+    # the reference's bound std::vector types are Python lists here
+    SamplePointList=_list_factory,
+    SampleStatisticsList=_list_factory,
+    BVCEvaluationPointList=_list_factory,
+    RWSEvaluationPointList=_list_factory,
+    # empty host callbacks (the solvers accept None and reject any non-empty callback)
+    get_empty_walk_state_callback=lambda dim=None, channels=1: None,
+    get_empty_terminal_contribution_callback=lambda dim=None, channels=1: None,
 )
 
 Samplers = _types.SimpleNamespace(
@@ -82,7 +114,22 @@ Samplers = _types.SimpleNamespace(
 
 Utils = _types.SimpleNamespace(
     DenseGrid=_dim_factory(DenseGrid),
-    load_boundary_mesh=_io.load_boundary_mesh,
+    FloatDenseGrid=_dim_factory(DenseGrid),
+    BoolDenseGrid=_api.bool_dense_grid,
+    get_dense_grid_indicator_callback=_api.get_dense_grid_indicator_callback,
+    load_boundary_mesh=_load_boundary_mesh,
+    load_textured_boundary_mesh=_load_textured_boundary_mesh,
+    build_bounding_box_mesh=lambda bounding_box_min, bounding_box_max, positions=None, indices=None, dim=None:
+        _io.build_bounding_box_mesh(bounding_box_min, bounding_box_max, positions, indices),
+    add_bounding_box_to_boundary_mesh=lambda bounding_box_min, bounding_box_max, positions, indices, dim=None:
+        _io.add_bounding_box_to_boundary_mesh(bounding_box_min, bounding_box_max, positions, indices),
+    compute_signed_volume=lambda boundary_positions, boundary_indices, dim=None:
+        _io.compute_signed_volume(boundary_positions, boundary_indices),
+    compute_dist_to_boundary=_api.compute_dist_to_boundary,
+    partition_boundary_mesh=lambda on_reflecting_boundary, positions, indices, *out, dim=None:
+        _io.partition_boundary_mesh(on_reflecting_boundary, positions, indices, *out),
+    get_spatially_sorted_point_indices=lambda points, out_indices=None, dim=None:
+        _io.get_spatially_sorted_point_indices(points, out_indices),
     write_boundary_mesh=_io.write_boundary_mesh,
     normalize=_io.normalize,
     apply_shift=_io.apply_shift,

@@ -294,6 +294,66 @@ def get_dense_grid_robin_coefficient_callback(*args, **kw):
     return _dense_grid_field(args, kw, aligned=True)
 
 
+class _Indicator:
+    """A host-side boolean field of points (the reference's FloatNToTypeFunc<bool, DIM>):
+    called with one point it returns a bool, with an [N, dim] array a bool array.  Used
+    where the reference takes an indicator on the host, e.g. PDE.has_reflecting_boundary_conditions
+    or the on_reflecting_boundary argument of partition_boundary_mesh."""
+
+    def __init__(self, fn):
+        self._fn = fn
+
+    def __call__(self, x):
+        x = np.asarray(x, np.float32)
+        if x.ndim == 1:
+            return bool(self._fn(x[None])[0])
+        return np.asarray(self._fn(x), bool)
+
+
+def get_constant_indicator_callback(value, dim=None):
+    """get_constant_indicator_callback (python/zombie_bindings.h:843-849)."""
+    v = bool(value)
+    return _Indicator(lambda x: np.full(x.shape[0], v, bool))
+
+
+def get_dense_grid_indicator_callback(*args, **kw):
+    """get_dense_grid_indicator_callback (python/zombie_bindings.h:852-862): nearest-cell lookup
+    of a boolean DenseGrid, or of raw boolean data with its shape, min and max."""
+    kw.pop("dim", None)
+    if args and isinstance(args[0], DenseGrid):
+        g = args[0]
+    else:
+        args = list(args)
+        data = args.pop(0) if args else kw.pop("grid_data")
+        shape = args.pop(0) if args else kw.pop("grid_shape")
+        gmin = args.pop(0) if args else kw.pop("grid_min")
+        gmax = args.pop(0) if args else kw.pop("grid_max")
+        g = DenseGrid(np.asarray(data, bool).astype(np.float32), shape, gmin, gmax, False)
+    return _Indicator(lambda x: np.asarray(g(x)) > 0.5)
+
+
+def bool_dense_grid(*args, dim=None, **kw):
+    """DenseGrid<bool, 1, DIM> (utils/dense_grid.h): a DenseGrid holding 0 / 1, looked up by
+    nearest cell (no interpolation)."""
+    if len(args) >= 4:
+        args = (np.asarray(args[0], bool).astype(np.float32),) + tuple(args[1:4])
+    kw.pop("enable_interpolation", None)
+    return DenseGrid(*args[:4] if len(args) >= 4 else args[:2], enable_interpolation=False, dim=dim)
+
+
+class IntersectionPoint:
+    """IntersectionPoint<DIM> (core/geometric_queries.h:29-41): a boundary point, its normal
+    and its distance along the query (FLT_MAX when nothing was hit)."""
+
+    def __init__(self, pt=None, normal=None, dist=None, dim=2):
+        self.pt = np.zeros(dim, np.float32) if pt is None else np.asarray(pt, np.float32)
+        self.normal = np.zeros(dim, np.float32) if normal is None else np.asarray(normal, np.float32)
+        self.dist = float(np.finfo(np.float32).max if dist is None else dist)
+
+    def __repr__(self):
+        return f"IntersectionPoint(pt={self.pt.tolist()}, normal={self.normal.tolist()}, dist={self.dist})"
+
+
 class PDE:
     """PDE<T,DIM> (core/pde.h:19-45)."""
 
@@ -310,6 +370,9 @@ class PDE:
         self.robin = Field.zero()
         self.robin_coeff = Field.zero()
         self.grid_memory = A.ZGPU_MEM_HOST   # where raw zgpu_grid values live (DenseGrid data is host)
+        # host-side indicator of points with reflecting conditions (PDE::hasReflectingBoundaryConditions,
+        # core/pde.h:44); the walks take the reflecting boundary from the geometric queries
+        self.has_reflecting_boundary_conditions = None
 
     def has_non_zero_robin_coeff(self, x=None):
         """PDE::hasNonZeroRobinCoeff (core/pde.h:62-78) at x (grids need x)."""
@@ -822,6 +885,21 @@ class GeometricQueries:
     def outside_bounding_domain(self, x):
         x = np.asarray(x).reshape(-1, self.dim)
         return np.any((x < self.domain_min) | (x > self.domain_max), axis=1)
+
+
+def compute_dist_to_boundary(geometric_queries, solve_locations, dist_to_absorbing_boundary=None,
+                             dist_to_reflecting_boundary=None, dim=None):
+    """compute_dist_to_boundary (python/zombie_bindings.h:732-749): unsigned distances of the
+    solve locations to the absorbing and the reflecting boundary (batched on the device).
+    Fills the output lists when given; returns both as arrays."""
+    x = np.asarray(solve_locations, np.float32).reshape(-1, geometric_queries.dim)
+    da = np.asarray(geometric_queries.compute_dist_to_absorbing_boundary(x), np.float32)
+    dr = np.asarray(geometric_queries.compute_dist_to_reflecting_boundary(x), np.float32)
+    for out, v in ((dist_to_absorbing_boundary, da), (dist_to_reflecting_boundary, dr)):
+        if out is not None:
+            out.clear()
+            out.extend(float(t) for t in v)
+    return da, dr
 
 
 def populate_geometric_queries_for_dirichlet_boundary(handler, geometric_queries, dim=None):

@@ -13,6 +13,7 @@ import math
 import numpy as np
 
 from . import _abi as A
+from . import io as _io
 
 
 # ----------------------------------------------------------------------------- meshes
@@ -139,22 +140,7 @@ def bounding_box(positions, make_square=True, scale=1.0):
 
 def partition_boundary_mesh(on_reflecting, positions, indices):
     """partitionBoundaryMesh (utils/fcpw_geometric_queries.h:460-510): split by primitive midpoint."""
-    positions = np.asarray(positions)
-    indices = np.asarray(indices)
-    dim = positions.shape[1]
-    mids = positions[indices].mean(1)
-    refl = np.asarray(on_reflecting(mids), bool)
-    out = []
-    for mask in (~refl, refl):
-        sub = indices[mask]
-        if sub.size == 0:
-            out.append((np.zeros((0, dim), np.float32), np.zeros((0, dim), np.int32)))
-            continue
-        uniq, inv = np.unique(sub.reshape(-1), return_inverse=True)
-        new_pos = positions[uniq]
-        new_idx = inv.reshape(sub.shape)
-        out.append((new_pos.astype(np.float32), new_idx.astype(np.int32)))
-    return out[0], out[1]
+    return _io.partition_boundary_mesh(on_reflecting, positions, indices)
 
 
 # ------------------------------------------------------------------ manufactured solutions

@@ -70,6 +70,47 @@ class EvaluationPoints:
         return e
 
 
+class EvaluationPoint:
+    """One rws::EvaluationPoint (reverse_walk_solver.h:19-45, :120-178): its running sums
+    (total_absorbing_boundary_contribution, ..., total_poisson_kernel_contribution) and
+    get_estimated_solution(n_absorbing, n_absorbing_aligned, n_reflecting, n_reflecting_aligned,
+    n_source).  Lists of these go through ReverseWalkOnStarsSolver.solve like EvaluationPoints."""
+
+    _TOTALS = {"total_absorbing_boundary_contribution": A.ZGPU_RWS_ABSORBING,
+               "total_absorbing_boundary_normal_aligned_contribution": A.ZGPU_RWS_ABSORBING_ALIGNED,
+               "total_reflecting_boundary_contribution": A.ZGPU_RWS_REFLECTING,
+               "total_reflecting_boundary_normal_aligned_contribution": A.ZGPU_RWS_REFLECTING_ALIGNED,
+               "total_source_contribution": A.ZGPU_RWS_SOURCE,
+               "total_poisson_kernel_contribution": A.ZGPU_RWS_POISSON_KERNEL}
+
+    def __init__(self, pt, normal, type, dist_to_absorbing_boundary, dist_to_reflecting_boundary):
+        self._pts = EvaluationPoints(np.asarray(pt, np.float32)[None], np.asarray(normal, np.float32)[None],
+                                     [int(type)], [dist_to_absorbing_boundary], [dist_to_reflecting_boundary])
+        self.pt, self.normal, self.type = self._pts.pt[0], self._pts.normal[0], SampleType(int(type))
+        self.dist_to_absorbing_boundary = float(dist_to_absorbing_boundary)
+        self.dist_to_reflecting_boundary = float(dist_to_reflecting_boundary)
+
+    def __getattr__(self, name):
+        if name in EvaluationPoint._TOTALS:
+            return float(self._pts.totals[0, EvaluationPoint._TOTALS[name]])
+        raise AttributeError(name)
+
+    def get_estimated_solution(self, n_absorbing, n_absorbing_aligned, n_reflecting, n_reflecting_aligned, n_source):
+        return float(self._pts.get_estimated_solution(n_absorbing, n_absorbing_aligned, n_reflecting,
+                                                      n_reflecting_aligned, n_source)[0])
+
+    def reset(self):
+        self._pts.reset()
+
+
+def _gather(points):
+    ev = EvaluationPoints(np.array([p.pt for p in points]), np.array([p.normal for p in points]),
+                          [int(p.type) for p in points], [p.dist_to_absorbing_boundary for p in points],
+                          [p.dist_to_reflecting_boundary for p in points], dim=points[0].pt.shape[0])
+    ev.totals[:] = np.concatenate([p._pts.totals for p in points])
+    return ev
+
+
 class ReverseWalkOnStarsSolver:
     """ReverseWalkOnStarsSolver<T,DIM> (reverse_walk_solver.h:47-118, :168-372)."""
 
@@ -136,8 +177,13 @@ class ReverseWalkOnStarsSolver:
     def solve(self, pde, walk_settings, normal_offset_for_absorbing_boundary, radius_clamp, kernel_regularization,
               evaluation_points, updated_eval_pt_locations=True, run_single_threaded=False, report_progress=None):
         """solve (reverse_walk_solver.h:304-338): one reverse walk per sample, progressive over
-        calls (call k draws pcg32 stream k of every sample)."""
-        ev = evaluation_points
+        calls (call k draws pcg32 stream k of every sample).  evaluation_points: EvaluationPoints
+        or a list of EvaluationPoint."""
+        listed = isinstance(evaluation_points, (list, tuple))
+        if listed and len(evaluation_points) == 0:
+            self.calls += 1
+            return
+        ev = _gather(evaluation_points) if listed else evaluation_points
         p = pde.to_c()
         ws = walk_settings.to_c() if hasattr(walk_settings, "to_c") else walk_settings
         q = self.queries.to_c()
@@ -171,6 +217,9 @@ class ReverseWalkOnStarsSolver:
             if not walk_settings.ignore_absorbing_boundary_contribution:
                 g = pde_evaluate(pde, ev.pt[on_abs], dim=self.dim, context=self.ctx)[1]
             ev.totals[on_abs, A.ZGPU_RWS_ABSORBING] = g
+        if listed:
+            for i, p in enumerate(evaluation_points):
+                p._pts.totals[0] = ev.totals[i]
 
     def get_absorbing_boundary_sample_pts(self, return_boundary_normal_aligned=False):
         return self.absorbing_aligned if return_boundary_normal_aligned else self.absorbing
@@ -194,6 +243,11 @@ class ReverseWalkOnStarsSolver:
         """The evaluation points' solution with this solver's sample counts times the number of
         solve calls whose walks the points accumulated."""
         k = max(self.calls, 1)
+        if isinstance(evaluation_points, (list, tuple)):
+            n = (k * self.get_absorbing_boundary_sample_count(), k * self.get_absorbing_boundary_sample_count(True),
+                 k * self.get_reflecting_boundary_sample_count(), k * self.get_reflecting_boundary_sample_count(True),
+                 k * self.get_domain_sample_count())
+            return [p.get_estimated_solution(*n) for p in evaluation_points]
         return evaluation_points.get_estimated_solution(
             k * self.get_absorbing_boundary_sample_count(), k * self.get_absorbing_boundary_sample_count(True),
             k * self.get_reflecting_boundary_sample_count(), k * self.get_reflecting_boundary_sample_count(True),
