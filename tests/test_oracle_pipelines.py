@@ -1,6 +1,7 @@
-"""The oracle's 3D boundary value caching and reverse Walk on Stars end to end on the CPU
-(displaced icosphere, level 4), with the host samplers of zombie_gb300.bvc and the oracle's own
-closest-point queries: the estimates recover manufactured solutions, and two FP32 / estimator
+"""The oracle's boundary value caching and reverse Walk on Stars end to end on the CPU (a 2D star
+polygon and a 3D displaced icosphere, level 4), with the host samplers of zombie_gb300.bvc and
+the oracle's own closest-point queries: the estimates (and the splatted gradients) recover
+manufactured solutions, and two FP32 / estimator
 properties of the reference's algorithm that the 3D GPU tests are configured around are pinned:
 
 * the 3D Yukawa ball evaluates I_{3/2}(mu R) as cosh(mu R) - sinh(mu R) / (mu R)
@@ -161,3 +162,60 @@ def test_oracle_unnormalised_reverse_estimate_ends_walks_in_the_epsilon_shell(or
         means[eps] = float((t[:, A.ZGPU_RWS_ABSORBING] / len(a))[far].mean())
     assert means[1e-4] - means[1e-3] > 0.04, means
     assert abs(means[1e-4] - 1.0) < 0.06, means
+
+
+def test_oracle_bvc_laplace_2d_splats_values_and_gradients(oracle):
+    """u = e^x cos y on the 1024-segment star polygon: 8192 boundary samples offset 1e-3 with
+    256 walks each for u and du/dn; the splat recovers u and grad u at interior grid points."""
+    from zombie_gb300 import bvc
+    pos, idx = P.star_polygon(1024)
+    ob = oracle.Boundary(2, pos, idx)
+
+    def inside(x):
+        return P.polygon_inside_and_radius(np.asarray(x, np.float64), pos)[0]
+
+    class Q2(_Queries):
+        dim = 2
+    q = Q2(ob, inside)
+    pde = P.make_pde(P.solution_expcos(0.0), source=False)
+    ws = P.default_walk_settings(eps_abs=1e-3, max_len=1024)
+    s = bvc.UniformLineSegmentBoundarySampler(pos, idx, inside, seed=11)
+    s.initialize(1e-3, False)
+    c = s.generate_samples(8192, int(SampleType.OnAbsorbingBoundary), 1e-3, q, False)
+    n = len(c)
+    pts = dict(pt=c.pt, normal=c.normal, type=c.type, estimation_quantity=np.full(n, 1, np.int32),
+               dist_to_absorbing=c.dist_to_absorbing, dist_to_reflecting=c.dist_to_reflecting,
+               n_walks=np.full(n, 256, np.int32), seed=c.seed, first_sphere_radius=np.zeros(n, np.float32),
+               direction_for_derivative=np.ascontiguousarray(c.normal))
+    st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
+              total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64),
+              gradient_mean=np.zeros((n, 2)), gradient_m2=np.zeros((n, 2)), n_gradient_estimates=np.zeros(n, np.int32),
+              total_first_source_contribution=np.zeros(n), total_derivative_contribution=np.zeros(n))
+    oracle.solve(A.ZGPU_SOLVER_WALK_ON_STARS, 2, ob, None, np.array([-1.3, -1.3]), np.array([1.3, 1.3]), pde, ws,
+                 pts, st)
+    c.solution[:] = st["solution_mean"]
+    c.normal_derivative[:] = st["total_derivative_contribution"] / np.maximum(st["n_solution_estimates"], 1)
+    g = (np.arange(24) + 0.5) / 24 * 2.6 - 1.3
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    grid = np.stack([X.ravel(), Y.ravel()], 1).astype(np.float32)
+    grid = grid[inside(grid)]
+    dist = ob.closest_point(grid)[2]
+    m = len(grid)
+    ev = dict(pt=np.ascontiguousarray(grid), type=np.zeros(m, np.int32), dist_to_absorbing=dist.astype(np.float32),
+              dist_to_reflecting=np.full(m, np.finfo(np.float32).max, np.float32), mean=np.zeros((m, 5)),
+              m2=np.zeros((m, 5)), count=np.zeros((m, 5), np.int32), gradient_mean=np.zeros((m, 5, 2)),
+              gradient_m2=np.zeros((m, 5, 2)))
+    smp = {k: np.ascontiguousarray(getattr(c, k)) for k in ("pt", "normal", "pdf", "type", "estimate_normal_aligned",
+                                                            "solution", "normal_derivative", "contribution",
+                                                            "robin_coeff")}
+    oracle.bvc_splat(2, 0.0, smp, ev, radius_clamp=1e-3, cutoff_absorbing=0.05)
+    far = dist >= 0.05
+    x = grid[far].astype(np.float64)
+    u = np.exp(x[:, 0]) * np.cos(x[:, 1])
+    gu = np.stack([u, -np.exp(x[:, 0]) * np.sin(x[:, 1])], 1).ravel()
+    est = ev["mean"].sum(1)[far]
+    ge = ev["gradient_mean"].sum(1)[far].ravel()
+    assert np.all(ev["count"][~far] == 0)
+    assert np.sqrt(np.mean((est - u) ** 2)) < 0.1 * np.std(u) + 0.02
+    assert np.sqrt(np.mean((ge - gu) ** 2)) < 0.25 * np.std(gu) + 0.05
+    assert np.corrcoef(ge, gu)[0, 1] > 0.98
