@@ -79,6 +79,29 @@ int main() {
     bad += e.getEstimatedSolution(10, 0, 0, 0, 8) != 2.5f;
     e.totalPoissonKernelContribution = 0.0;
     bad += e.getEstimatedSolution(10, 0, 0, 0, 8) != 1.1f;
+    // sample generation against queries without boundaries (host-only distances: FLT_MAX)
+    zg::GeometricQueries<3> noBoundary(true, zg::Vector3(0, 0, 0), zg::Vector3(1, 1, 1));
+    std::vector<zg::SamplePoint<float, 3>> sp;
+    s.initialize(0.0f, false);
+    s.generateSamples(1200, zg::SampleType::OnAbsorbingBoundary, 0.0f, noBoundary, sp);
+    int onFace = 0, unitNormal = 0, pdfOk = 0;
+    for (const auto& q : sp) {
+        int faces = 0;
+        for (int k = 0; k < 3; k++) faces += std::fabs(q.pt[k]) < 1e-6f || std::fabs(q.pt[k] - 1.0f) < 1e-6f;
+        onFace += faces >= 1;
+        const float nn = q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2];
+        const float nmax = std::max(std::fabs(q.normal[0]), std::max(std::fabs(q.normal[1]), std::fabs(q.normal[2])));
+        unitNormal += std::fabs(nn - 1.0f) < 1e-5f && std::fabs(nmax - 1.0f) < 1e-5f;
+        pdfOk += std::fabs(q.pdf - 1.0f / 6.0f) < 1e-6f && q.type == zg::SampleType::OnAbsorbingBoundary &&
+                 q.distToAbsorbingBoundary == std::numeric_limits<float>::max();
+    }
+    bad += !(sp.size() == 1200 && onFace == 1200 && unitNormal == 1200 && pdfOk == 1200);
+    zg::UniformDomainSampler<float, 3> ds([](const zg::Vector3& x) { return x[0] < 0.5f; }, zg::Vector3(0, 0, 0),
+                                          zg::Vector3(1, 1, 1), 0.5f, 9);
+    ds.generateSamples(2000, noBoundary, sp);
+    int inRegion = 0;
+    for (const auto& q : sp) inRegion += q.pt[0] < 0.5f && q.pdf == 2.0f && q.type == zg::SampleType::InDomain;
+    bad += !(sp.size() > 1900 && sp.size() < 2100 && inRegion == (int)sp.size());
     zg::bvc::EvaluationPoint<float, 3> ep(zg::Vector3(), zg::Vector3(), zg::SampleType::InDomain, 1.0f, 1.0f);
     std::vector<float> grad;
     ep.getEstimatedGradient(grad);
@@ -117,8 +140,10 @@ def test_facade_host_classes_run_without_a_gpu(tmp_path):
     context is created): SampleStatistics::merge (Chan et al.) gives the pooled mean 3 and
     variance 4 of {1, 3, 5}; a DenseGrid becomes a grid field; settings carry over; a cube's
     triangle sampler splits sample counts by side and keeps none outside the solve region;
-    negative or missing primitive weights and mis-sized grids throw INVALID_ARG; the
-    reverse-walk evaluation point self-normalises its absorbing part."""
+    negative or missing primitive weights and mis-sized grids throw INVALID_ARG; cube-surface
+    samples lie on its faces with pdf 1 / area and unit axis-aligned normals, domain samples
+    stay in the solve region with pdf 1 / volume (queries without boundaries answer on the
+    host); the reverse-walk evaluation point self-normalises its absorbing part."""
     from zombie_gb300 import build
     build.build()
     LIBDIR = build.LIBDIR
