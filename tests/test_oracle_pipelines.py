@@ -1,7 +1,8 @@
 """The oracle's boundary value caching and reverse Walk on Stars end to end on the CPU (a 2D star
 polygon and a 3D displaced icosphere, level 4), with the host samplers of zombie_gb300.bvc and
 the oracle's own closest-point queries: the estimates (and the splatted gradients) recover
-manufactured solutions, and two FP32 / estimator
+manufactured solutions; the reverse walks' splat weights match an FP64 restatement (one step
+per walk, 2D / 3D, harmonic / Yukawa); and two FP32 / estimator
 properties of the reference's algorithm that the 3D GPU tests are configured around are pinned:
 
 * the 3D Yukawa ball evaluates I_{3/2}(mu R) as cosh(mu R) - sinh(mu R) / (mu R)
@@ -219,3 +220,70 @@ def test_oracle_bvc_laplace_2d_splats_values_and_gradients(oracle):
     assert np.sqrt(np.mean((est - u) ** 2)) < 0.1 * np.std(u) + 0.02
     assert np.sqrt(np.mean((ge - gu) ** 2)) < 0.25 * np.std(gu) + 0.05
     assert np.corrcoef(ge, gu)[0, 1] > 0.98
+
+
+@pytest.mark.parametrize("dim,sigma", [(2, 0.0), (2, 2.0), (3, 0.0), (3, 2.0)])
+def test_oracle_reverse_splat_matches_an_independent_restatement(oracle, dim, sigma):
+    """One step per reverse walk (max walk length 1, maximal spheres from the first step, no
+    reflecting boundary): every sample splats only its first ball, centred at the sample with
+    radius its distance to the absorbing boundary, so each evaluation point's totals are
+    sum_s G_ball(max(clamp, |x - y_s|); R_s) / pdf_s * contribution_s (divided by the normal
+    offset for absorbing samples; the Poisson-kernel total adds the weights of unscreened
+    absorbing samples) over the balls holding it (splatContribution,
+    variance_reduction/reverse_walk_solver.h:236-302).  The ball Green's functions are
+    restated in FP64 with scipy's Bessel functions (core/distributions.h:453-1005)."""
+    from scipy import special
+    rng = np.random.default_rng(70 + dim + int(sigma))
+    if dim == 2:
+        pos, idx = P.star_polygon(1024)
+        inside = lambda x: P.polygon_inside_and_radius(np.asarray(x, np.float64), pos)[0]
+        lo, hi = np.array([-1.3, -1.3]), np.array([1.3, 1.3])
+    else:
+        pos, idx, sh = P.displaced_icosphere(3, 0)
+        inside = lambda x: np.linalg.norm(np.asarray(x, np.float64), axis=1) < sh.radius(np.asarray(x, np.float64))
+        lo, hi = pos.min(0) - 0.05, pos.max(0) + 0.05
+    ob = oracle.Boundary(dim, pos, idx)
+
+    def interior(n):
+        x = rng.uniform(lo, hi, (4 * n, dim)).astype(np.float32)
+        return x[inside(x)][:n]
+    ns, ne, offset, clamp = 64, 600, 0.01, 1e-3
+    y = interior(ns)
+    R = ob.closest_point(y)[2].astype(np.float32)
+    typ = np.where(np.arange(ns) % 2 == 0, 0, 1).astype(np.int32)       # source / absorbing samples
+    pdf = rng.uniform(0.5, 2.0, ns).astype(np.float32)
+    contrib = rng.uniform(-1.0, 1.0, ns).astype(np.float32)
+    smp = dict(pt=y, normal=np.zeros_like(y), type=typ, estimate_normal_aligned=np.zeros(ns, np.int32), pdf=pdf,
+               contribution=contrib, dist_to_absorbing=R, seed=np.arange(1, ns + 1, dtype=np.uint64))
+    x = interior(ne)
+    ev = dict(pt=x, normal=np.zeros_like(x), type=np.zeros(len(x), np.int32), totals=np.zeros((len(x), 6)))
+    pde = P.make_pde(P.solution_expcos(0.0), sigma=sigma)
+    ws = P.default_walk_settings(eps_abs=1e-4, max_len=1, maximal=0)
+    oracle.rws_solve(dim, ob, None, lo, hi, pde, ws, smp, ev, offset, radius_clamp=clamp, stream=0)
+
+    # FP64 restatement
+    mu = np.sqrt(sigma)
+    d = np.linalg.norm(x.astype(np.float64)[:, None, :] - y.astype(np.float64)[None, :, :], axis=2)   # [ne, ns]
+    Rd = R.astype(np.float64)[None, :]
+    r = np.maximum(clamp, d)
+    if dim == 2 and sigma == 0:
+        G = np.log(Rd / r) / (2 * np.pi)
+    elif dim == 2:
+        G = (special.k0(mu * r) - special.i0(mu * r) * special.k0(mu * Rd) / special.i0(mu * Rd)) / (2 * np.pi)
+    elif sigma == 0:
+        G = (1.0 / r - 1.0 / Rd) / (4 * np.pi)
+    else:
+        G = (np.exp(-mu * r) - np.exp(-mu * Rd) * np.sinh(mu * r) / np.sinh(mu * Rd)) / (4 * np.pi * r)
+    inball = d < Rd
+    w = np.where(inball, G / pdf[None, :], 0.0)
+    w = np.where(typ[None, :] == 1, w / offset, w)
+    src = (w * np.where(typ == 0, contrib, 0.0)[None, :]).sum(1)
+    ab = (w * np.where(typ == 1, contrib, 0.0)[None, :]).sum(1)
+    pk = (w * (typ == 1)[None, :]).sum(1) if sigma == 0 else np.zeros(len(x))
+    # points within FP32 rounding of a ball's edge may fall either side: leave them out
+    clear = np.all(np.abs(d - Rd) > 1e-4 * Rd, axis=1)
+    t = ev["totals"]
+    assert np.sum(np.any(inball, axis=1) & clear) > 50
+    for got, want in ((t[:, 4], src), (t[:, 0], ab), (t[:, 5], pk)):
+        assert np.allclose(got[clear], want[clear], rtol=2e-4, atol=2e-5 * np.abs(want).max() + 1e-12)
+    assert np.all(t[:, [1, 2, 3]] == 0.0)
