@@ -142,3 +142,12 @@ def test_list_types_empty_callbacks_and_rws_point_sums():
     assert p.get_estimated_solution(10, 0, 0, 0, 8) == pytest.approx(0.6 + 0.5)
     p.reset()
     assert p.total_source_contribution == 0.0
+
+
+def test_host_utilities_accept_empty_inputs():
+    out = [1, 2]
+    assert Z.Utils.get_spatially_sorted_point_indices(np.zeros((0, 3)), out).size == 0 and out == []
+    assert io.compute_signed_volume(np.zeros((0, 2)), np.zeros((0, 2), np.int32)) == 0.0
+    assert io.compute_signed_volume(np.zeros((0, 3)), np.zeros((0, 3), np.int32)) == 0.0
+    (ap, ai), (rp, ri) = io.partition_boundary_mesh(lambda m: m[:, 0] > 0, np.zeros((0, 2)), np.zeros((0, 2), np.int32))
+    assert ap.shape == (0, 2) and ri.shape == (0, 2)

@@ -253,6 +253,10 @@ def get_spatially_sorted_point_indices(points, out_indices=None):
     bounding box, 21 bits per axis.  The reference returns its k-d tree's leaf order
     (nanoflann); both are spatially coherent orders, not the same permutation."""
     x = np.asarray(points, np.float64)
+    if x.size == 0:
+        if out_indices is not None:
+            out_indices.clear()
+        return np.zeros(0, np.uint32)
     n, dim = x.shape
     lo, hi = x.min(0), x.max(0)
     q = np.floor((x - lo) / np.where(hi > lo, hi - lo, 1.0) * ((1 << 21) - 1)).astype(np.uint64)
