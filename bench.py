@@ -178,43 +178,71 @@ def algorithmic_bytes_per_step(problem, n_points=None):
     return per_step, {k: {kk: vv / max(steps, 1) for kk, vv in v.items()} for k, v in c.items()}
 
 
-def cpu_baseline(problem, budget_s=15.0, threads=None):
-    """The restated reference CPU path (oracle, all host threads) on a bounded sample of the
-    same workload: a random subset of the points with the full walk count."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    from zombie_gb300 import problems as P
-    from zombie_gb300 import _abi as A
-    pr = problem
-    D = pr.dim
-    threads = threads or os.cpu_count()
-    ab = O.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
-    rf = None
-    if pr.reflecting is not None and len(pr.reflecting[1]):
-        k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32) if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN else None
-        rf = O.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
-                        silhouette_precision=pr.ignore_silhouette_precision)
-    rng = np.random.default_rng(11)
-    order = rng.permutation(pr.points.shape[0])
-    done_steps, t_used, used_pts = 0, 0.0, 0
-    chunk = 64
-    while t_used < budget_s and used_pts < len(order):
-        idx = order[used_pts:used_pts + chunk]
-        pts = pr.points[idx]
-        n = pts.shape[0]
-        d = ab.closest_point(pts)[2] if ab is not None else \
+# points in the fixed CPU sample of each workload (full walk count per point): about 10 s of
+# the restated CPU path on 16 cores for the default workload
+CPU_SAMPLE_POINTS = {"mixed_wost_2d": 4096, "mixed_wost_2d_screened": 4096, "mixed_wost_2d_small": 2048,
+                     "laplace_wos_2d": 4096, "robin_wost_3d": 256, "robin_wost_3d_small": 256,
+                     "screened_wos_3d": 4096, "screened_wos_3d_small": 4096}
+
+
+class CpuSample:
+    """A fixed, seeded sample of a workload's points for the restated reference CPU path
+    (the oracle on all host threads, dynamic scheduling over points like TBB's parallel_for).
+    Every timing of the same workload runs exactly these points with their full walk counts."""
+
+    def __init__(self, problem, n_points, seed=11):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        from zombie_gb300 import problems as P
+        from zombie_gb300 import _abi as A
+        self.O, self.pr = O, problem
+        pr = problem
+        D = pr.dim
+        self.ab = O.Boundary(D, *pr.absorbing) if pr.absorbing is not None and len(pr.absorbing[1]) else None
+        self.rf = None
+        if pr.reflecting is not None and len(pr.reflecting[1]):
+            k = np.full(len(pr.reflecting[1]), pr.robin_coeff, np.float32) \
+                if pr.reflecting_kind == A.ZGPU_BOUNDARY_ROBIN else None
+            self.rf = O.Boundary(D, *pr.reflecting, kind=pr.reflecting_kind, kmin=k, kmax=k,
+                                 silhouette_precision=pr.ignore_silhouette_precision)
+        n_all = pr.points.shape[0]
+        self.idx = np.sort(np.random.default_rng(seed).choice(n_all, min(n_points, n_all), replace=False))
+        pts = pr.points[self.idx]
+        self.pts = pts
+        self.dist = self.ab.closest_point(pts)[2] if self.ab is not None else \
             np.linalg.norm(np.minimum(pr.domain_min - pts, pts - pr.domain_max), axis=1).astype(np.float32)
-        sp = dict(pt=pts, dist_to_absorbing=d, n_walks=pr.n_walks[idx], seed=P.seeds_for(n, 99),
-                  first_sphere_radius=np.zeros(n, np.float32))
+        self.seeds = P.seeds_for(len(self.idx), 99)
+        self.n_all = n_all
+
+    def run(self, threads, first=None):
+        """One solve of the sample (or of its first `first` points); returns (steps, seconds)."""
+        pr, n = self.pr, len(self.idx) if first is None else min(first, len(self.idx))
+        sp = dict(pt=self.pts[:n], dist_to_absorbing=self.dist[:n], n_walks=pr.n_walks[self.idx[:n]],
+                  seed=self.seeds[:n], first_sphere_radius=np.zeros(n, np.float32))
         st = dict(solution_mean=np.zeros(n), solution_m2=np.zeros(n), n_solution_estimates=np.zeros(n, np.int32),
                   total_walk_length=np.zeros(n, np.int64), total_splits=np.zeros(n, np.int64))
         t0 = time.perf_counter()
-        done_steps += O.solve(pr.solver, D, ab, rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings, sp, st, threads)
-        t_used += time.perf_counter() - t0
-        used_pts += n
-        chunk = min(chunk * 2, 4096)
-    return dict(value=done_steps / t_used, unit="walk-steps/s", cores=threads, kind="port",
-                sample=f"{used_pts} of {pr.points.shape[0]} points x full walks/point, {done_steps} steps in {t_used:.1f} s")
+        steps = self.O.solve(pr.solver, pr.dim, self.ab, self.rf, pr.domain_min, pr.domain_max, pr.pde, pr.settings,
+                             sp, st, threads)
+        return steps, time.perf_counter() - t0
+
+    def describe(self, steps, seconds, runs=1):
+        return (f"fixed seeded sample of {len(self.idx)} of {self.n_all} points x full walks/point"
+                f"{'' if runs == 1 else f', {runs} runs'}: {steps} steps in {seconds:.1f} s")
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def cpu_baseline(problem, workload, n_points=None, threads=None):
+    """The restated reference CPU path (oracle, all host threads) on the workload's fixed
+    sample of points with the full walk count per point."""
+    threads = threads or cpu_threads()
+    smp = CpuSample(problem, n_points or CPU_SAMPLE_POINTS.get(workload, 2048))
+    steps, dt = smp.run(threads)
+    return dict(value=steps / dt, unit="walk-steps/s", cores=threads, kind="port",
+                build="g++ -O3 (portable: no -march / -mcpu tuning)", sample=smp.describe(steps, dt))
 
 
 def make_problem(name):
@@ -468,22 +496,30 @@ def P_mod():
 
 
 def run_reference(args):
+    """The reference arm: the restated reference CPU path on the host cores, each step one
+    solve of the workload's fixed point sample (warm-up steps run its first 256 points)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     pr, desc = make_problem(args.workload)
-    vals = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        base = cpu_baseline(pr, budget_s=args.cpu_budget / max(1, args.steps))
-        if i >= args.warmup:
-            vals.append(base["value"])
-    v = float(np.mean(vals))
+    threads = cpu_threads()
+    smp = CpuSample(pr, args.cpu_points or CPU_SAMPLE_POINTS.get(args.workload, 2048))
+    for _ in range(args.warmup):
+        smp.run(threads, first=256)
+    tot_steps, tot_s, per = 0, 0.0, []
+    for _ in range(args.steps):
+        st, dt = smp.run(threads)
+        tot_steps += st
+        tot_s += dt
+        per.append(dt)
+    v = tot_steps / tot_s
     line = {"impl": "reference", "metric": "walk-steps/s", "value": v, "unit": "walk-steps/s", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "description": desc},
-            "cpu_baseline": dict(base, value=v),
+            "cpu_baseline": {"value": v, "unit": "walk-steps/s", "cores": threads, "kind": "port",
+                             "build": "g++ -O3 (portable: no -march / -mcpu tuning)",
+                             "sample": smp.describe(tot_steps, tot_s, runs=args.steps)},
             "e2e": {"value": v, "unit": "walk-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -597,7 +633,7 @@ def run_gpu(args):
         tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
         if os.path.exists(tp):
             traffic = json.load(open(tp)).get("dram_bytes_per_launch")
-        cpu = cpu_baseline(pr, budget_s=args.cpu_budget) if not args.skip_cpu else None
+        cpu = cpu_baseline(pr, args.workload, args.cpu_points) if not args.skip_cpu else None
         line = {
             "metric": "walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -752,7 +788,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-points", type=int, default=0,
+                    help="points in the CPU path's fixed sample (0 = the workload's default)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-build-times", action="store_true",
                     help="skip the host vs device boundary build timings")

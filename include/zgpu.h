@@ -359,8 +359,10 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
  * GPU loading the library holds until process exit.
  * Limits: points->n <= ZGPU_STATIC_MAX_POINTS; points and statistics in ZGPU_MEM_DEVICE;
  * no walk splitting (splitting_threshold must be FLT_MAX).  Larger inputs are rejected with
- * ZGPU_ERR_INVALID_ARG.  The first call on a device looks up the array's device address;
- * make that first call before any stream capture.  Every call shares the one array and
+ * ZGPU_ERR_INVALID_ARG.  Solution only, single scene: gradient statistics arrays or a
+ * scene_id array are rejected with ZGPU_ERR_UNSUPPORTED.  The first call on a device looks
+ * up the array's device address and keeps it until exit (it assumes the device's primary
+ * context is not reset meanwhile); make that first call before any stream capture.  Every call shares the one array and
  * clears what must start at zero: calls that overlap on the GPU (two streams, two host
  * threads) race and must be serialised by the caller.  The call returns after the stream
  * has drained (it reads back the counters for the report and the error word).

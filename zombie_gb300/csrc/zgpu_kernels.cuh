@@ -271,7 +271,8 @@ struct Walker {
     }
 
     __device__ __noinline__ void pushSplit() {
-        if (nStack < kSplitStack) storeSplit<D>(splitSlots + 3 * nStack++, pt, nrm, prevDir, prevDist, thr, onRefl);
+        // no split slots (a solve that runs without split scratch): report instead of storing
+        if (P.splitStack && nStack < kSplitStack) storeSplit<D>(splitSlots + 3 * nStack++, pt, nrm, prevDir, prevDist, thr, onRefl);
         else err |= kErrSplitOverflow;
     }
 
@@ -296,6 +297,13 @@ struct Walker {
     ZG_D bool weightWindow() {
         const float sT = SC().ws.splitting_threshold, rT = SC().ws.russian_roulette_threshold;
         if (thr > sT) {
+            if (!(thr <= kFltMax)) {
+                // a throughput that overflowed to inf (reflectance bounds up to 2 with negative
+                // Robin coefficients) cannot be split into finite states: report it, keep sT
+                err |= kErrSplitOverflow;
+                thr = sT;
+                return false;
+            }
             float left = thr - sT;
             thr = sT;
             for (int guard = 0; left > sT && guard < 1 << 20; guard++) {
@@ -620,7 +628,7 @@ __global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant
     CoopWork* coopWork = reinterpret_cast<CoopWork*>(dynStack + 2 * P.stackEntries * blockDim.x) + (threadIdx.x >> 5);
     using WalkerT = Walker<D, SOLVER, SCREENED, BATCHED, COOP>;
     WalkerT W(P, S);
-    W.splitSlots = P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack;
+    W.splitSlots = P.splitStack ? P.splitStack + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 3 * kSplitStack : nullptr;
     const int lane = threadIdx.x & 31;
     const long long total = (long long)__ldg(P.walkStart + P.nPoints);
     bool active = false, exhausted = false;

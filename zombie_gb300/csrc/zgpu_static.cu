@@ -7,7 +7,13 @@
 // pass `gStaticScratch` itself to a kernel (in host code the name is a host-side shadow, not
 // a device address), so the device address is looked up once per device with
 // cudaGetSymbolAddress, with that device current.  Every call shares the array; calls that
-// overlap on the GPU race.
+// overlap on the GPU race.  The looked-up address is kept for the life of the process: it
+// assumes the device's primary context lives until exit (after cudaDeviceReset the module is
+// loaded again and the kept address is stale).
+//
+// Limits: solution estimates only (no gradient statistics), one scene (no scene_id), no walk
+// splitting.  A throughput that would split (thr > splitting_threshold = FLT_MAX, i.e. thr
+// overflowed to inf) raises the device error word instead of storing a split state.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -83,6 +89,12 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
     if (!stats->solution_mean || !stats->solution_m2 || !stats->n_solution_estimates || !stats->total_walk_length ||
         !stats->total_splits)
         return fail(ZGPU_ERR_INVALID_ARG, "statistics arrays are required");
+    // solution estimates of one scene only: gradient moments and a scene table would need
+    // scratch (and staging) this entry point does not have
+    if (stats->gradient_mean || stats->gradient_m2 || stats->n_gradient_estimates)
+        return fail(ZGPU_ERR_UNSUPPORTED, "zgpu_solve_static estimates solutions only: pass no gradient statistics");
+    if (pts->scene_id)
+        return fail(ZGPU_ERR_UNSUPPORTED, "zgpu_solve_static solves one scene: scene_id must be NULL");
     if (!(ws->splitting_threshold >= 3.402823466e+38f))
         return fail(ZGPU_ERR_INVALID_ARG, "zgpu_solve_static does not split walks: splitting_threshold must be FLT_MAX");
     if (ws->max_walk_length <= 0 || !(ws->epsilon_shell_for_absorbing_boundary >= 0.0f) || !(pde->absorption_coeff >= 0.0f))
@@ -117,7 +129,7 @@ extern "C" int zgpu_solve_static(void* stream, int solver, const zgpu_geometric_
     P.aligned = pts->estimate_normal_aligned;
     P.statMean = stats->solution_mean; P.statM2 = stats->solution_m2; P.statN = stats->n_solution_estimates;
     P.statLen = (long long*)stats->total_walk_length; P.statSplits = (long long*)stats->total_splits;
-    P.splitStack = nullptr;   // never touched: splitting is disabled above
+    P.splitStack = nullptr;   // no split slots: the walk kernel reports a split instead of storing it
     P.stackEntries = 8;
     if (P.sc.hasAbs) P.stackEntries = P.sc.absorbing.stackEntries > P.stackEntries ? P.sc.absorbing.stackEntries : P.stackEntries;
     if (P.sc.hasRefl) P.stackEntries = P.sc.reflecting.stackEntries > P.stackEntries ? P.sc.reflecting.stackEntries : P.stackEntries;
