@@ -56,6 +56,10 @@ WORKLOADS = {
     "rws_mixed_2d": dict(fn=None, kw={}, desc="reverse Walk on Stars, 2D mixed Dirichlet/Neumann (4096-segment "
                          "star polygon, f=-1): 32,768 absorbing + 32,768 reflecting + 65,536 domain samples, one "
                          "walk each, splatting onto the 256x256 grid's interior points"),
+    "screened_wos_3d_200k": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=200_000, spp=16),
+                                 desc="3D screened WoS sigma=4, icosphere L8 (1,310,720 tris), 200k points, 16 spp"),
+    "robin_wost_3d_200k": dict(fn="robin_wost_3d", kw=dict(level=6, n_points=200_000, spp=32),
+                               desc="3D Robin WoSt, icosphere L6 (81,920 tris), 200k points, 32 spp, kappa=2"),
     "screened_wos_3d_small": dict(fn="screened_wos_3d", kw=dict(level=8, n_points=16384, spp=4),
                                   desc="profiling case: 3D screened WoS sigma=4, icosphere L8, 16384 points, 4 spp"),
 }
@@ -182,7 +186,8 @@ def algorithmic_bytes_per_step(problem, n_points=None):
 # the restated CPU path on 16 cores for the default workload
 CPU_SAMPLE_POINTS = {"mixed_wost_2d": 4096, "mixed_wost_2d_screened": 4096, "mixed_wost_2d_small": 2048,
                      "laplace_wos_2d": 4096, "robin_wost_3d": 256, "robin_wost_3d_small": 256,
-                     "screened_wos_3d": 4096, "screened_wos_3d_small": 4096}
+                     "robin_wost_3d_200k": 512, "screened_wos_3d": 4096, "screened_wos_3d_200k": 4096,
+                     "screened_wos_3d_small": 4096}
 
 
 class CpuSample:
@@ -543,7 +548,22 @@ def run_gpu(args):
     from zombie_gb300.runner import GpuProblem, summarize
     pr, desc = make_problem(args.workload)
     ctx = Context(local)
-    gp = GpuProblem(pr, context=ctx, seed_base=0x5eed + rank)
+    options = None
+    if args.bvh_width or args.query_mode:
+        options = A.SolveOptions()
+        options.bvh_width = args.bvh_width
+        options.query_mode = args.query_mode
+    gp = GpuProblem(pr, context=ctx, seed_base=0x5eed + rank, options=options)
+    if args.autotune:
+        import ctypes as C
+        from zombie_gb300._lib import check, lib
+        tuned, rate = A.SolveOptions(), C.c_float()
+        sp, _ = gp.host_arrays().to_c()
+        q, pde = gp.queries.to_c(), gp.pde.to_c()
+        check(lib().zgpu_autotune(ctx.h, pr.solver, C.byref(q), C.byref(pde), C.byref(pr.settings), C.byref(sp),
+                                  4096, 8, C.byref(tuned), C.byref(rate)))
+        gp.solver.options = tuned
+        log("autotuned", {k: getattr(tuned, k) for k, _ in tuned._fields_}, rate.value)
     P_all = pr.points.shape[0]
     dev = gp.device_arrays()
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -629,10 +649,15 @@ def run_gpu(args):
         mean_kernel_ms = float(np.mean(kernel_ms))
         steps_per_launch = total_steps / args.steps / (ws if dist else 1)
         achieved = per_step_bytes * steps_per_launch / (mean_kernel_ms / 1e3) / 1e9
-        traffic = None
+        # DRAM bytes of one launch and the issue-side counters, from the committed ncu summary
+        # of this workload's walk kernel (ncu cannot run inside the timed bench)
+        traffic, counters = None, None
         tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
         if os.path.exists(tp):
-            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+            prof = json.load(open(tp))
+            traffic = prof.get("dram_bytes_per_launch")
+            counters = {k: prof[k] for k in ("threads_per_warp_instruction", "warp_execution_efficiency",
+                                              "issue_active_pct", "l1_hit_pct", "l2_hit_pct", "source") if k in prof}
         cpu = cpu_baseline(pr, args.workload, args.cpu_points) if not args.skip_cpu else None
         line = {
             "metric": "walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -640,13 +665,19 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "description": desc, "points": int(P_all),
                        "walks_per_point": int(pr.n_walks[0]), "parallelism": f"points x{ws}",
+                       "solve_options": ({k: getattr(gp.solver.options, k) for k, _ in gp.solver.options._fields_}
+                                         if gp.solver.options is not None else "defaults"),
                        "l2": "256 MiB buffer written between timed steps"},
             "rmse_vs_exact": g["rmse"], "mean_walk_length": g["mean_walk_length"],
             "e2e": {"value": e2e_val, "unit": "walk-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": 6 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                         "bytes_per_step": per_step_bytes, "kernel_ms": mean_kernel_ms},
+                         "bytes_per_step": per_step_bytes, "kernel_ms": mean_kernel_ms,
+                         "limiter": "instruction issue under divergence; the scene is L1/L2-resident, so "
+                                    "achieved is tree bytes consumed per second, not DRAM bandwidth",
+                         "traffic_source": "committed ncu capture of one launch of this workload (profiles/)",
+                         "ncu": counters},
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
@@ -706,59 +737,101 @@ def boundary_build_times(ctx):
     return out
 
 
-def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2), budget_s=150.0, level=8):
-    """Time to reach RMSE targets against the analytic solution on the 3D screened Poisson
-    problem (sigma = 4, icosphere L8, u = exp(0.5x) cos y + z^2): plain Walk on Spheres with
-    progressively doubled walk counts, against the neural cache (online training on the
-    solver's own estimates, held-out gate, then cached walks, doubled the same way).  Wall
-    time on the GPU-resident problem; the cache's time includes all of its training."""
+def fit_arm(hist):
+    """Fits an arm's progressive solves: rmse^2 = b^2 + a^2 / spp (least squares over the
+    recorded solves; b is the arm's error floor, 0 for an unbiased walk) and wall time
+    t = t0 + c * spp.  Returns (a, b, t0, c)."""
+    spp = np.array([h["spp"] for h in hist], np.float64)
+    r2 = np.array([h["rmse"] ** 2 for h in hist], np.float64)
+    t = np.array([h["t"] for h in hist], np.float64)
+    coef = np.linalg.lstsq(np.stack([np.ones_like(spp), 1.0 / spp], 1), r2, rcond=None)[0]
+    b2, a2 = max(float(coef[0]), 0.0), max(float(coef[1]), 1e-30)
+    c, t0 = (np.polyfit(spp, t, 1) if len(spp) > 1 else (t[0] / spp[0], 0.0))
+    return float(np.sqrt(a2)), float(np.sqrt(b2)), float(t0), float(c)
+
+
+def time_at(fit, target, hist):
+    """Wall time at which the fitted arm reaches `target`, with the walk count and whether
+    it lies inside the measured walk counts ("interpolated") or beyond ("extrapolated");
+    None when the arm's error floor is at or above the target."""
+    a, b, t0, c = fit
+    if target * target <= b * b:
+        return None
+    spp = a * a / (target * target - b * b)
+    lo, hi = min(h["spp"] for h in hist), max(h["spp"] for h in hist)
+    return {"t": t0 + c * spp, "spp": spp, "kind": "interpolated" if lo <= spp <= hi else "extrapolated"}
+
+
+def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2, 1e-3), budget_s=600.0, level=8, train_points=None,
+                 train_spp=64):
+    """Time to reach RMSE targets against the FP64 analytic solution on the 3D screened Poisson
+    problem (sigma = 4, icosphere L8, u = exp(0.5x) cos y + z^2): plain Walk on Spheres against
+    the neural cache (online training on the solver's own estimates, calibration, held-out
+    gate, then cached walks).  Each arm runs progressive solves (walk counts doubled) and is
+    fitted with rmse^2 = b^2 + a^2/spp and t = t0 + c spp; the time to a target is read off the
+    fit (interpolated inside the measured walk counts, extrapolated beyond them).  The gate
+    admits the cache for a target only if the error it adds to a solve is at most target / 3;
+    otherwise the neural-cache solver falls back to the plain walk and its time is the training
+    time plus the plain arm's.  Wall time on the GPU-resident problem; the cache's time
+    includes all of its training."""
     import torch
     from zombie_gb300 import problems as P
     from zombie_gb300.neural import NeuralCacheSolver, make_cache
     from zombie_gb300.runner import GpuProblem
+    train_points = train_points or n_points
+    start = time.perf_counter()
     pr = P.screened_wos_3d(level=level, n_points=n_points, spp=16)
     gp = GpuProblem(pr, context=ctx)
     ex = pr.exact()
-    goal = min(targets)
 
     def rmse(arr):
         return float(np.sqrt(np.mean((arr["solution_mean"].cpu().numpy() - ex) ** 2)))
 
-    def progressive(arr, t0, cache=None, first_spp=16, deadline=None):
-        hist, total, spp = [], 0, first_spp
+    def progressive(arr, t0, deadline, cache=None, first=16):
+        """Solves with walk counts doubled (16, 16, 32, 64, ... accumulated into the same
+        statistics) until the RMSE is below every target or the next solve would end past the
+        deadline; at least three solves."""
+        hist, total, spp = [], 0, first
+        # walks per point and call: at most 2^28 walks a call (a cached walk keeps a 32-byte
+        # record until the inference pass), more calls accumulate into the same statistics
+        chunk = max(16, (1 << 28) // n_points)
+        s0 = time.perf_counter()
         while True:
-            arr["n_walks"].fill_(spp)
-            rep = gp.solve(arr, cache=cache, cache_min_distance=0.05)
+            done, steps, walks = 0, 0, 0
+            while done < spp:
+                c = min(chunk, spp - done)
+                arr["n_walks"].fill_(c)
+                rep = gp.solve(arr, cache=cache, cache_min_distance=0.05)
+                steps += rep.total_steps
+                walks += rep.total_walks
+                done += c
             torch.cuda.synchronize()
             total += spp
-            r = rmse(arr)
-            hist.append(dict(t=time.perf_counter() - t0, spp=total, rmse=r, steps_per_walk=rep.total_steps / max(1, rep.total_walks)))
+            now = time.perf_counter()
+            hist.append(dict(t=now - t0, spp=total, rmse=rmse(arr), steps_per_walk=steps / max(1, walks)))
             log("time-to-rmse", "cache" if cache is not None else "plain", hist[-1])
-            if r <= goal or time.perf_counter() > deadline:
-                return hist
+            if hist[-1]["rmse"] <= min(targets):
+                break
+            per_spp = (now - s0) / total
+            if len(hist) >= 3 and now + per_spp * total > deadline:
+                break
             spp = total
+        return hist
 
-    def first(hist, tgt):
-        for h in hist:
-            if h["rmse"] <= tgt:
-                return h
-        return None
-
-    start = time.perf_counter()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    plain = progressive(gp.device_arrays(n_walks=16), t0, deadline=t0 + budget_s / 2)
-    # neural cache: train, gate, then cached walks
+    plain = progressive(gp.device_arrays(n_walks=16), t0, deadline=t0 + 0.4 * budget_s)
+    # neural cache: train on the solver's own estimates, calibrate, gate, then cached walks
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     cache = make_cache(gp.queries, 3, log2_table_size=19, max_resolution=64.0, learning_rate_grid=1e-2,
                        learning_rate_mlp=5e-3, context=ctx)
-    ncs = NeuralCacheSolver(gp.solver, gp.pde, pr.settings, cache, min_distance=0.05, error_bound=5e-3)
+    ncs = NeuralCacheSolver(gp.solver, gp.pde, pr.settings, cache, min_distance=0.05, error_bound=min(targets) / 3)
     rng = np.random.default_rng(1234)
-    xt, dt = ncs.sample_interior(1 << 20, rng)
-    ncs.train(xt, dt, spp=16, steps=2000, batch_size=1 << 16)
-    for r in range(6):
-        # self-training on cached walks
+    xt, dt = ncs.sample_interior(train_points, rng)
+    ncs.train(xt, dt, spp=train_spp, steps=2000, batch_size=1 << 16)
+    for r in range(4):
+        # self-training on cached walks from fresh points
         xt, dt = ncs.sample_interior(1 << 20, rng)
         ncs.train(xt, dt, spp=16, steps=1000, batch_size=1 << 16, seed_base=(r + 2) << 44, cached=True)
     xc, dc = ncs.sample_interior(8192, np.random.default_rng(98))
@@ -766,17 +839,37 @@ def time_to_rmse(ctx, n_points, targets=(2e-2, 1e-2), budget_s=150.0, level=8):
     xh, dh = ncs.sample_interior(4096, np.random.default_rng(99))
     gate = ncs.gate(xh, dh, spp=512)
     gate["calibrated_offset"], gate["termination_throughput"] = offset, tau
+    torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
+    added = gate["solve_error"]
+    admitted = {str(t): added <= t / 3 for t in targets}
     log("time-to-rmse cache training", round(train_s, 2), "s; gate", gate, "; rounds", ncs.history)
-    cached = progressive(gp.device_arrays(n_walks=16), t0, cache=cache if gate["enabled"] else None,
-                         deadline=time.perf_counter() + budget_s / 2)
-    out = {"problem": f"3D screened Poisson sigma=4, icosphere L{level}, {n_points} evaluation points",
-           "cache_train_s": train_s, "gate": gate,
-           "plain": plain, "cached": cached, "targets": {}}
+    cached = None
+    if any(admitted.values()):
+        cached = progressive(gp.device_arrays(n_walks=16), t0, start + budget_s, cache=cache)
+    fp = fit_arm(plain)
+    fc = fit_arm(cached) if cached else None
+    out = {"problem": f"3D screened Poisson sigma=4, icosphere L{level}, {n_points} evaluation points, RMSE against "
+                      f"the FP64 analytic solution",
+           "cache_training": {"points": int(train_points), "spp": train_spp, "seconds": train_s,
+                              "self_training_rounds": 4},
+           "gate": gate, "admitted_at": admitted, "plain": plain, "cached": cached,
+           "fit": {"plain": dict(zip(("a", "b", "t0", "c"), fp)),
+                   "cached": dict(zip(("a", "b", "t0", "c"), fc)) if fc else None},
+           "targets": {}}
     for tgt in targets:
-        a, b = first(plain, tgt), first(cached, tgt)
-        out["targets"][str(tgt)] = {"plain_s": a["t"] if a else None, "cache_s": b["t"] if b else None,
-                                    "speedup": (a["t"] / b["t"]) if (a and b) else None}
+        tp = time_at(fp, tgt, plain)
+        if admitted[str(tgt)] and fc is not None:
+            tc = time_at(fc, tgt, cached)
+            status = "cache admitted"
+        else:
+            tc = {"t": train_s + tp["t"], "spp": tp["spp"], "kind": tp["kind"]} if tp else None
+            status = f"cache refused by the gate (added error {added:.2e} > target/3): plain walk after training"
+        rec = {"plain_s": tp["t"] if tp else None, "plain_fit": tp["kind"] if tp else "unreachable",
+               "cache_s": tc["t"] if tc else None, "cache_fit": tc["kind"] if tc else "unreachable (error floor)",
+               "status": status}
+        rec["speedup"] = rec["plain_s"] / rec["cache_s"] if (tp and tc) else None
+        out["targets"][str(tgt)] = rec
     out["wall_s"] = time.perf_counter() - start
     return out
 
@@ -788,14 +881,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--bvh-width", type=int, default=0, help="solve option bvh_width (8: 8-wide 3D absorbing tree)")
+    ap.add_argument("--query-mode", type=int, default=0, help="solve option query_mode (1 lane, 2 warp per query)")
+    ap.add_argument("--autotune", action="store_true", help="run zgpu_autotune on the workload before timing")
     ap.add_argument("--cpu-points", type=int, default=0,
                     help="points in the CPU path's fixed sample (0 = the workload's default)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-build-times", action="store_true",
                     help="skip the host vs device boundary build timings")
-    ap.add_argument("--ttr-points", type=int, default=1 << 19,
+    ap.add_argument("--ttr-points", type=int, default=4_000_000,
                     help="evaluation points of the neural-cache time-to-RMSE comparison (0 = skip)")
-    ap.add_argument("--ttr-budget", type=float, default=300.0, help="seconds allowed for that comparison")
+    ap.add_argument("--ttr-budget", type=float, default=600.0, help="seconds allowed for that comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

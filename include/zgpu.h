@@ -195,6 +195,10 @@ typedef struct zgpu_solve_options {
     int64_t step_budget;       /* per-walk-state cap on device loop iterations (0: none beyond
                                   max_walk_length); a walk that reaches it is dropped and the
                                   solve returns ZGPU_ERR_TIMEOUT_BUDGET */
+    int32_t bvh_width;         /* 0 / 4: the boundaries' own trees; 8: an 8-wide tree of a 3D
+                                  absorbing boundary built on the host (built once, on first use,
+                                  from the boundary's copy of its mesh) */
+    int32_t reserved;
 } zgpu_solve_options;
 
 /* counters returned by a solve */
@@ -248,7 +252,9 @@ void* zgpu_context_stream(zgpu_context* ctx);
  * positions: [n_vertices*dim] host floats; indices: [n_prims*dim] host ints.
  * min/max_robin_coeff: [n_prims] (ROBIN only, else NULL).
  * solve_double_sided/silhouette_precision feed getIgnoreCandidateSilhouetteCallback (:1029-1038).
- * bvh_width: 4 or 8 (0 -> 4).
+ * bvh_width: 4 or 8 (0 -> 4); 8-wide trees are built for 3D absorbing boundaries only
+ * (other boundaries return ZGPU_ERR_UNSUPPORTED for 8), and they do not serve
+ * zgpu_query_sample_boundary.
  */
 int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int n_vertices,
                          const int* indices, int n_prims, int kind,
@@ -267,6 +273,19 @@ int zgpu_boundary_signed_volume(zgpu_boundary* b, float* out);
 
 /* ---------------------- batched geometric queries ------------------------- */
 /* All arrays live in `memory`; n queries; vectors are [n*dim].                */
+
+/*
+ * How the batched queries below traverse the tree (no counterpart in the reference, whose
+ * queries run one CPU thread per query): ZGPU_QUERY_MODE_AUTO / _LANE answer each query on one
+ * GPU lane; ZGPU_QUERY_MODE_WARP answers closest-point queries, and star-radius queries of
+ * Robin boundaries, with a whole warp per query (the traversal the walk kernel uses on large
+ * scenes with zgpu_solve_options.query_mode = 2).  Both modes return the same primitive for
+ * every closest-point query; Robin radii agree up to node bounds met in another order.
+ */
+#define ZGPU_QUERY_MODE_AUTO 0
+#define ZGPU_QUERY_MODE_LANE 1
+#define ZGPU_QUERY_MODE_WARP 2
+int zgpu_boundary_set_query_mode(zgpu_boundary* b, int mode);
 
 /* computeDistToAbsorbingBoundary / projectToAbsorbingBoundary
  * (utils/fcpw_geometric_queries.h:1069-1096; reflecting twins :1150-1177):
@@ -336,12 +355,14 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
 
 /*
  * Autotuner (no counterpart in the reference): times launch configurations (block size
- * 32/64/128 x blocks per SM auto/2/4, and the query mode for Walk on Spheres and for Walk
- * on Stars on a Robin boundary) on a stride
- * sample of `sample_points` points with `sample_walks` walks each, and writes the fastest
- * into `out_options`.  Results are cached in the context per scene signature (dimension,
- * solver, log2 primitive counts, reflecting kind, screening); a cached answer returns with
- * *best_steps_per_s = -1.  The BVH width is fixed at 4 in this build.
+ * 32/64/128 x blocks per SM auto/2/4, the query mode for Walk on Spheres and for Walk on
+ * Stars on a Robin boundary, and the BVH node width 4 / 8 of a 3D absorbing boundary) on a
+ * stride sample of `sample_points` points with `sample_walks` walks each, and writes the
+ * fastest into `out_options`.  Results are cached in the context per scene signature
+ * (dimension, solver, log2 primitive counts, reflecting kind, screening); a cached answer
+ * returns with *best_steps_per_s = -1.  There is no walks-per-thread knob: the persistent
+ * walk kernel refills each lane from a global walk counter whenever its walk ends, so a lane
+ * runs as many walks as the load demands.
  */
 int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries, const zgpu_pde* pde,
                   const zgpu_walk_settings* settings, const zgpu_sample_points* points, int32_t sample_points,

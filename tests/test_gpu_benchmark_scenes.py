@@ -1,0 +1,380 @@
+"""GPU parity on the scenes of the benchmark workloads themselves, through the C ABI.
+
+The scenes: the 4,096-segment star polygon of the mixed Dirichlet / Neumann workload (its
+Neumann half carries the silhouette-candidate tree), the level-6 displaced icosphere of the
+Robin workload (81,920 triangles, kappa = 2) and the level-8 displaced icosphere of the
+screened-Poisson workload (1,310,720 triangles).  Queries run one lane per query and, where
+the walk kernel uses them on these scenes, one warp per query; every answer is compared
+with the oracle's.  Closest-primitive indices must match except at ties, and every index
+mismatch is shown to be a tie: the GPU's primitive lies as close to the query as the
+oracle's (FP64 distances of the FP32 inputs, equal within the FP32 resolution below).
+Distances agree within 1e-6 relative, with an absolute floor of 2.4e-7 (two units in the
+last place of an FP32 coordinate of magnitude ~1: for queries within ~1e-3 of the surface
+the difference x - closest point cancels, and neither side can resolve more).
+
+Solves: sub-sampled points of every benchmark workload at its stated walk count, GPU
+against the oracle on the same pcg32 streams (per-point |z| <= 3 for at least 99% of the
+points) and against the FP64 manufactured solution (RMSE and mean z).
+"""
+import numpy as np
+import pytest
+
+from zombie_gb300 import _abi as A
+from zombie_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+DIST_REL, DIST_ABS = 1e-6, 2.4e-7
+
+
+# --------------------------------------------------------------------- FP64 distances
+def _segment_dist(x, a, b):
+    u = b - a
+    t = np.clip(np.einsum("ij,ij->i", x - a, u) / np.maximum(np.einsum("ij,ij->i", u, u), 1e-300), 0.0, 1.0)
+    return np.linalg.norm(x - (a + t[:, None] * u), axis=1)
+
+
+def _triangle_dist(p, a, b, c):
+    """Distance from points to triangles in FP64 (closest point by Voronoi regions)."""
+    ab, ac, ap = b - a, c - a, p - a
+    dot = lambda u, v: np.einsum("ij,ij->i", u, v)
+    d1, d2 = dot(ab, ap), dot(ac, ap)
+    bp = p - b
+    d3, d4 = dot(ab, bp), dot(ac, bp)
+    cp = p - c
+    d5, d6 = dot(ab, cp), dot(ac, cp)
+    vc = d1 * d4 - d3 * d2
+    vb = d5 * d2 - d1 * d6
+    va = d3 * d6 - d5 * d4
+    denom = np.where(va + vb + vc == 0, 1.0, va + vb + vc)
+    q = a + (vb / denom)[:, None] * ab + (vc / denom)[:, None] * ac          # interior
+    with np.errstate(divide="ignore", invalid="ignore"):
+        e_bc = b + np.nan_to_num(((d4 - d3) / ((d4 - d3) + (d5 - d6))))[:, None] * (c - b)
+        e_ac = a + np.nan_to_num((d2 / (d2 - d6)))[:, None] * ac
+        e_ab = a + np.nan_to_num((d1 / (d1 - d3)))[:, None] * ab
+    m = lambda cond: cond[:, None]
+    q = np.where(m((va <= 0) & (d4 - d3 >= 0) & (d5 - d6 >= 0)), e_bc, q)
+    # regions in reverse order of precedence (vertex a first, then b, edge ab, c, edge ac, edge bc)
+    q = np.where(m((vb <= 0) & (d2 >= 0) & (d6 <= 0)), e_ac, q)
+    q = np.where(m((d6 >= 0) & (d5 <= d6)), c, q)
+    q = np.where(m((vc <= 0) & (d1 >= 0) & (d3 <= 0)), e_ab, q)
+    q = np.where(m((d3 >= 0) & (d4 <= d3)), b, q)
+    q = np.where(m((d1 <= 0) & (d2 <= 0)), a, q)
+    return np.linalg.norm(p - q, axis=1)
+
+
+def prim_dist64(pos, idx, prim, x):
+    """FP64 distance from x[i] to primitive prim[i] of the mesh (pos, idx)."""
+    pos = pos.astype(np.float64)
+    x = x.astype(np.float64)
+    v = idx[prim]
+    if idx.shape[1] == 2:
+        return _segment_dist(x, pos[v[:, 0]], pos[v[:, 1]])
+    return _triangle_dist(x, pos[v[:, 0]], pos[v[:, 1]], pos[v[:, 2]])
+
+
+def assert_closest_parity(pos, idx, x, g, o):
+    """GPU answer g = (pt, n, d, prim) against the oracle's o: distances within tolerance,
+    indices equal except at ties, and every mismatch proven a tie."""
+    gp, gn, gd, gi = g
+    op, on, od, oi = o
+    tol = np.maximum(DIST_REL * od, DIST_ABS)
+    assert np.all(np.abs(gd - od) <= tol), np.max(np.abs(gd - od) - tol)
+    same = gi == oi
+    assert same.mean() > 0.99
+    bad = np.nonzero(~same)[0]
+    if len(bad):
+        dg = prim_dist64(pos, idx, gi[bad], x[bad])
+        do = prim_dist64(pos, idx, oi[bad], x[bad])
+        assert np.all(np.abs(dg - do) <= np.maximum(DIST_REL * do, DIST_ABS)), "an index mismatch is not a tie"
+    assert np.allclose(gp[same], op[same], atol=2e-6)
+    assert np.allclose(gn[same], on[same], atol=1e-5)
+    return int(len(bad))
+
+
+# --------------------------------------------------------------------------- scenes
+@pytest.fixture(scope="module")
+def polygon():
+    pr = P.mixed_wost_2d(n_segments=4096, grid=64, spp=1)
+    pos, idx = P.star_polygon(4096)
+    return dict(full=(pos, idx), absorbing=pr.absorbing, neumann=pr.reflecting)
+
+
+@pytest.fixture(scope="module")
+def sphere6():
+    pos, idx, sh = P.displaced_icosphere(6, seed=0)
+    return pos, idx, sh
+
+
+@pytest.fixture(scope="module")
+def sphere8():
+    pos, idx, sh = P.displaced_icosphere(8, seed=0)
+    return pos, idx, sh
+
+
+def _queries_2d(n, seed):
+    """Points over the polygon's box, half of them within 1e-2 of the curve."""
+    rng = np.random.default_rng(seed)
+    t = rng.uniform(0, 2 * np.pi, n)
+    r = 1.0 + 0.3 * np.sin(5 * t)
+    near = np.stack([r * np.cos(t), r * np.sin(t)], 1) * (1.0 + rng.uniform(-1e-2, 1e-2, n))[:, None]
+    far = rng.uniform(-1.4, 1.4, (n, 2))
+    return np.where((rng.random(n) < 0.5)[:, None], near, far).astype(np.float32)
+
+
+def _queries_3d(sh, n, seed):
+    """Points inside and around the displaced sphere, half of them within 1e-2 of it."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    near = d * (sh.radius(d) * (1.0 + rng.uniform(-1e-2, 1e-2, n)))[:, None]
+    far = rng.uniform(-1.4, 1.4, (n, 3))
+    return np.where((rng.random(n) < 0.5)[:, None], near, far).astype(np.float32)
+
+
+def _gpu(dim, pos, idx, kind=A.ZGPU_BOUNDARY_ABSORBING, kappa=None, mode=A.ZGPU_QUERY_MODE_LANE, width=4):
+    from zombie_gb300 import api
+    ic = api.IgnoreCandidateSilhouette(False, 0.0)
+    if kind == A.ZGPU_BOUNDARY_ABSORBING:
+        h = api.GpuDirichletBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx, bvh_width=width)
+    elif kind == A.ZGPU_BOUNDARY_NEUMANN:
+        h = api.GpuNeumannBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx, ic)
+    else:
+        k = np.full(idx.shape[0], kappa, np.float32)
+        h = api.GpuRobinBoundaryHandler(dim)
+        h.build_acceleration_structure(pos, idx, ic, k, k)
+    h.set_query_mode(mode)
+    return h
+
+
+# ----------------------------------------------------------------- closest points
+@pytest.mark.parametrize("part", ["full", "absorbing", "neumann"])
+def test_closest_point_on_the_4096_segment_polygon(zgpu, oracle, polygon, part):
+    pos, idx = polygon[part]
+    x = _queries_2d(20000, 1)
+    g = _gpu(2, pos, idx).closest_point(x)
+    o = oracle.Boundary(2, pos, idx, use_bvh=False).closest_point(x)
+    assert_closest_parity(pos, idx, x, g, o)
+
+
+@pytest.mark.parametrize("mode", [A.ZGPU_QUERY_MODE_LANE, A.ZGPU_QUERY_MODE_WARP])
+def test_closest_point_on_the_level6_sphere(zgpu, oracle, sphere6, mode):
+    pos, idx, sh = sphere6
+    x = _queries_3d(sh, 4000, 2)
+    g = _gpu(3, pos, idx, mode=mode).closest_point(x)
+    o = oracle.Boundary(3, pos, idx, use_bvh=False).closest_point(x)
+    assert_closest_parity(pos, idx, x, g, o)
+
+
+@pytest.mark.parametrize("mode", [A.ZGPU_QUERY_MODE_LANE, A.ZGPU_QUERY_MODE_WARP])
+def test_closest_point_on_the_level8_sphere(zgpu, oracle, sphere8, mode):
+    """1.31M triangles: the oracle answers through its binary SAH tree (pinned against brute
+    force on smaller meshes by the oracle's own tests); a sub-sample is re-checked by brute
+    force here as well."""
+    pos, idx, sh = sphere8
+    x = _queries_3d(sh, 4000, 3)
+    g = _gpu(3, pos, idx, mode=mode).closest_point(x)
+    o = oracle.Boundary(3, pos, idx, use_bvh=True).closest_point(x)
+    assert_closest_parity(pos, idx, x, g, o)
+    sub = slice(0, 64)
+    ob = oracle.Boundary(3, pos, idx, use_bvh=False).closest_point(x[sub])
+    assert_closest_parity(pos, idx, x[sub], tuple(a[sub] for a in g), ob)
+
+
+def test_warp_and_lane_closest_points_are_identical_on_the_level8_sphere(zgpu, sphere8):
+    """One lane or one warp per query, 4- or 8-wide nodes: the same primitive and the same
+    FP32 distance for every query."""
+    pos, idx, sh = sphere8
+    x = _queries_3d(sh, 20000, 4)
+    a = _gpu(3, pos, idx, mode=A.ZGPU_QUERY_MODE_LANE).closest_point(x)
+    for width in (4, 8):
+        for mode in (A.ZGPU_QUERY_MODE_LANE, A.ZGPU_QUERY_MODE_WARP):
+            b = _gpu(3, pos, idx, mode=mode, width=width).closest_point(x)
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v), (width, mode)
+
+
+@pytest.mark.parametrize("mode", [A.ZGPU_QUERY_MODE_LANE, A.ZGPU_QUERY_MODE_WARP])
+def test_eight_wide_tree_answers_like_the_oracle_on_the_level8_sphere(zgpu, oracle, sphere8, mode):
+    pos, idx, sh = sphere8
+    x = _queries_3d(sh, 4000, 12)
+    g = _gpu(3, pos, idx, mode=mode, width=8)
+    assert g.info()["node_bytes"] == 256 * g.info()["n_nodes"]
+    o = oracle.Boundary(3, pos, idx, use_bvh=True)
+    assert_closest_parity(pos, idx, x, g.closest_point(x), o.closest_point(x))
+    rng = np.random.default_rng(13)
+    n = 8000
+    org = rng.uniform(-0.7, 0.7, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tm = rng.uniform(0.05, 2.5, n).astype(np.float32)
+    gh, _, _, gt, gi = g.intersect(org, np.zeros_like(org), d, tm, np.zeros(n, np.int32))
+    oh, _, _, ot, oi = o.intersect(org, np.zeros_like(org), d, tm, np.zeros(n, np.int32))
+    assert (gh == oh).mean() > 0.9995
+    both = (gh == 1) & (oh == 1)
+    assert np.all(np.abs(gt[both] - ot[both]) <= 1e-5 * np.maximum(ot[both], 1.0))
+    big = np.full(n, 1e30, np.float32)
+    assert np.mean(g.count_hits(org, d, big) == o.count_hits(org, d, big)) > 0.9995
+
+
+def test_eight_wide_solves_run_the_four_wide_walks(zgpu):
+    """Walk on Spheres on the level-8 sphere with zgpu_solve_options.bvh_width = 8 (an 8-wide
+    twin of the absorbing tree): every closest point is the same, so the walks are the same."""
+    from zombie_gb300.runner import GpuProblem
+    pr = P.screened_wos_3d(level=8, n_points=3000, spp=16)
+    out = []
+    for width, mode in ((4, 1), (8, 1), (8, 2)):
+        opt = A.SolveOptions()
+        opt.bvh_width = width
+        opt.query_mode = mode
+        gp = GpuProblem(pr, options=opt)
+        d = gp.device_arrays()
+        rep = gp.solve(d)
+        assert rep.error_word == 0
+        out.append((rep.total_steps, {k: d[k].cpu().numpy() for k in ("n_solution_estimates", "total_walk_length",
+                                                                     "solution_mean")}))
+    for steps, arr in out[1:]:
+        assert steps == out[0][0]
+        assert np.array_equal(arr["total_walk_length"], out[0][1]["total_walk_length"])
+        assert np.allclose(arr["solution_mean"], out[0][1]["solution_mean"], rtol=1e-12, atol=1e-15)
+
+
+def test_autotuner_chooses_a_node_width_on_the_level8_sphere(zgpu):
+    import ctypes as C
+    from zombie_gb300 import _lib
+    from zombie_gb300.runner import GpuProblem
+    pr = P.screened_wos_3d(level=8, n_points=20000, spp=8)
+    gp = GpuProblem(pr)
+    arr = gp.device_arrays()
+    sp, _ = arr.to_c()
+    opt = A.SolveOptions()
+    rate = C.c_float()
+    q, pde = gp.queries.to_c(), gp.pde.to_c()
+    _lib.check(_lib.lib().zgpu_autotune(gp.ctx.h, pr.solver, C.byref(q), C.byref(pde), C.byref(pr.settings),
+                                         C.byref(sp), 4096, 8, C.byref(opt), C.byref(rate)))
+    print("autotuned", opt.bvh_width, opt.query_mode, opt.block_size, opt.blocks_per_sm, rate.value)
+    assert opt.bvh_width in (4, 8) and rate.value > 0
+    rep = gp.solve(arr, options=opt)
+    assert rep.error_word == 0 and rep.total_steps > 0
+
+
+# ------------------------------------------------------------------- star radii
+def test_neumann_star_radius_on_the_4096_segment_polygon(zgpu, oracle, polygon):
+    """The benchmark's Neumann half with silhouette precision 0 (as the workload sets it)."""
+    pos, idx = polygon["neumann"]
+    rng = np.random.default_rng(5)
+    n = 12000
+    x = _queries_2d(n, 6)
+    mn = np.full(n, 1e-3, np.float32)
+    mx = rng.uniform(0.01, 2.0, n).astype(np.float32)
+    fl = np.zeros(n, np.int32)
+    g = _gpu(2, pos, idx, A.ZGPU_BOUNDARY_NEUMANN).star_radius(x, mn, mx, 0.0, fl)
+    o = oracle.Boundary(2, pos, idx, kind=A.ZGPU_BOUNDARY_NEUMANN, silhouette_precision=0.0,
+                        use_bvh=False).star_radius(x, mn, mx, 0.0, fl)
+    rel = np.abs(g - o) / np.maximum(o, 1e-30)
+    assert np.quantile(rel, 0.999) <= 1e-5
+    assert np.mean(rel <= 1e-6) > 0.99
+
+
+@pytest.mark.parametrize("mode", [A.ZGPU_QUERY_MODE_LANE, A.ZGPU_QUERY_MODE_WARP])
+def test_robin_star_radius_on_the_level6_sphere(zgpu, oracle, sphere6, mode):
+    """kappa = 2 everywhere, one lane and one warp per query, against the oracle's tree.  The
+    Robin bound r = (h/c) exp(...) amplifies FP32 rounding of its inputs (ill-conditioned for
+    small h), hence the 2e-3 bound at the 99.9th percentile; most radii agree to 1e-5."""
+    pos, idx, sh = sphere6
+    rng = np.random.default_rng(7)
+    n = 4000
+    x = _queries_3d(sh, n, 8) * 0.98
+    mn = np.full(n, 1e-3, np.float32)
+    mx = rng.uniform(0.01, 2.0, n).astype(np.float32)
+    fl = np.zeros(n, np.int32)
+    k = np.full(idx.shape[0], 2.0, np.float32)
+    g = _gpu(3, pos, idx, A.ZGPU_BOUNDARY_ROBIN, 2.0, mode).star_radius(x, mn, mx, 1e-3, fl)
+    o = oracle.Boundary(3, pos, idx, kind=A.ZGPU_BOUNDARY_ROBIN, kmin=k, kmax=k, silhouette_precision=0.0,
+                        use_bvh=True).star_radius(x, mn, mx, 1e-3, fl)
+    rel = np.abs(g - o) / np.maximum(o, 1e-30)
+    assert np.median(rel) <= 1e-6
+    assert np.quantile(rel, 0.999) <= 2e-3
+    assert np.mean(rel <= 1e-5) > 0.97
+    assert np.all(g <= np.maximum(mx, mn) * (1 + 1e-6))
+    # a sub-sample against the oracle's brute force over all 81,920 triangles
+    sub = slice(0, 48)
+    ob = oracle.Boundary(3, pos, idx, kind=A.ZGPU_BOUNDARY_ROBIN, kmin=k, kmax=k, silhouette_precision=0.0,
+                         use_bvh=False).star_radius(x[sub], mn[sub], mx[sub], 1e-3, fl[sub])
+    relb = np.abs(g[sub] - ob) / np.maximum(ob, 1e-30)
+    assert np.quantile(relb, 0.5) <= 1e-6 and relb.max() <= 2e-3
+
+
+# ------------------------------------------------------------------------- rays
+@pytest.mark.parametrize("scene", ["neumann_polygon", "sphere6", "sphere8"])
+def test_ray_hits_on_benchmark_scenes(zgpu, oracle, polygon, sphere6, sphere8, scene):
+    if scene == "neumann_polygon":
+        (pos, idx), dim = polygon["neumann"], 2
+    else:
+        (pos, idx, _), dim = (sphere6 if scene == "sphere6" else sphere8), 3
+    rng = np.random.default_rng(9)
+    n = 20000
+    o = rng.uniform(-0.7, 0.7, (n, dim)).astype(np.float32)
+    d = rng.normal(size=(n, dim)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tm = rng.uniform(0.05, 2.5, n).astype(np.float32)
+    z = np.zeros_like(o)
+    on = np.zeros(n, np.int32)
+    kind = A.ZGPU_BOUNDARY_NEUMANN if dim == 2 else A.ZGPU_BOUNDARY_ABSORBING
+    g = _gpu(dim, pos, idx, kind)
+    ob = oracle.Boundary(dim, pos, idx, kind=kind, use_bvh=True)
+    gh, gpt, gn, gt, gi = g.intersect(o, z, d, tm, on)
+    oh, opt, on_, ot, oi = ob.intersect(o, z, d, tm, on)
+    agree = gh == oh
+    assert agree.mean() > 0.9995          # differences only for hits within float noise of tMax
+    both = (gh == 1) & (oh == 1)
+    assert np.all(np.abs(gt[both] - ot[both]) <= 1e-5 * np.maximum(ot[both], 1.0))
+    same = gi[both] == oi[both]
+    assert same.mean() > 0.999            # the rest: the ray crosses a shared edge / vertex
+    cnt = g.count_hits(o, d, np.full(n, 1e30, np.float32))
+    assert np.mean(cnt == ob.count_hits(o, d, np.full(n, 1e30, np.float32))) > 0.9995
+
+
+# ----------------------------------------------------------------------- solves
+def _subsample(pr, n, seed):
+    if pr.points.shape[0] > n:
+        idx = np.sort(np.random.default_rng(seed).choice(pr.points.shape[0], n, replace=False))
+        pr.points, pr.n_walks = pr.points[idx], pr.n_walks[idx]
+    return pr
+
+
+SOLVES = {
+    # workload: (problem at its stated walk count, points kept, oracle threads used)
+    "laplace_wos_2d": lambda: _subsample(P.laplace_wos_2d(n_segments=1024, grid=128, spp=256), 400, 1),
+    "mixed_wost_2d": lambda: _subsample(P.mixed_wost_2d(n_segments=4096, grid=256, spp=512), 300, 2),
+    "mixed_wost_2d_screened": lambda: _subsample(P.mixed_wost_2d(n_segments=4096, grid=256, spp=512, sigma=1.0), 300, 3),
+    "robin_wost_3d": lambda: P.robin_wost_3d(level=6, n_points=48, spp=128),
+    "screened_wos_3d": lambda: P.screened_wos_3d(level=8, n_points=300, spp=64),
+}
+
+
+@pytest.mark.parametrize("case", sorted(SOLVES))
+def test_benchmark_workload_solves_match_oracle_and_exact(zgpu, oracle, case):
+    from zombie_gb300.runner import GpuProblem, summarize
+    import test_oracle_solvers as T
+    pr = SOLVES[case]()
+    gp = GpuProblem(pr)
+    arr = gp.host_arrays()
+    rep = gp.solve(arr)
+    assert rep.error_word == 0 and rep.total_steps > 0
+    g = summarize(arr, pr.exact())
+    st, steps = T.run_oracle(oracle, pr, seeds=gp.seeds)
+    # the same walks on the same pcg32 streams: step totals and per-point estimates agree
+    assert abs(rep.total_steps - steps) <= 0.02 * steps
+    n = st["n_solution_estimates"].astype(np.float64)
+    se_o = np.sqrt(st["solution_m2"] / np.maximum(n - 1, 1) / np.maximum(n, 1))
+    z = (g["mean"] - st["solution_mean"]) / np.maximum(np.sqrt(g["se"] ** 2 + se_o ** 2), 1e-12)
+    assert np.mean(np.abs(z) > 3) <= 0.01
+    # and the FP64 manufactured solution: unbiased within the standard errors
+    ez = g["err"] / np.maximum(g["se"], 1e-12)
+    assert abs(ez.mean()) <= 0.5
+    assert np.mean(np.abs(ez) > 3.5) <= 0.05
+    rmse_bound = 4.0 * np.sqrt(np.mean(g["se"] ** 2)) + 2e-3
+    assert g["rmse"] <= rmse_bound, (g["rmse"], rmse_bound)

@@ -49,6 +49,7 @@ ZGPU_MAX_TERMS = 8
 ZGPU_STATIC_MAX_POINTS = 65536
 ZGPU_STATIC_SCRATCH_BYTES = 4 << 20
 FLT_MAX = 3.4028234663852886e38
+ZGPU_QUERY_MODE_AUTO, ZGPU_QUERY_MODE_LANE, ZGPU_QUERY_MODE_WARP = 0, 1, 2
 
 
 class Analytic(C.Structure):
@@ -157,6 +158,8 @@ class SolveOptions(C.Structure):
         ("use_graph", C.c_int32),
         ("query_mode", C.c_int32),
         ("step_budget", C.c_int64),
+        ("bvh_width", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

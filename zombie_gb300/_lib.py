@@ -46,6 +46,7 @@ def lib():
         L.zgpu_boundary_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64)]
         L.zgpu_boundary_signed_volume.argtypes = [vp, C.POINTER(C.c_float)]
+        L.zgpu_boundary_set_query_mode.argtypes = [vp, i32]
         L.zgpu_query_closest_point.argtypes = [vp, i64, vp, i32, vp, vp, vp, vp, i32]
         L.zgpu_query_intersect.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32]
         L.zgpu_query_count_hits.argtypes = [vp, i64, vp, vp, vp, vp, i32]

@@ -694,6 +694,12 @@ class _BoundaryHandler:
         except Exception:
             pass
 
+    def set_query_mode(self, mode):
+        """ZGPU_QUERY_MODE_LANE (one GPU lane per query, the default) or ZGPU_QUERY_MODE_WARP
+        (a warp per closest-point query and per Robin star-radius query) for the batched
+        queries below."""
+        check(lib().zgpu_boundary_set_query_mode(self.h, int(mode)))
+
     # batched geometric queries on host arrays (device tensors: pass memory=1 arrays)
     def closest_point(self, x, compute_signed=False):
         x = np.ascontiguousarray(x, np.float32).reshape(-1, self.dim)
@@ -784,8 +790,9 @@ class GpuDirichletBoundaryHandler(_BoundaryHandler):
     kind = A.ZGPU_BOUNDARY_ABSORBING
 
     def build_acceleration_structure(self, positions, indices, build_bvh=True, enable_bvh_vectorization=False,
-                                     print_stats=False, build_on_device=False):
-        self._build(positions, indices, build_on_device=build_on_device)
+                                     print_stats=False, build_on_device=False, bvh_width=4):
+        """bvh_width = 8 builds 8-wide nodes (3D, host build) for closest-point and ray queries."""
+        self._build(positions, indices, bvh_width=bvh_width, build_on_device=build_on_device)
 
 
 class GpuNeumannBoundaryHandler(_BoundaryHandler):

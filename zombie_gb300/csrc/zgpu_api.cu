@@ -99,6 +99,12 @@ struct zgpu_boundary {
     int* primIndex = nullptr;
     std::vector<int> primIndexHost;   // leaf slot -> caller index (for coefficient updates)
     BoundaryView view;
+    int queryMode = ZGPU_QUERY_MODE_AUTO;   // batched closest-point / Robin star-radius queries
+    // 3D absorbing boundaries built on the host keep their mesh, from which an 8-wide twin of
+    // the tree is built on first use (zgpu_solve_options.bvh_width = 8, the autotuner)
+    std::vector<float> hostPos;
+    std::vector<int> hostIdx;
+    zgpu_boundary* twin8 = nullptr;
 };
 
 namespace {
@@ -247,18 +253,21 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     *out = nullptr;
     if (dim != 2 && dim != 3) return fail(ZGPU_ERR_INVALID_ARG, "dim must be 2 or 3, got %d", dim);
     if (kind < ZGPU_BOUNDARY_ABSORBING || kind > ZGPU_BOUNDARY_ROBIN) return fail(ZGPU_ERR_INVALID_ARG, "unknown boundary kind %d", kind);
-    if (bvh_width != 0 && bvh_width != 4) return fail(ZGPU_ERR_UNSUPPORTED, "bvh_width %d not supported (4)", bvh_width);
+    if (bvh_width == 0) bvh_width = 4;
+    if (bvh_width != 4 && bvh_width != 8) return fail(ZGPU_ERR_INVALID_ARG, "bvh_width must be 4 or 8, got %d", bvh_width);
+    if (bvh_width == 8 && (dim != 3 || kind != ZGPU_BOUNDARY_ABSORBING))
+        return fail(ZGPU_ERR_UNSUPPORTED, "8-wide nodes are built for 3D absorbing boundaries only");
     if (n_prims > 0 && (!positions || !indices)) return fail(ZGPU_ERR_INVALID_ARG, "positions/indices are NULL");
     if (kind == ZGPU_BOUNDARY_ROBIN && n_prims > 0 && (!min_robin || !max_robin))
         return fail(ZGPU_ERR_INVALID_ARG, "Robin boundary needs min/max Robin coefficients per primitive");
     HostBoundary hb;
     std::string err;
     if (!buildBoundary(dim, positions, n_vertices, indices, n_prims, kind, min_robin, max_robin,
-                       solve_double_sided != 0, silhouette_precision, hb, err))
+                       solve_double_sided != 0, silhouette_precision, hb, err, bvh_width))
         return fail(ZGPU_ERR_INVALID_ARG, "boundary build: %s", err.c_str());
-    if (hb.depth > kMaxWideDepth || hb.silDepth > kMaxWideDepth)
-        return fail(ZGPU_ERR_UNSUPPORTED, "boundary BVH depth %d/%d exceeds the traversal stack (max %d)", hb.depth,
-                    hb.silDepth, kMaxWideDepth);
+    if (hb.depth > kMaxWideDepth || hb.silDepth > kMaxWideDepth || (bvh_width - 1) * hb.depth + 2 > kMaxStack)
+        return fail(ZGPU_ERR_UNSUPPORTED, "boundary BVH depth %d/%d exceeds the traversal stack (max %d entries)",
+                    hb.depth, hb.silDepth, kMaxStack);
     ZG_CUDA(cudaSetDevice(ctx->device));
     zgpu_boundary* b = new zgpu_boundary();
     b->ctx = ctx; b->dim = dim; b->kind = kind; b->nPrims = n_prims; b->nNodes = hb.nNodes; b->depth = hb.depth;
@@ -285,10 +294,15 @@ int zgpu_boundary_create(zgpu_context* ctx, int dim, const float* positions, int
     }
     b->view.nodes = b->nodes; b->view.cones = b->cones; b->view.prims = b->prims; b->view.sil = b->sil; b->view.primIndex = b->primIndex;
     b->view.nNodes = b->nNodes; b->view.nPrims = b->nPrims;
-    b->view.stackEntries = stackEntriesForDepth(std::max(b->depth, hb.silDepth));
+    b->view.stackEntries = std::max(stackEntriesForDepth(b->depth, bvh_width), stackEntriesForDepth(hb.silDepth));
+    b->view.width = bvh_width;
     b->view.silTree = b->silTree; b->view.silCones = b->silCones; b->view.silFeat = b->silFeat;
     b->view.silNodes = hb.silNodes;
     b->view.robin = kind == ZGPU_BOUNDARY_ROBIN;
+    if (dim == 3 && kind == ZGPU_BOUNDARY_ABSORBING && bvh_width == 4 && n_prims > 0) {
+        b->hostPos.assign(positions, positions + (size_t)n_vertices * 3);
+        b->hostIdx.assign(indices, indices + (size_t)n_prims * 3);
+    }
     *out = b;
     return ZGPU_OK;
 }
@@ -401,6 +415,7 @@ int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* posi
 int zgpu_boundary_destroy(zgpu_boundary* b) {
     if (!b) return ZGPU_OK;
     if (b->ctx) cudaSetDevice(b->ctx->device);
+    if (b->twin8) zgpu_boundary_destroy(b->twin8);
     cudaFree(b->silTree); cudaFree(b->silCones); cudaFree(b->silFeat);
     cudaFree(b->nodes); cudaFree(b->cones); cudaFree(b->prims); cudaFree(b->sil); cudaFree(b->primIndex);
     delete b;
@@ -459,7 +474,7 @@ int zgpu_boundary_info(zgpu_boundary* b, int64_t* n_nodes, int32_t* depth, int64
     if (!b) return fail(ZGPU_ERR_INVALID_ARG, "boundary is NULL");
     if (n_nodes) *n_nodes = b->nNodes;
     if (depth) *depth = b->depth;
-    if (node_bytes) *node_bytes = (int64_t)b->nNodes * 128;
+    if (node_bytes) *node_bytes = (int64_t)b->nNodes * 32 * b->view.width;
     if (prim_bytes) *prim_bytes = (int64_t)b->nPrims * (b->dim == 2 ? 16 : 48);
     return ZGPU_OK;
 }
@@ -491,6 +506,14 @@ static int queryEpilogue(zgpu_context* ctx, unsigned int* errw) {
     return ZGPU_OK;
 }
 
+int zgpu_boundary_set_query_mode(zgpu_boundary* b, int mode) {
+    if (!b) return fail(ZGPU_ERR_INVALID_ARG, "boundary is NULL");
+    if (mode != ZGPU_QUERY_MODE_AUTO && mode != ZGPU_QUERY_MODE_LANE && mode != ZGPU_QUERY_MODE_WARP)
+        return fail(ZGPU_ERR_INVALID_ARG, "unknown query mode %d", mode);
+    b->queryMode = mode;
+    return ZGPU_OK;
+}
+
 int zgpu_query_closest_point(zgpu_boundary* b, int64_t n, const float* x, int compute_signed, float* out_pt,
                              float* out_normal, float* out_dist, int32_t* out_prim, int memory) {
     ZG_QUERY_PROLOGUE();
@@ -505,7 +528,10 @@ int zgpu_query_closest_point(zgpu_boundary* b, int64_t n, const float* x, int co
         ZG_TRY(scratch<float>(ctx, zgpu_context::kQ3, (size_t)n, &dd));
         ZG_TRY(scratch<int>(ctx, zgpu_context::kQ4, (size_t)n, &dp));
     }
-    ZG_CUDA(launchClosest(b->view, D, n, dx, compute_signed, dpt, dn, dd, dp, errw, ctx->stream));
+    if (b->queryMode == ZGPU_QUERY_MODE_WARP)
+        ZG_CUDA(launchClosestCoop(b->view, D, n, dx, compute_signed, dpt, dn, dd, dp, errw, ctx->stream));
+    else
+        ZG_CUDA(launchClosest(b->view, D, n, dx, compute_signed, dpt, dn, dd, dp, errw, ctx->stream));
     ZG_TRY(stageOut<float>(ctx, dpt, out_pt, (size_t)n * D, memory));
     ZG_TRY(stageOut<float>(ctx, dn, out_normal, (size_t)n * D, memory));
     ZG_TRY(stageOut<float>(ctx, dd, out_dist, (size_t)n, memory));
@@ -572,7 +598,10 @@ int zgpu_query_star_radius(zgpu_boundary* b, int64_t n, const float* x, const fl
     ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ2, max_radius, (size_t)n, memory, &dmax));
     ZG_TRY(stageIn<int>(ctx, zgpu_context::kQ3, flip, (size_t)n, memory, &dflip));
     if (memory == ZGPU_MEM_DEVICE) dout = out_radius; else ZG_TRY(scratch<float>(ctx, zgpu_context::kQ4, (size_t)n, &dout));
-    ZG_CUDA(launchStarRadius(b->view, D, n, dx, dmin, dmax, silhouette_precision, dflip, dout, errw, ctx->stream));
+    if (b->queryMode == ZGPU_QUERY_MODE_WARP && b->kind == ZGPU_BOUNDARY_ROBIN)
+        ZG_CUDA(launchStarRadiusCoop(b->view, D, n, dx, dmin, dmax, silhouette_precision, dflip, dout, errw, ctx->stream));
+    else
+        ZG_CUDA(launchStarRadius(b->view, D, n, dx, dmin, dmax, silhouette_precision, dflip, dout, errw, ctx->stream));
     ZG_TRY(stageOut<float>(ctx, dout, out_radius, (size_t)n, memory));
     return queryEpilogue(ctx, errw);
 }
@@ -604,6 +633,7 @@ int zgpu_query_sample_boundary(zgpu_boundary* b, int64_t n, const float* x, cons
     if (n == 0) return ZGPU_OK;
     if (!x || !radius || !rand_nums || !out_found || !out_pt || !out_normal || !out_pdf)
         return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    if (b->view.width != 4) return fail(ZGPU_ERR_UNSUPPORTED, "boundary sampling needs a 4-wide tree");
     const float *dx, *dr, *du; int* dfound; float *dpt, *dn, *dpdf;
     ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ0, x, (size_t)n * D, memory, &dx));
     ZG_TRY(stageIn<float>(ctx, zgpu_context::kQ1, radius, (size_t)n, memory, &dr));
@@ -686,6 +716,24 @@ SceneDesc sceneOf(const zgpu_geometric_queries* q, const zgpu_pde* pde, const zg
     return d;
 }
 
+// The 8-wide twin of a 3D absorbing boundary (the boundary itself if it is 8-wide), built
+// from the boundary's host copy of its mesh on first use.
+int wideTwin(zgpu_boundary* b, zgpu_boundary** out) {
+    if (b->view.width == 8) { *out = b; return ZGPU_OK; }
+    if (!b->twin8) {
+        if (b->hostIdx.empty())
+            return fail(ZGPU_ERR_UNSUPPORTED, "bvh_width 8 needs a 3D absorbing boundary built on the host");
+        zgpu_boundary* t = nullptr;
+        ZG_TRY(zgpu_boundary_create(b->ctx, 3, b->hostPos.data(), (int)(b->hostPos.size() / 3), b->hostIdx.data(),
+                                    (int)(b->hostIdx.size() / 3), ZGPU_BOUNDARY_ABSORBING, nullptr, nullptr, 0, 0.0f, 8,
+                                    &t));
+        t->queryMode = b->queryMode;
+        b->twin8 = t;
+    }
+    *out = b->twin8;
+    return ZGPU_OK;
+}
+
 // zgpu_solve, zgpu_solve_cached and zgpu_solve_batched.  nScenes > 1: points->scene_id
 // selects each point's row of q / pde / ws.
 int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_queries* q, const zgpu_pde* pde,
@@ -709,6 +757,16 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     if (!stats->solution_mean || !stats->solution_m2 || !stats->n_solution_estimates || !stats->total_walk_length ||
         !stats->total_splits)
         return fail(ZGPU_ERR_INVALID_ARG, "statistics arrays are required");
+    zgpu_geometric_queries qWide;
+    if (opt && opt->bvh_width != 0 && opt->bvh_width != 4) {
+        if (opt->bvh_width != 8) return fail(ZGPU_ERR_INVALID_ARG, "bvh_width must be 0, 4 or 8");
+        if (batched) return fail(ZGPU_ERR_UNSUPPORTED, "bvh_width 8 serves single-scene solves");
+        if (q->absorbing && q->absorbing->nPrims > 0) {
+            qWide = *q;
+            ZG_TRY(wideTwin(q->absorbing, &qWide.absorbing));
+            q = &qWide;
+        }
+    }
 
     ZG_CUDA(cudaSetDevice(ctx->device));
     const int64_t n = pts->n;
@@ -864,7 +922,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     if (n > 0) ZG_CUDA(launchWalk(P, D, blocks, threads, s));
     if (cache && n > 0)
         ZG_CUDA(launchCacheAccumulate(cache, P.cacheRec, P.counters + kCtrCache, P.cacheCap, P.accSum, P.accSq,
-                                      P.accN, P.accLen, s));
+                                      P.accN, P.accLen, P.errorWord, s));
     ZG_CUDA(cudaEventRecord(ctx->ev[2], s));
     ZG_CUDA(launchFinalize(P, D, s));
     }
@@ -1001,9 +1059,13 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
                              q->reflecting->kind == ZGPU_BOUNDARY_ROBIN);
     const int threadsC[3] = {32, 64, 128};
     const int perSMC[3] = {0, 2, 4};
+    // node widths: 8-wide trees for 3D absorbing boundaries with a host copy of their mesh
+    const bool sweepWidth = D == 3 && q->absorbing && q->absorbing->nPrims > 0 &&
+                            (q->absorbing->view.width == 8 || !q->absorbing->hostIdx.empty());
     zgpu_solve_options best;
     std::memset(&best, 0, sizeof(best));
     double bestRate = -1.0;
+    for (int wi = 0; wi < (sweepWidth ? 2 : 1); wi++)
     for (int qm = sweepQuery ? 1 : 0; qm <= (sweepQuery ? 2 : 0); qm++)
         for (int ti = 0; ti < 3; ti++)
             for (int pi = 0; pi < 3; pi++) {
@@ -1012,6 +1074,7 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
                 o.block_size = threadsC[ti];
                 o.blocks_per_sm = perSMC[pi];
                 o.query_mode = qm;
+                o.bvh_width = wi == 0 ? 4 : 8;
                 double rate = 0.0;
                 for (int rep = 0; rep < 2; rep++) {
                     std::fill(cnt.begin(), cnt.end(), 0);

@@ -113,21 +113,26 @@ struct Builder {
 
 int makeLeafRef(int first, int count) { return -(1 + ((first << 3) | (count - 1))); }
 
+// Collapses the binary tree into nodes of `width` (4 or 8) children: 2 * width float4 per
+// node, in the layout of zgpu_scene.cuh (per group of 4 children: lower bounds per axis,
+// upper bounds per axis, child references, areas).
 struct Collapser {
     int D;
     const std::vector<BNode>& bn;
     std::vector<float4>& out;
+    int width = 4;
     int maxDepth = 0;
-    std::vector<std::array<int, 4>> kidsOf;   // wide node -> binary node of each child (-1 empty)
+    std::vector<std::array<int, 8>> kidsOf;   // wide node -> binary node of each child (-1 empty)
 
     int emit(int b, int depth) {
         maxDepth = std::max(maxDepth, depth);
-        int id = (int)(out.size() / 8);
-        out.resize(out.size() + 8);
-        kidsOf.push_back({-1, -1, -1, -1});
-        // gather up to 4 children by opening the largest internal child
+        const int stride = 2 * width, G = width / 4;
+        int id = (int)(out.size() / stride);
+        out.resize(out.size() + stride);
+        kidsOf.push_back({-1, -1, -1, -1, -1, -1, -1, -1});
+        // gather up to `width` children by opening the largest internal child
         std::vector<int> kids = {bn[b].left, bn[b].right};
-        while ((int)kids.size() < 4) {
+        while ((int)kids.size() < width) {
             int pick = -1; float pa = -1.0f;
             for (int i = 0; i < (int)kids.size(); i++) {
                 const BNode& k = bn[kids[i]];
@@ -139,9 +144,9 @@ struct Collapser {
             kids.push_back(bn[k].left);
             kids.push_back(bn[k].right);
         }
-        float lo[3][4], hi[3][4], area[4];
-        int child[4];
-        for (int c = 0; c < 4; c++) {
+        float lo[3][8], hi[3][8], area[8];
+        int child[8];
+        for (int c = 0; c < 8; c++) {
             for (int i = 0; i < 3; i++) { lo[i][c] = kInf; hi[i][c] = -kInf; }
             area[c] = 0.0f; child[c] = kEmpty;
         }
@@ -155,14 +160,17 @@ struct Collapser {
         for (int c = 0; c < (int)kids.size(); c++) {
             if (bn[kids[c]].count == 0) child[c] = emit(kids[c], depth + 1);
         }
-        float4* p = &out[(size_t)id * 8];
-        for (int i = 0; i < D; i++) {
-            p[i] = make_float4(lo[i][0], lo[i][1], lo[i][2], lo[i][3]);
-            p[D + i] = make_float4(hi[i][0], hi[i][1], hi[i][2], hi[i][3]);
+        float4* p = &out[(size_t)id * stride];
+        for (int g = 0; g < G; g++) {
+            const int c0 = 4 * g;
+            for (int i = 0; i < D; i++) {
+                p[i * G + g] = make_float4(lo[i][c0], lo[i][c0 + 1], lo[i][c0 + 2], lo[i][c0 + 3]);
+                p[(D + i) * G + g] = make_float4(hi[i][c0], hi[i][c0 + 1], hi[i][c0 + 2], hi[i][c0 + 3]);
+            }
+            int4 ci = make_int4(child[c0], child[c0 + 1], child[c0 + 2], child[c0 + 3]);
+            std::memcpy(&p[2 * D * G + g], &ci, sizeof(int4));
+            p[(2 * D + 1) * G + g] = make_float4(area[c0], area[c0 + 1], area[c0 + 2], area[c0 + 3]);
         }
-        int4 ci = make_int4(child[0], child[1], child[2], child[3]);
-        std::memcpy(&p[2 * D], &ci, sizeof(int4));
-        p[2 * D + 1] = make_float4(area[0], area[1], area[2], area[3]);
         return id;
     }
 };
@@ -236,7 +244,7 @@ void coneOf(int D, const std::vector<BNode>& bn, int node, const std::vector<int
 // `order` (leaf slot -> item) and returns the collapsed nodes (+ per-wide-node binary kids).
 struct WideTree {
     std::vector<float4> nodes;
-    std::vector<std::array<int, 4>> kids;
+    std::vector<std::array<int, 8>> kids;
     std::vector<BNode> bnodes;
     std::vector<int> order;
     int depth = 0;
@@ -265,7 +273,7 @@ void buildWideTree(int D, const std::vector<Box>& boxes, const std::vector<float
         int4 ci = make_int4(makeLeafRef(0, bld.nodes[0].count), kEmpty, kEmpty, kEmpty);
         std::memcpy(&out.nodes[2 * D], &ci, sizeof(int4));
         out.nodes[2 * D + 1] = make_float4(bld.nodes[0].area, 0, 0, 0);
-        out.kids.push_back({0, -1, -1, -1});
+        out.kids.push_back({0, -1, -1, -1, -1, -1, -1, -1});
         out.depth = 1;
         return;
     }
@@ -297,9 +305,13 @@ void coneOverNormals(int D, const std::vector<const float*>& ns, bool open, floa
 }  // namespace
 
 bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int kind, const float* kmin,
-                   const float* kmax, bool doubleSided, float silPrec, HostBoundary& hb, std::string& err) {
+                   const float* kmax, bool doubleSided, float silPrec, HostBoundary& hb, std::string& err, int width) {
     hb = HostBoundary();
-    hb.dim = D; hb.kind = kind; hb.nPrims = nP;
+    hb.dim = D; hb.kind = kind; hb.nPrims = nP; hb.width = width;
+    if (width != 4 && !(width == 8 && D == 3 && kind == 0)) {
+        err = "8-wide nodes are built for 3D absorbing boundaries only";
+        return false;
+    }
     if (D != 2 && D != 3) { err = "dim must be 2 or 3"; return false; }
     if (nP < 0 || nV < 0) { err = "negative sizes"; return false; }
     for (int i = 0; i < nP * D; i++)
@@ -400,20 +412,21 @@ bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int 
     // ---- wide layout
     if (bld.nodes[0].count > 0) {
         // tiny scene: a root whose single child is the leaf
-        hb.nodes.resize(8);
-        float lo[3][4], hi[3][4];
-        for (int i = 0; i < 3; i++) for (int c = 0; c < 4; c++) { lo[i][c] = kInf; hi[i][c] = -kInf; }
-        for (int i = 0; i < D; i++) { lo[i][0] = bld.nodes[0].box.lo[i]; hi[i][0] = bld.nodes[0].box.hi[i]; }
-        for (int i = 0; i < D; i++) {
-            hb.nodes[i] = make_float4(lo[i][0], lo[i][1], lo[i][2], lo[i][3]);
-            hb.nodes[D + i] = make_float4(hi[i][0], hi[i][1], hi[i][2], hi[i][3]);
+        const int G = width / 4;
+        hb.nodes.assign((size_t)2 * width, make_float4(0, 0, 0, 0));
+        for (int g = 0; g < G; g++) {
+            for (int i = 0; i < D; i++) {
+                hb.nodes[i * G + g] = make_float4(g == 0 ? bld.nodes[0].box.lo[i] : kInf, kInf, kInf, kInf);
+                hb.nodes[(D + i) * G + g] = make_float4(g == 0 ? bld.nodes[0].box.hi[i] : -kInf, -kInf, -kInf, -kInf);
+            }
+            int4 ci = make_int4(g == 0 ? makeLeafRef(0, bld.nodes[0].count) : kEmpty, kEmpty, kEmpty, kEmpty);
+            std::memcpy(&hb.nodes[2 * D * G + g], &ci, sizeof(int4));
+            hb.nodes[(2 * D + 1) * G + g] = make_float4(g == 0 ? bld.nodes[0].area : 0.0f, 0, 0, 0);
         }
-        int4 ci = make_int4(makeLeafRef(0, bld.nodes[0].count), kEmpty, kEmpty, kEmpty);
-        std::memcpy(&hb.nodes[2 * D], &ci, sizeof(int4));
-        hb.nodes[2 * D + 1] = make_float4(bld.nodes[0].area, 0, 0, 0);
         hb.depth = 1;
     } else {
         Collapser col{D, bld.nodes, hb.nodes};
+        col.width = width;
         col.emit(0, 1);
         hb.depth = col.maxDepth;
         if (kind != 0) {
@@ -435,7 +448,7 @@ bool buildBoundary(int D, const float* pos, int nV, const int* idx, int nP, int 
             }
         }
     }
-    hb.nNodes = (int)(hb.nodes.size() / 8);
+    hb.nNodes = (int)(hb.nodes.size() / (2 * width));
     if (kind != 0 && hb.cones.empty()) {
         // single-leaf scene: an always-visit cone
         hb.cones.assign(8, make_float4(0, 0, 0, 3.14159265f));

@@ -14,8 +14,9 @@ struct HostBoundary {
     int nPrims = 0;
     int nNodes = 0;
     int depth = 0;
+    int width = 4;                // children per node (8: 3D absorbing boundaries only)
     float signedVolume = 0.0f;
-    std::vector<float4> nodes;    // nNodes * 8
+    std::vector<float4> nodes;    // nNodes * 2 * width
     std::vector<float4> cones;    // reflecting only: nNodes * 8 (per child cone, then per-child max Robin coeff)
     std::vector<float4> prims;    // nPrims * (1 | 3)
     std::vector<float4> sil;      // reflecting only: nPrims * (2 | 3)
@@ -33,6 +34,6 @@ struct HostBoundary {
 // kind: 0 absorbing, 1 Neumann, 2 Robin (include/zgpu.h).  Returns false with a message.
 bool buildBoundary(int dim, const float* positions, int nVertices, const int* indices, int nPrims, int kind,
                    const float* minRobin, const float* maxRobin, bool solveDoubleSided, float silhouettePrecision,
-                   HostBoundary& out, std::string& error);
+                   HostBoundary& out, std::string& error, int width = 4);
 
 }  // namespace zg

@@ -11,6 +11,7 @@
 
 #include "zgpu_cache.cuh"
 #include "zgpu_internal.h"
+#include "zgpu_umma.cuh"
 
 using namespace zg;
 using namespace zg::cache;
@@ -309,6 +310,193 @@ evalKernel(const Net N, const float* __restrict__ x, float* __restrict__ y, int6
     }
 }
 
+// ------------------------------------------------------------------ tcgen05 inference
+// One CTA of 128 threads per 128-point tile, one thread per point: the thread encodes its
+// point into its row of the A operand, one thread issues the layer's MMAs (M = 128, N = 64,
+// K = 16 each: D = A * W^T with BF16 hi + lo operand pairs, three products per K step, FP32
+// accumulation in 64 tensor-memory columns), and every thread reads its row of the
+// accumulator back (tcgen05.ld), applies bias + ReLU and writes the next layer's A row.  The
+// output layer (64 -> 1) is a per-thread dot product.  Weights are staged once per CTA.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 64;                 // tensor-memory columns (one 128 x 64 FP32 tile)
+constexpr long long kTcWaitLimit = 1ll << 24;    // mbarrier polls before a wait gives up
+constexpr unsigned kErrTensorWait = 32u;         // error word bit: an MMA completion wait gave up
+
+struct TcShared {
+    unsigned char E[2][kTcRows * kInputs * 2];   // encoding rows, hi / lo  (K = 32)
+    unsigned char H[2][kTcRows * kHidden * 2];   // hidden-1 rows, hi / lo  (K = 64)
+    unsigned char W1[2][kHidden * kInputs * 2];  // [out][in], hi / lo
+    unsigned char W2[2][kHidden * kHidden * 2];
+    float b1[kHidden], b2[kHidden], w3[kHidden];
+    float b3;
+    uint64_t mbar;
+    uint32_t tmem;
+};
+constexpr size_t kTcSmem = sizeof(TcShared);
+
+// 8 consecutive values of a row as BF16 hi and lo (remainder) packs of 16 bytes each
+ZG_D void splitPack8(const float* v, uint4& hi, uint4& lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) pack2split(v[2 * j], v[2 * j + 1], h[j], l[j]);
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+template <int D, int MODE>
+__global__ void __launch_bounds__(kTcRows, 1)
+evalKernelTc(const Net N, const float* __restrict__ x, float* __restrict__ y, int64_t n,
+             const float4* __restrict__ rec, const unsigned long long* __restrict__ recCount, double* accSum,
+             double* accSq, int* accN, long long* accLen, unsigned int* errw) {
+    extern __shared__ __align__(128) unsigned char smemTc[];
+    TcShared& S = *reinterpret_cast<TcShared*>(smemTc);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kHidden * kInputs; i += kTcRows) {
+        const uint32_t off = umma::canonicalOffset<kInputs>(i / kInputs, i % kInputs);
+        *reinterpret_cast<__nv_bfloat16*>(S.W1[0] + off) = N.W1[i];
+        *reinterpret_cast<__nv_bfloat16*>(S.W1[1] + off) = N.W1lo[i];
+    }
+    for (int i = tid; i < kHidden * kHidden; i += kTcRows) {
+        const uint32_t off = umma::canonicalOffset<kHidden>(i / kHidden, i % kHidden);
+        *reinterpret_cast<__nv_bfloat16*>(S.W2[0] + off) = N.W2[i];
+        *reinterpret_cast<__nv_bfloat16*>(S.W2[1] + off) = N.W2lo[i];
+    }
+    for (int i = tid; i < kHidden; i += kTcRows) { S.b1[i] = N.b1[i]; S.b2[i] = N.b2[i]; S.w3[i] = N.w3[i]; }
+    if (tid == 0) { S.b3 = *N.b3; umma::mbarInit(&S.mbar, 1); }
+    if (warp == 0) umma::alloc(&S.tmem, kTcCols);
+    umma::fenceProxyAsync();
+    umma::fenceBeforeSync();
+    __syncthreads();
+    umma::fenceAfterSync();
+    const uint32_t tmem = S.tmem;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    const uint32_t idesc = umma::instrBf16(kTcRows, kHidden);
+    const uint32_t sE0 = umma::smemAddr(S.E[0]), sE1 = umma::smemAddr(S.E[1]);
+    const uint32_t sH0 = umma::smemAddr(S.H[0]), sH1 = umma::smemAddr(S.H[1]);
+    const uint32_t sA0 = umma::smemAddr(S.W1[0]), sA1 = umma::smemAddr(S.W1[1]);
+    const uint32_t sB0 = umma::smemAddr(S.W2[0]), sB1 = umma::smemAddr(S.W2[1]);
+    const int64_t total = MODE == 1 ? (int64_t)min((unsigned long long)n, *recCount) : n;
+    const int64_t tiles = (total + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const int64_t r = tile * kTcRows + tid;
+        const bool valid = r < total;
+        float xp[3] = {0.0f, 0.0f, 0.0f};
+        if (valid) {
+            if (MODE == 0) {
+#pragma unroll
+                for (int i = 0; i < D; i++) xp[i] = __ldg(x + r * D + i);
+            } else {
+                const float4 a = __ldg(rec + 2 * r);
+                xp[0] = a.x; xp[1] = a.y; xp[2] = a.z;
+            }
+        }
+        // encoding row (levels beyond N.levels and rows beyond the data encode 0)
+#pragma unroll 1
+        for (int kg = 0; kg < kInputs / 8; kg++) {
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int l = 4 * kg + j;
+                float2 f = make_float2(0.0f, 0.0f);
+                if (valid && l < N.levels) f = encodeLevel<D>(N, l, xp);
+                v[2 * j] = f.x; v[2 * j + 1] = f.y;
+            }
+            uint4 hi, lo;
+            splitPack8(v, hi, lo);
+            const uint32_t off = umma::canonicalOffset<kInputs>(tid, 8 * kg);
+            *reinterpret_cast<uint4*>(S.E[0] + off) = hi;
+            *reinterpret_cast<uint4*>(S.E[1] + off) = lo;
+        }
+        umma::fenceProxyAsync();
+        umma::fenceBeforeSync();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fenceAfterSync();
+#pragma unroll
+            for (int ks = 0; ks < kInputs / 16; ks++) {
+                const uint32_t k = 256u * ks;      // two core matrices along K per step
+                const uint64_t aHi = umma::descriptor(sE0 + k, 128, 16 * kInputs);
+                const uint64_t aLo = umma::descriptor(sE1 + k, 128, 16 * kInputs);
+                const uint64_t bHi = umma::descriptor(sA0 + k, 128, 16 * kInputs);
+                const uint64_t bLo = umma::descriptor(sA1 + k, 128, 16 * kInputs);
+                umma::mma(tmem, aHi, bHi, idesc, ks > 0);
+                umma::mma(tmem, aLo, bHi, idesc, true);
+                umma::mma(tmem, aHi, bLo, idesc, true);
+            }
+            umma::commit(&S.mbar);
+        }
+        ok = __syncthreads_and(umma::mbarWait(&S.mbar, phase, kTcWaitLimit));
+        phase ^= 1u;
+        if (!ok) break;
+        umma::fenceAfterSync();
+        // hidden layer 1: bias + ReLU, then this row of the layer-2 operand
+#pragma unroll 1
+        for (int c = 0; c < kHidden / 16; c++) {
+            float v[16];
+            umma::load16(taddr + 16u * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j] + S.b1[16 * c + j], 0.0f);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint4 hi, lo;
+                splitPack8(v + 8 * h, hi, lo);
+                const uint32_t off = umma::canonicalOffset<kHidden>(tid, 16 * c + 8 * h);
+                *reinterpret_cast<uint4*>(S.H[0] + off) = hi;
+                *reinterpret_cast<uint4*>(S.H[1] + off) = lo;
+            }
+        }
+        umma::fenceProxyAsync();
+        umma::fenceBeforeSync();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fenceAfterSync();
+#pragma unroll
+            for (int ks = 0; ks < kHidden / 16; ks++) {
+                const uint32_t k = 256u * ks;
+                const uint64_t aHi = umma::descriptor(sH0 + k, 128, 16 * kHidden);
+                const uint64_t aLo = umma::descriptor(sH1 + k, 128, 16 * kHidden);
+                const uint64_t bHi = umma::descriptor(sB0 + k, 128, 16 * kHidden);
+                const uint64_t bLo = umma::descriptor(sB1 + k, 128, 16 * kHidden);
+                umma::mma(tmem, aHi, bHi, idesc, ks > 0);
+                umma::mma(tmem, aLo, bHi, idesc, true);
+                umma::mma(tmem, aHi, bLo, idesc, true);
+            }
+            umma::commit(&S.mbar);
+        }
+        ok = __syncthreads_and(umma::mbarWait(&S.mbar, phase, kTcWaitLimit));
+        phase ^= 1u;
+        if (!ok) break;
+        umma::fenceAfterSync();
+        float out = S.b3;
+#pragma unroll 1
+        for (int c = 0; c < kHidden / 16; c++) {
+            float v[16];
+            umma::load16(taddr + 16u * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) out += S.w3[16 * c + j] * fmaxf(v[j] + S.b2[16 * c + j], 0.0f);
+        }
+        if (valid) {
+            if (MODE == 0) {
+                y[r] = out;
+            } else {
+                const float4 a = __ldg(rec + 2 * r), b = __ldg(rec + 2 * r + 1);
+                const int point = __float_as_int(b.y);
+                const double v = (double)(b.x + a.w * out);
+                atomicAdd(accSum + point, v);
+                atomicAdd(accSq + point, v * v);
+                atomicAdd(accN + point, 1);
+                atomicAdd(reinterpret_cast<unsigned long long*>(accLen + point), (unsigned long long)__float_as_int(b.z));
+            }
+        }
+        umma::fenceBeforeSync();
+    }
+    if (!ok && tid == 0 && errw) atomicOr(errw, kErrTensorWait);
+    __syncthreads();
+    if (warp == 0) umma::dealloc(tmem, kTcCols);
+}
+
 // FP32 encoding of each point (levels beyond n_levels are 0): enc [n][32]
 template <int D>
 __global__ void encodeKernel(const Net N, const float* __restrict__ x, float* __restrict__ enc, int64_t n) {
@@ -379,6 +567,7 @@ struct zgpu_cache {
     __nv_bfloat16* W1lo = nullptr;
     __nv_bfloat16* W2lo = nullptr;
     double* loss = nullptr;
+    unsigned int* err = nullptr;       // device error word of the inference kernel
     float* stageX = nullptr;
     float* stageT = nullptr;
     int64_t stageCap = 0;
@@ -479,17 +668,17 @@ namespace zg {
 // walk-record accumulation used by zgpu_solve_cached (zgpu_api.cu)
 cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
                                   int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,
-                                  cudaStream_t s) {
+                                  unsigned int* errw, cudaStream_t s) {
     static bool a2 = false, a3 = false;
-    if (!a2) { cudaFuncSetAttribute(evalKernel<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem); a2 = true; }
-    if (!a3) { cudaFuncSetAttribute(evalKernel<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem); a3 = true; }
-    const int blocks = c->numSMs * 4;
+    if (!a2) { cudaFuncSetAttribute(evalKernelTc<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem); a2 = true; }
+    if (!a3) { cudaFuncSetAttribute(evalKernelTc<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem); a3 = true; }
+    const int blocks = c->numSMs * 2;
     if (c->cfg.dim == 2)
-        evalKernel<2, 1><<<blocks, kWarps * 32, kEvalSmem, s>>>(c->net, nullptr, nullptr, cap, rec, recCount, accSum,
-                                                               accSq, accN, accLen);
+        evalKernelTc<2, 1><<<blocks, kTcRows, kTcSmem, s>>>(c->net, nullptr, nullptr, cap, rec, recCount, accSum, accSq,
+                                                            accN, accLen, errw);
     else
-        evalKernel<3, 1><<<blocks, kWarps * 32, kEvalSmem, s>>>(c->net, nullptr, nullptr, cap, rec, recCount, accSum,
-                                                               accSq, accN, accLen);
+        evalKernelTc<3, 1><<<blocks, kTcRows, kTcSmem, s>>>(c->net, nullptr, nullptr, cap, rec, recCount, accSum, accSq,
+                                                            accN, accLen, errw);
     return cudaGetLastError();
 }
 int cacheDim(const zgpu_cache* c) { return c->cfg.dim; }
@@ -554,7 +743,7 @@ int zgpu_cache_create(zgpu_context* ctx, const zgpu_cache_config* cfg, zgpu_cach
         cudaMalloc(&c->W2b, kHidden * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
         cudaMalloc(&c->W1lo, kHidden * kInputs * sizeof(__nv_bfloat16)) != cudaSuccess ||
         cudaMalloc(&c->W2lo, kHidden * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
-        cudaMalloc(&c->loss, sizeof(double)) != cudaSuccess)
+        cudaMalloc(&c->loss, sizeof(double)) != cudaSuccess || cudaMalloc(&c->err, sizeof(unsigned int)) != cudaSuccess)
         return cleanup(cfail(ZGPU_ERR_OUT_OF_MEMORY, "cannot allocate the cache parameters (%zu bytes each)", bytes));
     N.table = reinterpret_cast<const __half2*>(c->tableHalf);
     N.W1 = c->W1b; N.W2 = c->W2b; N.W1lo = c->W1lo; N.W2lo = c->W2lo;
@@ -585,7 +774,8 @@ int zgpu_cache_destroy(zgpu_cache* c) {
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
     for (void* p : {(void*)c->master, (void*)c->grad, (void*)c->m, (void*)c->v, (void*)c->tableHalf, (void*)c->W1b,
-                    (void*)c->W2b, (void*)c->W1lo, (void*)c->W2lo, (void*)c->loss, (void*)c->stageX, (void*)c->stageT})
+                    (void*)c->W2b, (void*)c->W1lo, (void*)c->W2lo, (void*)c->loss, (void*)c->err, (void*)c->stageX,
+                    (void*)c->stageT})
         if (p) cudaFree(p);
     delete c;
     return ZGPU_OK;
@@ -699,19 +889,23 @@ int zgpu_cache_evaluate(zgpu_cache* c, int64_t n, const float* x, float* y, int 
     float* dy = y;
     if (memory == ZGPU_MEM_HOST) dy = c->stageT;
     static bool a2 = false, a3 = false;
-    if (!a2) { cudaFuncSetAttribute(evalKernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem); a2 = true; }
-    if (!a3) { cudaFuncSetAttribute(evalKernel<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvalSmem); a3 = true; }
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + kBlockRows - 1) / kBlockRows, (int64_t)c->numSMs * 8));
+    if (!a2) { cudaFuncSetAttribute(evalKernelTc<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem); a2 = true; }
+    if (!a3) { cudaFuncSetAttribute(evalKernelTc<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem); a3 = true; }
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, (int64_t)c->numSMs * 2));
+    ZC_CUDA(cudaMemsetAsync(c->err, 0, sizeof(unsigned int), c->stream));
     if (c->cfg.dim == 2)
-        evalKernel<2, 0><<<blocks, kWarps * 32, kEvalSmem, c->stream>>>(c->net, dx, dy, n, nullptr, nullptr, nullptr,
-                                                                        nullptr, nullptr, nullptr);
+        evalKernelTc<2, 0><<<blocks, kTcRows, kTcSmem, c->stream>>>(c->net, dx, dy, n, nullptr, nullptr, nullptr,
+                                                                    nullptr, nullptr, nullptr, c->err);
     else
-        evalKernel<3, 0><<<blocks, kWarps * 32, kEvalSmem, c->stream>>>(c->net, dx, dy, n, nullptr, nullptr, nullptr,
-                                                                        nullptr, nullptr, nullptr);
+        evalKernelTc<3, 0><<<blocks, kTcRows, kTcSmem, c->stream>>>(c->net, dx, dy, n, nullptr, nullptr, nullptr,
+                                                                    nullptr, nullptr, nullptr, c->err);
     ZC_CUDA(cudaGetLastError());
     if (memory == ZGPU_MEM_HOST)
         ZC_CUDA(cudaMemcpyAsync(y, dy, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    unsigned int err = 0;
+    ZC_CUDA(cudaMemcpyAsync(&err, c->err, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     ZC_CUDA(cudaStreamSynchronize(c->stream));
+    if (err) return cfail(ZGPU_ERR_DEVICE_STATE, "cache inference: device error word 0x%x", err);
     return ZGPU_OK;
 }
 

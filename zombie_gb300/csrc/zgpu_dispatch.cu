@@ -94,6 +94,17 @@ cudaError_t launchClosest(const BoundaryView& b, int dim, int64_t n, const float
     return dim == 2 ? Launch<2>::closest(b, n, x, computeSigned, pt, nrm, dist, prim, err, s)
                     : Launch<3>::closest(b, n, x, computeSigned, pt, nrm, dist, prim, err, s);
 }
+cudaError_t launchClosestCoop(const BoundaryView& b, int dim, int64_t n, const float* x, int computeSigned, float* pt,
+                              float* nrm, float* dist, int* prim, unsigned int* err, cudaStream_t s) {
+    return dim == 2 ? Launch<2>::closestCoop(b, n, x, computeSigned, pt, nrm, dist, prim, err, s)
+                    : Launch<3>::closestCoop(b, n, x, computeSigned, pt, nrm, dist, prim, err, s);
+}
+cudaError_t launchStarRadiusCoop(const BoundaryView& b, int dim, int64_t n, const float* x, const float* minR,
+                                 const float* maxR, float prec, const int* flip, float* out, unsigned int* err,
+                                 cudaStream_t s) {
+    return dim == 2 ? Launch<2>::starRadiusCoop(b, n, x, minR, maxR, prec, flip, out, err, s)
+                    : Launch<3>::starRadiusCoop(b, n, x, minR, maxR, prec, flip, out, err, s);
+}
 cudaError_t launchIntersect(const BoundaryView& b, int dim, int64_t n, const float* o, const float* nrmIn,
                             const float* dir, const float* tmax, const int* onb, int* hit, float* pt, float* nrm,
                             float* dist, int* prim, unsigned int* err, cudaStream_t s) {

@@ -110,7 +110,7 @@ int checkPdeFields(const zgpu_pde* pde, int D, bool hostGrids);
 // neural cache pass over the walk records (zgpu_cache.cu)
 cudaError_t launchCacheAccumulate(const zgpu_cache* c, const float4* rec, const unsigned long long* recCount,
                                   int64_t cap, double* accSum, double* accSq, int* accN, long long* accLen,
-                                  cudaStream_t s);
+                                  unsigned int* errw, cudaStream_t s);
 int cacheDim(const zgpu_cache* c);
 cudaStream_t cacheStream(const zgpu_cache* c);
 int contextDevice(const zgpu_context* ctx);
@@ -221,6 +221,12 @@ cudaError_t launchCountHits(const BoundaryView& b, int dim, int64_t n, const flo
 cudaError_t launchStarRadius(const BoundaryView& b, int dim, int64_t n, const float* x, const float* minR,
                              const float* maxR, float prec, const int* flip, float* out, unsigned int* err,
                              cudaStream_t s);
+// the same queries answered by one warp per query (closest points; Robin star radii)
+cudaError_t launchClosestCoop(const BoundaryView& b, int dim, int64_t n, const float* x, int computeSigned,
+                              float* pt, float* nrm, float* dist, int* prim, unsigned int* err, cudaStream_t s);
+cudaError_t launchStarRadiusCoop(const BoundaryView& b, int dim, int64_t n, const float* x, const float* minR,
+                                 const float* maxR, float prec, const int* flip, float* out, unsigned int* err,
+                                 cudaStream_t s);
 cudaError_t launchOccluded(const BoundaryView& b, int dim, int64_t n, const float* xi, const float* xj,
                            const float* ni, const float* nj, const int* oi, const int* oj, int* out,
                            unsigned int* err, cudaStream_t s);

@@ -600,6 +600,10 @@ struct Walker {
 };
 
 constexpr int kWalkThreads = 128;
+// minimum resident blocks per SM the walk kernel is compiled for (caps its registers)
+#ifndef ZG_WALK_MIN_BLOCKS
+#define ZG_WALK_MIN_BLOCKS 1
+#endif
 
 // Warp-cooperative search: the largest i in [0, nPoints) with walkStart[i] <= id (all 32
 // lanes take part; 32-ary narrowing with one coalesced probe per lane per round).
@@ -621,7 +625,7 @@ ZG_D int warpFindPoint(const SolveParams& P, long long id, int lane) {
 }
 
 template <int D, int SOLVER, bool SCREENED, bool BATCHED, bool COOP>
-__global__ void __launch_bounds__(kWalkThreads) walkKernel(const __grid_constant__ SolveParams P) {
+__global__ void __launch_bounds__(kWalkThreads, ZG_WALK_MIN_BLOCKS) walkKernel(const __grid_constant__ SolveParams P) {
     extern __shared__ int dynStack[];
     TravStack S{dynStack + threadIdx.x, reinterpret_cast<float*>(dynStack + P.stackEntries * blockDim.x) + threadIdx.x,
                 (int)blockDim.x, P.stackEntries};
@@ -939,6 +943,55 @@ __global__ void __launch_bounds__(kQueryThreads) starRadiusKernel(BoundaryView b
     if (err) atomicOr(errw, err);
 }
 
+// Warp-cooperative versions of the closest-point and Robin star-radius queries (the walk
+// kernel's coopClosest / coopRobinStarRadius): one warp answers one query at a time.
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) coopClosestKernel(BoundaryView b, int64_t n, const float* x,
+                                                                   int computeSigned, float* pt, float* nrm,
+                                                                   float* dist, int* prim, unsigned int* errw) {
+    __shared__ CoopWork work[kQueryThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t stride = (int64_t)gridDim.x * (kQueryThreads / 32);
+    uint32_t err = 0;
+    for (int64_t i = (int64_t)blockIdx.x * (kQueryThreads / 32) + warp; i < n; i += stride) {
+        const V<D> q = vload<D>(x + (size_t)i * D);
+        float d;
+        int slot;
+        coopClosest<D>(b, q, work[warp], lane, d, slot, err);
+        if (lane != 0) continue;
+        V<D> cp = q, nn = vzero<D>();
+        int idx = -1;
+        if (slot >= 0) {
+            const Prim<D> t = loadPrim<D>(b, slot);
+            closestOnPrim(t, q, cp);
+            nn = primNormal<D>(t);
+            idx = b.primIndex[slot];
+            if (computeSigned && dot(q - cp, nn) < 0.0f) d = -d;
+        }
+        if (pt) vstore<D>(cp, pt + (size_t)i * D);
+        if (nrm) vstore<D>(nn, nrm + (size_t)i * D);
+        if (dist) dist[i] = d;
+        if (prim) prim[i] = idx;
+    }
+    if (err && (threadIdx.x & 31) == 0) atomicOr(errw, err);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kQueryThreads) coopStarRadiusKernel(BoundaryView b, int64_t n, const float* x,
+                                                                      const float* minR, const float* maxR, float prec,
+                                                                      const int* flip, float* out, unsigned int* errw) {
+    __shared__ CoopWork work[kQueryThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t stride = (int64_t)gridDim.x * (kQueryThreads / 32);
+    uint32_t err = 0;
+    for (int64_t i = (int64_t)blockIdx.x * (kQueryThreads / 32) + warp; i < n; i += stride) {
+        const float r = coopRobinStarRadius<D>(b, vload<D>(x + (size_t)i * D), minR[i], maxR[i], prec,
+                                               flip && flip[i], work[warp], lane, err);
+        if (lane == 0) out[i] = r;
+    }
+    if (err && lane == 0) atomicOr(errw, err);
+}
+
 template <int D>
 __global__ void __launch_bounds__(kQueryThreads) occludedKernel(BoundaryView b, int64_t n, const float* xi, const float* xj, const float* ni,
                                const float* nj, const int* oi, const int* oj, int* out, unsigned int* errw) {
@@ -1073,6 +1126,21 @@ struct Launch {
         if (n == 0) return cudaSuccess;
         allowStack(detail::starRadiusKernel<D>);
         detail::starRadiusKernel<D><<<detail::gridFor(n, detail::kQueryThreads), detail::kQueryThreads, smemBytes(b.stackEntries, detail::kQueryThreads), s>>>(b, n, x, minR, maxR, prec, flip, out, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t closestCoop(const BoundaryView& b, int64_t n, const float* x, int computeSigned, float* pt,
+                                   float* nrm, float* dist, int* prim, unsigned int* err, cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        detail::coopClosestKernel<D><<<detail::gridFor(n, detail::kQueryThreads / 32), detail::kQueryThreads, 0, s>>>(
+            b, n, x, computeSigned, pt, nrm, dist, prim, err);
+        return cudaGetLastError();
+    }
+    static cudaError_t starRadiusCoop(const BoundaryView& b, int64_t n, const float* x, const float* minR,
+                                      const float* maxR, float prec, const int* flip, float* out, unsigned int* err,
+                                      cudaStream_t s) {
+        if (n == 0) return cudaSuccess;
+        detail::coopStarRadiusKernel<D><<<detail::gridFor(n, detail::kQueryThreads / 32), detail::kQueryThreads, 0, s>>>(
+            b, n, x, minR, maxR, prec, flip, out, err);
         return cudaGetLastError();
     }
     static cudaError_t occluded(const BoundaryView& b, int64_t n, const float* xi, const float* xj, const float* ni,

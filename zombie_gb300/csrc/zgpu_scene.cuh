@@ -25,7 +25,11 @@ constexpr int kEmptyChild = 0x7fffffff;
 constexpr int kMaxStack = 64;      // upper bound of the per-thread traversal stack (shared memory)
 constexpr int kMaxWideDepth = 20;   // 3 * depth + 2 <= kMaxStack
 // stack entries a traversal of a tree of the given wide depth can hold at once
-inline int stackEntriesForDepth(int depth) { int e = 3 * depth + 2; return e < 8 ? 8 : (e > kMaxStack ? kMaxStack : e); }
+// (a traversal holds at most width - 1 pushed siblings per level, plus slack)
+inline int stackEntriesForDepth(int depth, int width = 4) {
+    int e = (width - 1) * depth + 2;
+    return e < 8 ? 8 : (e > kMaxStack ? kMaxStack : e);
+}
 
 // Per-thread traversal stack in shared memory: entry k of this thread at [k * stride + lane].
 // Every query of a walk step reuses the same stack (they run one after another).
@@ -61,6 +65,7 @@ struct BoundaryView {
     const float4* silFeat = nullptr;
     int silNodes = 0;
     int robin = 0;
+    int width = 4;          // children per node: 4, or 8 (3D absorbing boundaries)
 };
 
 ZG_HD bool isLeaf(int c) { return c < 0; }
@@ -68,28 +73,38 @@ ZG_HD int leafFirst(int c) { return (-c - 1) >> 3; }
 ZG_HD int leafCount(int c) { return ((-c - 1) & 7) + 1; }
 ZG_HD int makeLeaf(int first, int count) { return -(1 + ((first << 3) | (count - 1))); }
 
-template <int D>
+// A node of W children (W = 4 or 8) is 2W float4: with G = W / 4 groups of 4 children,
+// float4 [i G + g] holds the lower bounds on axis i of children 4g .. 4g + 3, [(D + i) G + g]
+// the upper bounds, [2 D G + g] the child references and [(2 D + 1) G + g] the areas.
+template <int D, int W = 4>
 struct WideNode {
-    float lo[D][4], hi[D][4];
-    int child[4];
+    float lo[D][W], hi[D][W];
+    int child[W];
 };
 
-template <int D>
-ZG_D void loadNode(const BoundaryView& b, int n, WideNode<D>& w) {
-    const float4* p = b.nodes + (size_t)n * 8;
+template <int D, int W = 4>
+ZG_D void loadNode(const BoundaryView& b, int n, WideNode<D, W>& w) {
+    constexpr int G = W / 4;
+    const float4* p = b.nodes + (size_t)n * (2 * W);
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        float4 l = __ldg(p + i), h = __ldg(p + D + i);
-        w.lo[i][0] = l.x; w.lo[i][1] = l.y; w.lo[i][2] = l.z; w.lo[i][3] = l.w;
-        w.hi[i][0] = h.x; w.hi[i][1] = h.y; w.hi[i][2] = h.z; w.hi[i][3] = h.w;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            float4 l = __ldg(p + i * G + g), h = __ldg(p + (D + i) * G + g);
+            w.lo[i][4 * g] = l.x; w.lo[i][4 * g + 1] = l.y; w.lo[i][4 * g + 2] = l.z; w.lo[i][4 * g + 3] = l.w;
+            w.hi[i][4 * g] = h.x; w.hi[i][4 * g + 1] = h.y; w.hi[i][4 * g + 2] = h.z; w.hi[i][4 * g + 3] = h.w;
+        }
     }
-    int4 c = __ldg(reinterpret_cast<const int4*>(p + 2 * D));
-    w.child[0] = c.x; w.child[1] = c.y; w.child[2] = c.z; w.child[3] = c.w;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        int4 c = __ldg(reinterpret_cast<const int4*>(p + 2 * D * G + g));
+        w.child[4 * g] = c.x; w.child[4 * g + 1] = c.y; w.child[4 * g + 2] = c.z; w.child[4 * g + 3] = c.w;
+    }
 }
 ZG_D float4 loadNodeArea(const BoundaryView& b, int n, int D) { return __ldg(b.nodes + (size_t)n * 8 + 2 * D + 1); }
 
-template <int D>
-ZG_D float boxDist2(const WideNode<D>& w, int k, V<D> x) {
+template <int D, int W>
+ZG_D float boxDist2(const WideNode<D, W>& w, int k, V<D> x) {
     float s = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
@@ -99,8 +114,8 @@ ZG_D float boxDist2(const WideNode<D>& w, int k, V<D> x) {
     return s;
 }
 // slab test: entry distance of the ray (o, invDir) into child k within [0, tMax], or inf
-template <int D>
-ZG_D float boxRay(const WideNode<D>& w, int k, V<D> o, V<D> inv, float tMax) {
+template <int D, int W>
+ZG_D float boxRay(const WideNode<D, W>& w, int k, V<D> o, V<D> inv, float tMax) {
     float t0 = 0.0f, t1 = tMax;
 #pragma unroll
     for (int i = 0; i < D; i++) {
@@ -217,29 +232,56 @@ ZG_D bool rayPrim(const Prim<3>& t, V<3> o, V<3> d, float tMax, float& tHit) {
 // select among 4 register values by a runtime index (no local-memory array)
 ZG_D int pick4(int k, int a0, int a1, int a2, int a3) { return k == 0 ? a0 : k == 1 ? a1 : k == 2 ? a2 : a3; }
 ZG_D float pick4f(int k, float a0, float a1, float a2, float a3) { return k == 0 ? a0 : k == 1 ? a1 : k == 2 ? a2 : a3; }
+// the same over W registers
+template <int W, typename T>
+ZG_D T pickW(int k, const T (&a)[W]) {
+    if constexpr (W == 4) {
+        return k == 0 ? a[0] : k == 1 ? a[1] : k == 2 ? a[2] : a[3];
+    } else {
+        T v = a[0];
+#pragma unroll
+        for (int j = 1; j < W; j++) v = k == j ? a[j] : v;
+        return v;
+    }
+}
 
 // ---------------------------------------------------------------- child ordering
-// Up to 4 internal children sorted by key with a fixed network (constant indices keep the
-// arrays in registers); invalid slots carry key = +inf.
-struct ChildOrder {
-    float k[4];
-    int c[4];
+// Up to W internal children sorted by key with a fixed network (constant indices keep the
+// arrays in registers); invalid slots carry key = +inf.  W = 4: 5 comparators; W = 8: the
+// 19-comparator network (Knuth, TAOCP 5.3.4).
+template <int W = 4>
+struct ChildOrderW {
+    float k[W];
+    int c[W];
     ZG_D void clear() {
 #pragma unroll
-        for (int i = 0; i < 4; i++) { k[i] = kFltMax; c[i] = -1; }
+        for (int i = 0; i < W; i++) { k[i] = kFltMax; c[i] = -1; }
     }
     ZG_D void cswap(int a, int b) {
         bool sw = k[b] < k[a];
         float tk = sw ? k[b] : k[a]; k[b] = sw ? k[a] : k[b]; k[a] = tk;
         int tc = sw ? c[b] : c[a]; c[b] = sw ? c[a] : c[b]; c[a] = tc;
     }
-    ZG_D void sort() { cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2); }
+    ZG_D void sort() {
+        if constexpr (W == 4) {
+            cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2);
+        } else {
+            cswap(0, 2); cswap(1, 3); cswap(4, 6); cswap(5, 7);
+            cswap(0, 4); cswap(1, 5); cswap(2, 6); cswap(3, 7);
+            cswap(0, 1); cswap(2, 3); cswap(4, 5); cswap(6, 7);
+            cswap(2, 4); cswap(3, 5);
+            cswap(1, 4); cswap(3, 6);
+            cswap(1, 2); cswap(3, 4); cswap(5, 6);
+        }
+    }
 };
+using ChildOrder = ChildOrderW<4>;
 
-// after sort(): descend into slot 0 now, push slots 3, 2, 1 (farthest first) when within bound
-ZG_D int descendAndPush(ChildOrder& o, float bound, TravStack& S, int& sp, uint32_t& err) {
+// after sort(): descend into slot 0 now, push slots W-1 .. 1 (farthest first) when within bound
+template <int W>
+ZG_D int descendAndPush(ChildOrderW<W>& o, float bound, TravStack& S, int& sp, uint32_t& err) {
 #pragma unroll
-    for (int i = 3; i >= 1; i--) {
+    for (int i = W - 1; i >= 1; i--) {
         if (o.c[i] >= 0 && o.k[i] <= bound) {
             if (sp < S.cap) S.put(sp++, o.c[i], o.k[i]); else err |= kErrStackOverflow;
         }
@@ -264,8 +306,8 @@ struct ClosestHit {
     V<D> pt;
 };
 
-template <int D>
-__device__ __noinline__ ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err) {
+template <int D, int W>
+__device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err) {
     ClosestHit<D> best; best.d = kFltMax; best.slot = -1; best.pt = vzero<D>();
     float best2 = kFltMax;
     int bestIdx = 0x7fffffff;
@@ -273,13 +315,13 @@ __device__ __noinline__ ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x
     int sp = 0;
     int node = 0;
     for (;;) {
-        WideNode<D> w;
-        loadNode<D>(b, node, w);
-        ChildOrder ord; ord.clear();
+        WideNode<D, W> w;
+        loadNode<D, W>(b, node, w);
+        ChildOrderW<W> ord; ord.clear();
         unsigned leaves = 0;
-        float lk[4];
+        float lk[W];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < W; k++) {
             int c = w.child[k];
             float d2 = boxDist2<D>(w, k, x);
             lk[k] = d2;
@@ -290,8 +332,8 @@ __device__ __noinline__ ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
-            if (pick4f(k, lk[0], lk[1], lk[2], lk[3]) > best2) continue;   // pruned by a closer hit
-            int c = pick4(k, w.child[0], w.child[1], w.child[2], w.child[3]);
+            if (pickW<W>(k, lk) > best2) continue;   // pruned by a closer hit
+            int c = pickW<W>(k, w.child);
             int first = leafFirst(c), count = leafCount(c);
 #pragma unroll 1
             for (int j = 0; j < count; j++) {
@@ -310,6 +352,15 @@ __device__ __noinline__ ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x
         if (node < 0) break;
     }
     return best;
+}
+
+// closest point on a boundary of either node width (8-wide trees exist for 3D only)
+template <int D>
+ZG_D ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err) {
+    if constexpr (D == 3) {
+        if (b.width == 8) return closestPointW<D, 8>(b, x, S, err);
+    }
+    return closestPointW<D, 4>(b, x, S, err);
 }
 
 // ---------------------------------------------------------------- warp-cooperative closest point
@@ -333,17 +384,19 @@ struct CoopWork {
 ZG_D float comp4(float4 v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
 ZG_D int comp4i(int4 v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
 
-template <int D>
+template <int D, int NW = 4>
 ZG_D float childBoxDist2(const BoundaryView& b, int node, int c, V<D> x, int& child) {
-    const float4* p = b.nodes + (size_t)node * 8;
+    constexpr int G = NW / 4;
+    const float4* p = b.nodes + (size_t)node * (2 * NW) + (c >> 2);
+    const int cc = c & 3;
     float s = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        float lo = comp4(__ldg(p + i), c), hi = comp4(__ldg(p + D + i), c);
+        float lo = comp4(__ldg(p + i * G), cc), hi = comp4(__ldg(p + (D + i) * G), cc);
         float d = fmaxf(fmaxf(lo - x[i], 0.0f), x[i] - hi);
         s += d * d;
     }
-    child = comp4i(__ldg(reinterpret_cast<const int4*>(p + 2 * D)), c);
+    child = comp4i(__ldg(reinterpret_cast<const int4*>(p + 2 * D * G)), cc);
     return s;
 }
 
@@ -357,20 +410,22 @@ ZG_D void warpBest(float d, int idx, int slot, float& bestD, int& bestIdx, int& 
     if (dmin < bestD || (dmin == bestD && im < bestIdx)) { bestD = dmin; bestIdx = im; bestSlot = smin; }
 }
 
-template <int D>
-__device__ __noinline__ void coopClosest(const BoundaryView& b, V<D> x, CoopWork& W, int lane, float& outD,
-                                         int& outSlot, uint32_t& err) {
+template <int D, int NW>
+__device__ __noinline__ void coopClosestW(const BoundaryView& b, V<D> x, CoopWork& W, int lane, float& outD,
+                                          int& outSlot, uint32_t& err) {
+    constexpr int kShift = NW == 8 ? 3 : 2;        // lane = NW * entry + child
+    constexpr int kTake = 32 / NW;                 // stack entries per round
     float bestD = kFltMax, best2 = kFltMax;
     int bestIdx = 0x7fffffff, bestSlot = -1;
     outD = kFltMax; outSlot = -1;
     if (b.nNodes == 0) return;
-    const int c = lane & 3;
+    const int c = lane & (NW - 1);
     // greedy descent: follow the nearest child to a leaf and test its primitives
     {
         int node = 0;
         for (int guard = 0; guard < kMaxWideDepth + 2; guard++) {
             int child;
-            float d2 = childBoxDist2<D>(b, node, c, x, child);
+            float d2 = childBoxDist2<D, NW>(b, node, c, x, child);
             if (child == kEmptyChild) d2 = kFltMax;
             unsigned m = __reduce_min_sync(0xffffffffu, __float_as_uint(d2));
             int k = __ffs(__ballot_sync(0xffffffffu, __float_as_uint(d2) == m)) - 1;
@@ -393,16 +448,16 @@ __device__ __noinline__ void coopClosest(const BoundaryView& b, V<D> x, CoopWork
     int sp = 1;
     __syncwarp();
     while (sp > 0) {
-        const int take = min(8, sp);
+        const int take = min(kTake, sp);
         sp -= take;
-        const int e = lane >> 2;
+        const int e = lane >> kShift;
         int node = -1;
         float key = kFltMax;
         if (e < take) { node = W.node[sp + e]; key = W.key[sp + e]; }
         __syncwarp();
         int child = kEmptyChild;
         float d2 = kFltMax;
-        if (node >= 0 && key <= best2) d2 = childBoxDist2<D>(b, node, c, x, child);
+        if (node >= 0 && key <= best2) d2 = childBoxDist2<D, NW>(b, node, c, x, child);
         const bool ok = child != kEmptyChild && d2 <= best2;
         const bool inner = ok && !isLeaf(child), leaf = ok && isLeaf(child);
         // push the internal children
@@ -443,6 +498,14 @@ __device__ __noinline__ void coopClosest(const BoundaryView& b, V<D> x, CoopWork
     outSlot = bestSlot;
 }
 
+template <int D>
+ZG_D void coopClosest(const BoundaryView& b, V<D> x, CoopWork& W, int lane, float& outD, int& outSlot, uint32_t& err) {
+    if constexpr (D == 3) {
+        if (b.width == 8) { coopClosestW<D, 8>(b, x, W, lane, outD, outSlot, err); return; }
+    }
+    coopClosestW<D, 4>(b, x, W, lane, outD, outSlot, err);
+}
+
 // ---------------------------------------------------------------- first ray hit
 template <int D>
 struct RayHit {
@@ -458,9 +521,9 @@ ZG_D V<D> safeInv(V<D> d) {
 }
 
 // anyHit = true stops at the first intersection (line-of-sight queries)
-template <int D>
-__device__ __noinline__ RayHit<D> intersectRay(const BoundaryView& b, V<D> o, V<D> dir, float tMax, bool anyHit,
-                                               TravStack& S, uint32_t& err) {
+template <int D, int W>
+__device__ __noinline__ RayHit<D> intersectRayW(const BoundaryView& b, V<D> o, V<D> dir, float tMax, bool anyHit,
+                                                TravStack& S, uint32_t& err) {
     RayHit<D> hit; hit.t = tMax; hit.slot = -1;
     int bestIdx = 0x7fffffff;
     if (b.nNodes == 0) return hit;
@@ -468,12 +531,12 @@ __device__ __noinline__ RayHit<D> intersectRay(const BoundaryView& b, V<D> o, V<
     int sp = 0;
     int node = 0;
     for (;;) {
-        WideNode<D> w;
-        loadNode<D>(b, node, w);
-        ChildOrder ord; ord.clear();
+        WideNode<D, W> w;
+        loadNode<D, W>(b, node, w);
+        ChildOrderW<W> ord; ord.clear();
         unsigned leaves = 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < W; k++) {
             int c = w.child[k];
             float tn = boxRay<D>(w, k, o, inv, hit.t);
             bool ok = c != kEmptyChild && tn != kFltMax;
@@ -483,7 +546,7 @@ __device__ __noinline__ RayHit<D> intersectRay(const BoundaryView& b, V<D> o, V<
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
-            int c = pick4(k, w.child[0], w.child[1], w.child[2], w.child[3]);
+            int c = pickW<W>(k, w.child);
             int first = leafFirst(c), count = leafCount(c);
 #pragma unroll 1
             for (int j = 0; j < count; j++) {
@@ -506,20 +569,30 @@ __device__ __noinline__ RayHit<D> intersectRay(const BoundaryView& b, V<D> o, V<
     return hit;
 }
 
-// number of hits within tMax (intersect...AllHits, used by insideDomain)
+// first hit (anyHit: any hit) on a boundary of either node width
 template <int D>
-__device__ __noinline__ int countHits(const BoundaryView& b, V<D> o, V<D> dir, float tMax, TravStack& S, uint32_t& err) {
+ZG_D RayHit<D> intersectRay(const BoundaryView& b, V<D> o, V<D> dir, float tMax, bool anyHit, TravStack& S,
+                            uint32_t& err) {
+    if constexpr (D == 3) {
+        if (b.width == 8) return intersectRayW<D, 8>(b, o, dir, tMax, anyHit, S, err);
+    }
+    return intersectRayW<D, 4>(b, o, dir, tMax, anyHit, S, err);
+}
+
+// number of hits within tMax (intersect...AllHits, used by insideDomain)
+template <int D, int W>
+__device__ __noinline__ int countHitsW(const BoundaryView& b, V<D> o, V<D> dir, float tMax, TravStack& S, uint32_t& err) {
     if (b.nNodes == 0) return 0;
     V<D> inv = safeInv<D>(dir);
     int sp = 1;
     S.put(0, 0, 0.0f);
     int hits = 0;
     while (sp > 0) {
-        WideNode<D> w;
-        loadNode<D>(b, S.nodeAt(--sp), w);
+        WideNode<D, W> w;
+        loadNode<D, W>(b, S.nodeAt(--sp), w);
         unsigned leaves = 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < W; k++) {
             int c = w.child[k];
             if (c == kEmptyChild || boxRay<D>(w, k, o, inv, tMax) == kFltMax) continue;
             if (isLeaf(c)) leaves |= 1u << k;
@@ -529,7 +602,7 @@ __device__ __noinline__ int countHits(const BoundaryView& b, V<D> o, V<D> dir, f
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
-            int c = pick4(k, w.child[0], w.child[1], w.child[2], w.child[3]);
+            int c = pickW<W>(k, w.child);
             int first = leafFirst(c), count = leafCount(c);
 #pragma unroll 1
             for (int j = 0; j < count; j++) {
@@ -539,6 +612,14 @@ __device__ __noinline__ int countHits(const BoundaryView& b, V<D> o, V<D> dir, f
         }
     }
     return hits;
+}
+
+template <int D>
+ZG_D int countHits(const BoundaryView& b, V<D> o, V<D> dir, float tMax, TravStack& S, uint32_t& err) {
+    if constexpr (D == 3) {
+        if (b.width == 8) return countHitsW<D, 8>(b, o, dir, tMax, S, err);
+    }
+    return countHitsW<D, 4>(b, o, dir, tMax, S, err);
 }
 
 // ---------------------------------------------------------------- silhouettes
