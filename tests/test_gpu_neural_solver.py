@@ -24,7 +24,9 @@ def _setup(seed=0):
     gp = GpuProblem(pr)
     cache = make_cache(gp.queries, 3, log2_table_size=17, max_resolution=48.0, learning_rate_grid=1e-2,
                        learning_rate_mlp=5e-3, seed=seed)
-    ncs = NeuralCacheSolver(gp.solver, gp.pde, pr.settings, cache, min_distance=0.05, error_bound=5e-3)
+    # the gate admits a cache that adds at most a third of the plain solve's error at the
+    # test's walk count (RMSE ~0.03 at 64 walks per point)
+    ncs = NeuralCacheSolver(gp.solver, gp.pde, pr.settings, cache, min_distance=0.05, error_bound=1e-2)
     return pr, gp, ncs
 
 
@@ -36,8 +38,8 @@ def test_trained_cache_gains_over_the_plain_walk(zgpu):
     pr, gp, ncs = _setup()
     rng = np.random.default_rng(1)
     x, d = ncs.sample_interior(1 << 18, rng)
-    ncs.train(x, d, spp=16, steps=2500, batch_size=1 << 15)
-    for r in range(3):
+    ncs.train(x, d, spp=16, steps=1500, batch_size=1 << 15)
+    for r in range(2):
         x, d = ncs.sample_interior(1 << 18, rng)
         ncs.train(x, d, spp=16, steps=800, batch_size=1 << 15, seed_base=(r + 2) << 44, cached=True)
     xc, dc = ncs.sample_interior(8192, np.random.default_rng(2))

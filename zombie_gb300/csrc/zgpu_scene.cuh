@@ -306,12 +306,21 @@ struct ClosestHit {
     V<D> pt;
 };
 
+// seed >= 0: a primitive slot tested first, whose distance bounds the search from the start
+// (the walk's previous closest primitive); the answer is the same primitive of least
+// (distance, index) with or without it, as every comparison and pruning test is inclusive.
 template <int D, int W>
-__device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err) {
+__device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err,
+                                                    int seed) {
     ClosestHit<D> best; best.d = kFltMax; best.slot = -1; best.pt = vzero<D>();
     float best2 = kFltMax;
     int bestIdx = 0x7fffffff;
     if (b.nNodes == 0) return best;
+    if (seed >= 0) {
+        V<D> q;
+        best.d = closestOnPrim(loadPrim<D>(b, seed), x, q);
+        best.slot = seed; best.pt = q; best2 = best.d * best.d; bestIdx = __ldg(b.primIndex + seed);
+    }
     int sp = 0;
     int node = 0;
     for (;;) {
@@ -356,11 +365,11 @@ __device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> 
 
 // closest point on a boundary of either node width (8-wide trees exist for 3D only)
 template <int D>
-ZG_D ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err) {
+ZG_D ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err, int seed = -1) {
     if constexpr (D == 3) {
-        if (b.width == 8) return closestPointW<D, 8>(b, x, S, err);
+        if (b.width == 8) return closestPointW<D, 8>(b, x, S, err, seed);
     }
-    return closestPointW<D, 4>(b, x, S, err);
+    return closestPointW<D, 4>(b, x, S, err, seed);
 }
 
 // ---------------------------------------------------------------- warp-cooperative closest point
