@@ -122,7 +122,7 @@ struct Walker {
     ZG_D void closestQuery() {
         if (kCoopClosest && SC().hasAbs) { queryPending = true; cpValid = false; return; }
         if (SC().hasAbs) {
-            ClosestHit<D> h = closestPoint<D>(SC().absorbing, pt, S, err, cpSeed);
+            ClosestHit<D> h = closestPoint<D, SOLVER == ZGPU_SOLVER_WALK_ON_STARS>(SC().absorbing, pt, S, err, cpSeed);
             cpSeed = h.slot;
             distAbs = h.d;
             cpPt = h.pt;

@@ -277,15 +277,32 @@ struct ChildOrderW {
 };
 using ChildOrder = ChildOrderW<4>;
 
-// after sort(): descend into slot 0 now, push slots W-1 .. 1 (farthest first) when within bound
-template <int W>
-ZG_D int descendAndPush(ChildOrderW<W>& o, float bound, TravStack& S, int& sp, uint32_t& err) {
+// Loop over W children either unrolled or kept as a loop (COMPACT): the Walk on Stars kernel
+// runs five traversals per step and is bound by instruction fetch under divergence, so its
+// traversals take the compact form (measured +11% walk-steps/s on the 2D mixed workload);
+// Walk on Spheres runs one traversal per step and keeps the unrolled form (the compact form
+// measured -27% there).
+template <int W, bool COMPACT, typename F>
+ZG_D void forChildren(F&& f) {
+    if constexpr (COMPACT) {
+#pragma unroll 1
+        for (int k = 0; k < W; k++) f(k);
+    } else {
 #pragma unroll
-    for (int i = W - 1; i >= 1; i--) {
+        for (int k = 0; k < W; k++) f(k);
+    }
+}
+
+// after sort(): descend into slot 0 now, push slots W-1 .. 1 (farthest first) when within bound
+template <int W, bool COMPACT = false>
+ZG_D int descendAndPush(ChildOrderW<W>& o, float bound, TravStack& S, int& sp, uint32_t& err) {
+    auto push = [&](int j) {
+        const int i = W - 1 - j;
         if (o.c[i] >= 0 && o.k[i] <= bound) {
             if (sp < S.cap) S.put(sp++, o.c[i], o.k[i]); else err |= kErrStackOverflow;
         }
-    }
+    };
+    forChildren<W - 1, COMPACT>(push);
     return (o.c[0] >= 0 && o.k[0] <= bound) ? o.c[0] : -1;
 }
 
@@ -309,7 +326,7 @@ struct ClosestHit {
 // seed >= 0: a primitive slot tested first, whose distance bounds the search from the start
 // (the walk's previous closest primitive); the answer is the same primitive of least
 // (distance, index) with or without it, as every comparison and pruning test is inclusive.
-template <int D, int W>
+template <int D, int W, bool COMPACT>
 __device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err,
                                                     int seed) {
     ClosestHit<D> best; best.d = kFltMax; best.slot = -1; best.pt = vzero<D>();
@@ -329,15 +346,14 @@ __device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> 
         ChildOrderW<W> ord; ord.clear();
         unsigned leaves = 0;
         float lk[W];
-#pragma unroll
-        for (int k = 0; k < W; k++) {
+        forChildren<W, COMPACT>([&](int k) {
             int c = w.child[k];
             float d2 = boxDist2<D>(w, k, x);
             lk[k] = d2;
             bool ok = c != kEmptyChild && d2 <= best2;
             if (ok && isLeaf(c)) leaves |= 1u << k;
             if (ok && !isLeaf(c)) { ord.k[k] = d2; ord.c[k] = c; }
-        }
+        });
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
@@ -356,7 +372,7 @@ __device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> 
             }
         }
         ord.sort();
-        int next = descendAndPush(ord, best2, S, sp, err);
+        int next = descendAndPush<W, COMPACT>(ord, best2, S, sp, err);
         node = next >= 0 ? next : popWithin(best2, S, sp);
         if (node < 0) break;
     }
@@ -364,12 +380,12 @@ __device__ __noinline__ ClosestHit<D> closestPointW(const BoundaryView& b, V<D> 
 }
 
 // closest point on a boundary of either node width (8-wide trees exist for 3D only)
-template <int D>
+template <int D, bool COMPACT = false>
 ZG_D ClosestHit<D> closestPoint(const BoundaryView& b, V<D> x, TravStack& S, uint32_t& err, int seed = -1) {
     if constexpr (D == 3) {
-        if (b.width == 8) return closestPointW<D, 8>(b, x, S, err, seed);
+        if (b.width == 8) return closestPointW<D, 8, COMPACT>(b, x, S, err, seed);
     }
-    return closestPointW<D, 4>(b, x, S, err, seed);
+    return closestPointW<D, 4, COMPACT>(b, x, S, err, seed);
 }
 
 // ---------------------------------------------------------------- warp-cooperative closest point
@@ -544,14 +560,13 @@ __device__ __noinline__ RayHit<D> intersectRayW(const BoundaryView& b, V<D> o, V
         loadNode<D, W>(b, node, w);
         ChildOrderW<W> ord; ord.clear();
         unsigned leaves = 0;
-#pragma unroll
-        for (int k = 0; k < W; k++) {
+        forChildren<W, true>([&](int k) {
             int c = w.child[k];
             float tn = boxRay<D>(w, k, o, inv, hit.t);
             bool ok = c != kEmptyChild && tn != kFltMax;
             if (ok && isLeaf(c)) leaves |= 1u << k;
             if (ok && !isLeaf(c)) { ord.k[k] = tn; ord.c[k] = c; }
-        }
+        });
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
@@ -571,7 +586,7 @@ __device__ __noinline__ RayHit<D> intersectRayW(const BoundaryView& b, V<D> o, V
             }
         }
         ord.sort();
-        int next = descendAndPush(ord, hit.t, S, sp, err);
+        int next = descendAndPush<W, true>(ord, hit.t, S, sp, err);
         node = next >= 0 ? next : popWithin(hit.t, S, sp);
         if (node < 0) break;
     }
@@ -600,14 +615,13 @@ __device__ __noinline__ int countHitsW(const BoundaryView& b, V<D> o, V<D> dir, 
         WideNode<D, W> w;
         loadNode<D, W>(b, S.nodeAt(--sp), w);
         unsigned leaves = 0;
-#pragma unroll
-        for (int k = 0; k < W; k++) {
+        forChildren<W, true>([&](int k) {
             int c = w.child[k];
-            if (c == kEmptyChild || boxRay<D>(w, k, o, inv, tMax) == kFltMax) continue;
+            if (c == kEmptyChild || boxRay<D>(w, k, o, inv, tMax) == kFltMax) return;
             if (isLeaf(c)) leaves |= 1u << k;
             else if (sp < S.cap) S.put(sp++, c, 0.0f);
             else err |= kErrStackOverflow;
-        }
+        });
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
@@ -921,15 +935,14 @@ __device__ __noinline__ float silhouetteRadius2(const BoundaryView& b, V<D> x, f
         loadNode<D>(t, node, w);
         ChildOrder ord; ord.clear();
         unsigned leaves = 0;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
+        forChildren<4, true>([&](int k) {
             int c = w.child[k];
             float d2 = boxDist2<D>(w, k, x);
             bool ok = c != kEmptyChild && d2 < r2 &&
                       coneMayHoldSilhouette<D>(__ldg(b.silCones + (size_t)node * 8 + k), w, k, x, prec);
             if (ok && isLeaf(c)) leaves |= 1u << k;
             if (ok && !isLeaf(c)) { ord.k[k] = d2; ord.c[k] = c; }
-        }
+        });
         while (leaves) {
             int k = __ffs(leaves) - 1;
             leaves &= leaves - 1;
@@ -939,7 +952,7 @@ __device__ __noinline__ float silhouetteRadius2(const BoundaryView& b, V<D> x, f
             for (int j = 0; j < count; j++) featureRadius(b, first + j, x, r2, flip, prec);
         }
         ord.sort();
-        int next = descendAndPush(ord, r2, S, sp, err);
+        int next = descendAndPush<4, true>(ord, r2, S, sp, err);
         node = next >= 0 ? next : popWithin(r2, S, sp);
         if (node < 0) break;
     }
