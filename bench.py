@@ -555,10 +555,11 @@ def run_gpu(args):
     pr, desc = make_problem(args.workload)
     ctx = Context(local)
     options = None
-    if args.bvh_width or args.query_mode:
+    if args.bvh_width or args.query_mode or args.schedule:
         options = A.SolveOptions()
         options.bvh_width = args.bvh_width
         options.query_mode = args.query_mode
+        options.schedule = args.schedule
     gp = GpuProblem(pr, context=ctx, seed_base=0x5eed + rank, options=options)
     if args.autotune:
         import ctypes as C
@@ -916,6 +917,8 @@ def main():
     ap.add_argument("--workload", default="mixed_wost_2d", choices=sorted(WORKLOADS))
     ap.add_argument("--bvh-width", type=int, default=0, help="solve option bvh_width (8: 8-wide 3D absorbing tree)")
     ap.add_argument("--query-mode", type=int, default=0, help="solve option query_mode (1 lane, 2 warp per query)")
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="solve option schedule of the Walk on Stars loop (0 auto, 1 persistent, 2 wavefront)")
     ap.add_argument("--autotune", action="store_true", help="run zgpu_autotune on the workload before timing")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) solves of extra lines")
     ap.add_argument("--cpu-points", type=int, default=0,

@@ -50,6 +50,7 @@ ZGPU_STATIC_MAX_POINTS = 65536
 ZGPU_STATIC_SCRATCH_BYTES = 4 << 20
 FLT_MAX = 3.4028234663852886e38
 ZGPU_QUERY_MODE_AUTO, ZGPU_QUERY_MODE_LANE, ZGPU_QUERY_MODE_WARP = 0, 1, 2
+ZGPU_SCHEDULE_AUTO, ZGPU_SCHEDULE_PERSISTENT, ZGPU_SCHEDULE_WAVEFRONT = 0, 1, 2
 
 
 class Analytic(C.Structure):
@@ -159,7 +160,7 @@ class SolveOptions(C.Structure):
         ("query_mode", C.c_int32),
         ("step_budget", C.c_int64),
         ("bvh_width", C.c_int32),
-        ("reserved", C.c_int32),
+        ("schedule", C.c_int32),
     ]
 
 

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["zgpu_walk_2d_wos.cu", "zgpu_walk_2d_wost.cu", "zgpu_walk_3d_wos.cu", "zgpu_walk_3d_wost.cu",
            "zgpu_kernels2.cu", "zgpu_kernels3.cu", "zgpu_dispatch.cu", "zgpu_api.cu", "zgpu_build.cpp", "zgpu_static.cu",
            "zgpu_cache.cu", "zgpu_devbuild.cu", "zgpu_bvc.cu", "zgpu_rws.cu"]
-HEADERS = ["zgpu_kernels.cuh", "zgpu_scene.cuh", "zgpu_math.cuh", "zgpu_internal.h", "zgpu_build.h", "zgpu_cache.cuh",
+HEADERS = ["zgpu_kernels.cuh", "zgpu_wave.cuh", "zgpu_scene.cuh", "zgpu_math.cuh", "zgpu_internal.h", "zgpu_build.h", "zgpu_cache.cuh",
            "zgpu_umma.cuh"]
 
 

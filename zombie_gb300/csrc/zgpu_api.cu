@@ -69,7 +69,7 @@ struct zgpu_context {
            kQ0, kQ1, kQ2, kQ3, kQ4, kQ5, kQ6, kQ7, kQ8, kQ9, kQ10, kQ11, kSplitScratch, kCacheRec, kSceneTable, kSceneId,
            kDistRefl, kGMean, kGM2, kGN, kAccGrad, kAccGradSq, kAccGradN, kDirDeriv, kFirstSrc, kDeriv, kAccFirstSrc,
            kAccDeriv, kB0, kB1, kB2, kB3, kB4, kB5, kB6, kB7, kB8, kB9, kB10, kB11, kB12, kB13, kB14, kB15, kB16, kB17,
-           kB18, kB19, kNumBufs };
+           kB18, kB19, kWaveA, kWaveB, kWaveKey, kWaveRank, kWaveCount, kWaveOffset, kWaveCtr, kNumBufs };
     Buf bufs[kNumBufs];
     unsigned long long* hostCounters = nullptr;   // pinned: counters + error word
     // use_graph: the captured prepare/scan/walk/finalize sequence, replayed while the solve's
@@ -736,6 +736,59 @@ int wideTwin(zgpu_boundary* b, zgpu_boundary** out) {
 
 // zgpu_solve, zgpu_solve_cached and zgpu_solve_batched.  nScenes > 1: points->scene_id
 // selects each point's row of q / pde / ws.
+// The sorted-wavefront Walk on Stars loop (zgpu_wave.cuh): iterations of sort, refill and
+// the two step kernels over a pool of walk records until no walk is left.  The host reads the
+// live count every kWaveCheck iterations (the iterations between run on an empty pool).
+constexpr long long kWavePool = 1LL << 21;
+constexpr int kWaveCheck = 8;
+
+int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s) {
+    using C = zgpu_context;
+    SolveParams P = P0;
+    P.splitStack = nullptr;   // no split scratch: a split reports kErrSplitOverflow
+    long long total = 0;
+    ZG_CUDA(cudaMemcpyAsync(&total, P.walkStart + P.nPoints, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+    if (total <= 0) return ZGPU_OK;
+    const long long pool = std::min(total, kWavePool);
+    const int vec = waveRecordVec(D);
+    WaveParams w;
+    float4 *a = nullptr, *b = nullptr;
+    ZG_TRY(scratch<float4>(ctx, C::kWaveA, (size_t)pool * vec, &a));
+    ZG_TRY(scratch<float4>(ctx, C::kWaveB, (size_t)pool * vec, &b));
+    ZG_TRY(scratch<uint32_t>(ctx, C::kWaveKey, (size_t)pool, &w.key));
+    ZG_TRY(scratch<uint32_t>(ctx, C::kWaveRank, (size_t)pool, &w.rank));
+    ZG_TRY(scratch<uint32_t>(ctx, C::kWaveCount, (size_t)kWaveCells, &w.count));
+    ZG_TRY(scratch<uint32_t>(ctx, C::kWaveOffset, (size_t)kWaveCells + 1, &w.offset));
+    ZG_TRY(scratch<long long>(ctx, C::kWaveCtr, 4, &w.ctr));
+    ZG_CUDA(cudaMemsetAsync(w.count, 0, kWaveCells * sizeof(uint32_t), s));
+    ZG_CUDA(cudaMemsetAsync(w.ctr, 0, 4 * sizeof(long long), s));
+    w.pool = pool;
+    const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.sc.pde.absorption_coeff > 0.0f);
+    // a slot holds one walk for at most max_walk_length + 1 iterations, so every walk has
+    // started after ceil(total / pool) such rounds and ended one round later
+    const double rounds = (double)((total + pool - 1) / pool + 1);
+    const double maxIter = rounds * ((double)P.sc.ws.max_walk_length + 1.0) + 2.0 * kWaveCheck;
+    float4* src = a;
+    float4* dst = b;
+    for (long long it = 0;;) {
+        for (int k = 0; k < kWaveCheck; k++, it++) {
+            w.src = src;
+            w.dst = dst;
+            ZG_CUDA(launchWaveIteration(P, w, D, blocks, ctx->numSMs, s));
+            std::swap(src, dst);
+        }
+        long long live = 0;
+        ZG_CUDA(cudaMemcpyAsync(&live, w.ctr + kWaveLive, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        ZG_CUDA(cudaStreamSynchronize(s));
+        if (live == 0) break;
+        if ((double)it > maxIter)
+            return fail(ZGPU_ERR_DEVICE_STATE, "the wavefront schedule still had %lld live walks after %lld iterations",
+                        live, it);
+    }
+    return ZGPU_OK;
+}
+
 int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_queries* q, const zgpu_pde* pde,
               const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,
               const zgpu_solve_options* opt, zgpu_cache* cache, float cacheMinDist, zgpu_solve_report* report) {
@@ -870,6 +923,20 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     // interior points under the reflectance bounds, the case the warp-wide traversal serves
     if (solver == ZGPU_SOLVER_WALK_ON_STARS && P.sc.hasRefl && q->reflecting->kind == ZGPU_BOUNDARY_ROBIN && !batched)
         P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
+    // the Walk on Stars loop's schedule: the sorted wavefront serves single-scene solution
+    // solves without neural cache, graph replay, split scratch or warp-wide queries
+    const int schedule = opt ? opt->schedule : ZGPU_SCHEDULE_AUTO;
+    if (schedule < ZGPU_SCHEDULE_AUTO || schedule > ZGPU_SCHEDULE_WAVEFRONT)
+        return fail(ZGPU_ERR_INVALID_ARG, "schedule must be 0, 1 or 2");
+    const bool waveServes = solver == ZGPU_SOLVER_WALK_ON_STARS && !batched && !gradients && !cache &&
+                            !(opt && opt->use_graph) && queryMode != ZGPU_QUERY_MODE_WARP &&
+                            P.sc.pde.are_robin_coeffs_nonnegative && P.sc.ws.splitting_threshold >= 2.0f;
+    if (schedule == ZGPU_SCHEDULE_WAVEFRONT && !waveServes)
+        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves Walk on Stars solves of one scene, solutions "
+                                          "only, without cache, graph or warp-wide queries, with non-negative Robin "
+                                          "coefficients and splitting_threshold >= 2");
+    const bool useWave = waveServes && (schedule == ZGPU_SCHEDULE_WAVEFRONT || (schedule == ZGPU_SCHEDULE_AUTO && D == 2));
+    if (useWave) P.coopStar = 0;
     if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
                                               : walkKernelMaxBlocksPerSM(D, solver, threads, P);
@@ -919,7 +986,10 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     }
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (P.coop) P.stackEntries = 0;     // the prepare kernel above used the per-thread stacks
-    if (n > 0) ZG_CUDA(launchWalk(P, D, blocks, threads, s));
+    if (n > 0) {
+        if (useWave) ZG_TRY(runWave(ctx, P, D, s));
+        else ZG_CUDA(launchWalk(P, D, blocks, threads, s));
+    }
     if (cache && n > 0)
         ZG_CUDA(launchCacheAccumulate(cache, P.cacheRec, P.counters + kCtrCache, P.cacheCap, P.accSum, P.accSq,
                                       P.accN, P.accLen, P.errorWord, s));

@@ -1,5 +1,5 @@
 // zgpu_dispatch.cu -- dimension dispatch of the kernel launchers and the walk-id scan.
-#include "zgpu_kernels.cuh"
+#include "zgpu_wave.cuh"
 
 namespace zg {
 
@@ -9,6 +9,8 @@ extern template struct WalkLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>;
 extern template struct WalkLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>;
 extern template struct WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>;
 extern template struct WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>;
+extern template struct WaveLaunch<2>;
+extern template struct WaveLaunch<3>;
 
 namespace detail {
 // ------------------------------------------------------------------------- scan
@@ -78,6 +80,13 @@ cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, c
     return wos ? WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::walk(p, blocks, threads, s)
                : WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::walk(p, blocks, threads, s);
 }
+cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s) {
+    return dim == 2 ? WaveLaunch<2>::iterate(p, w, blocks, numSMs, s) : WaveLaunch<3>::iterate(p, w, blocks, numSMs, s);
+}
+int waveBlocksPerSM(int dim, bool screened) {
+    return dim == 2 ? WaveLaunch<2>::blocksPerSM(screened) : WaveLaunch<3>::blocksPerSM(screened);
+}
+int waveRecordVec(int dim) { return dim == 2 ? WaveLaunch<2>::kVec : WaveLaunch<3>::kVec; }
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p) {
     const bool wos = solver == ZGPU_SOLVER_WALK_ON_SPHERES;
     const size_t smem = walkSmemBytes(p, threads);

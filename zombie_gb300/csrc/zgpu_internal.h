@@ -92,6 +92,22 @@ struct SolveParams {
     long long stepBudget;
 };
 
+// the sorted-wavefront Walk on Stars schedule (zgpu_wave.cuh): its pool of walk records and
+// the sort's scratch (device memory)
+struct WaveParams {
+    const float4* src;        // records of the previous iteration
+    float4* dst;              // records of this iteration (sorted, then refilled)
+    uint32_t* key;            // [pool] Morton cell of each record of src (kWaveCells: free)
+    uint32_t* rank;           // [pool] the record's place in its cell
+    uint32_t* count;          // [kWaveCells] records per cell (zeroed by the scan)
+    uint32_t* offset;         // [kWaveCells + 1] first slot of each cell in dst
+    long long* ctr;           // [0] next walk id, [1] sorted live records, [2] first new id, [3] live slots
+    long long pool;           // records per buffer
+};
+
+enum : int { kWaveNext = 0, kWaveSorted = 1, kWaveFirstNew = 2, kWaveLive = 3 };
+constexpr int kWaveCells = 1 << 16;   // cells of the sort (2D 256^2; 3D uses the first 32^3)
+
 constexpr int kSplitStack = 8;
 // Walk on Spheres in 3D answers closest-point queries with a whole warp from this many
 // absorbing primitives on (query_mode 0)
@@ -104,6 +120,11 @@ cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);
 cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStream_t s);
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
+// one iteration of the sorted-wavefront Walk on Stars loop (zgpu_wave.cuh); blocks: of the
+// two step kernels (numSMs x waveBlocksPerSM)
+cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s);
+int waveBlocksPerSM(int dim, bool screened);
+int waveRecordVec(int dim);
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p);
 // validates a PDE's field kinds and grids (hostGrids: grid values may be in host memory)
 int checkPdeFields(const zgpu_pde* pde, int D, bool hostGrids);

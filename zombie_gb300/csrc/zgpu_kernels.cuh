@@ -601,6 +601,195 @@ struct Walker {
         }
         return stepWoSt();
     }
+
+    // ------------------------------------------------- sorted-wavefront Walk on Stars step
+    // The wavefront schedule (zgpu_wave.cuh) keeps each walk's state in a record in device
+    // memory between kernels and runs one step as two kernels over records sorted by
+    // position: waveRadius (the closest-point query that ends the previous step, the
+    // absorbing-boundary test and this step's star radius) and waveAdvance (the rest of the
+    // step).  Together they run stepWoSt's statements in its order; only the closest-point
+    // query moves from the end of one step to the start of the next, with no random number
+    // drawn in between.  Solves on this schedule have no neural cache, no gradient walks, no
+    // split scratch and no warp-wide queries, so those branches of stepWoSt are absent here;
+    // stepWoSt itself stays as it is, its code generation being sensitive to its shape.
+    static constexpr int kWaveVec = D == 2 ? 5 : 6;   // float4 per record
+
+    // record words: pt, nrm, prevDir (D each), prevDist, thr, distAbs, fsr (this step's
+    // radius once waveRadius has run), totRefl, totSrc, pcg32 state and increment (two words
+    // each), point (-1: a free slot), wlen, closest-point seed, flags
+    ZG_D void waveLoad(const float4* rec) {
+        float w[4 * kWaveVec];
+#pragma unroll
+        for (int v = 0; v < kWaveVec; v++) {
+            const float4 q = rec[v];
+            w[4 * v] = q.x; w[4 * v + 1] = q.y; w[4 * v + 2] = q.z; w[4 * v + 3] = q.w;
+        }
+#pragma unroll
+        for (int i = 0; i < D; i++) { pt[i] = w[i]; nrm[i] = w[D + i]; prevDir[i] = w[2 * D + i]; }
+        constexpr int o = 3 * D;
+        prevDist = w[o]; thr = w[o + 1]; distAbs = w[o + 2]; fsr = w[o + 3]; totRefl = w[o + 4]; totSrc = w[o + 5];
+        rng.state = (uint64_t)__float_as_uint(w[o + 6]) | ((uint64_t)__float_as_uint(w[o + 7]) << 32);
+        rng.inc = (uint64_t)__float_as_uint(w[o + 8]) | ((uint64_t)__float_as_uint(w[o + 9]) << 32);
+        point = __float_as_int(w[o + 10]);
+        wlen = __float_as_int(w[o + 11]);
+        cpSeed = __float_as_int(w[o + 12]);
+        const int f = __float_as_int(w[o + 13]);
+        onRefl = (f & 1) != 0; flip = (f & 2) != 0; pointFlip = (f & 4) != 0; firstStep = (f & 8) != 0;
+        g.yukawa = (f & 16) != 0;
+        // what start() leaves in the fields a record does not hold
+        walkTotal = 0.0f; success = false; splits = 0; lenSum = 0; nStack = 0; gradMode = false; cpValid = false;
+        queryPending = radiusPending = radiusReady = false; pendingCode = -1;
+        iters = wlen;   // every step() call before this one advanced wlen
+    }
+    ZG_D void waveStore(float4* rec) const {
+        float w[4 * kWaveVec];
+#pragma unroll
+        for (int i = 0; i < D; i++) { w[i] = pt[i]; w[D + i] = nrm[i]; w[2 * D + i] = prevDir[i]; }
+        constexpr int o = 3 * D;
+        w[o] = prevDist; w[o + 1] = thr; w[o + 2] = distAbs; w[o + 3] = fsr; w[o + 4] = totRefl; w[o + 5] = totSrc;
+        w[o + 6] = __uint_as_float((uint32_t)rng.state); w[o + 7] = __uint_as_float((uint32_t)(rng.state >> 32));
+        w[o + 8] = __uint_as_float((uint32_t)rng.inc); w[o + 9] = __uint_as_float((uint32_t)(rng.inc >> 32));
+        w[o + 10] = __int_as_float(point);
+        w[o + 11] = __int_as_float(wlen);
+        w[o + 12] = __int_as_float(cpSeed);
+        w[o + 13] = __int_as_float((onRefl ? 1 : 0) | (flip ? 2 : 0) | (pointFlip ? 4 : 0) | (firstStep ? 8 : 0) |
+                                   (g.yukawa ? 16 : 0));
+#pragma unroll
+        for (int k = o + 14; k < 4 * kWaveVec; k++) w[k] = 0.0f;
+#pragma unroll
+        for (int v = 0; v < kWaveVec; v++) rec[v] = make_float4(w[4 * v], w[4 * v + 1], w[4 * v + 2], w[4 * v + 3]);
+    }
+    static constexpr int kWavePointWord = 3 * D + 10;
+
+    // first kernel of a step; false when the walk ended (terminated or out of budget)
+    ZG_D bool waveRadius() {
+        if (P.stepBudget > 0 && ++iters > P.stepBudget) { err |= kErrBudget; return false; }
+        const zgpu_walk_settings& ws = SC().ws;
+        if (!firstStep) closestQuery();
+        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        if (firstStep && fsr > 0.0f) return true;   // the first sphere radius is this step's
+        float R;
+        flip = false;
+        if (ws.solve_double_sided && onRefl && prevDist > 0.0f && dot(prevDir, nrm) < 0.0f) {
+            nrm = -nrm;
+            flip = true;
+        }
+        if (ws.steps_before_using_maximal_spheres <= wlen) {
+            R = distAbs;
+        } else if (onRefl && pde.hasNonZeroRobinCoeff(pt)) {
+            R = ws.epsilon_shell_for_reflecting_boundary;
+        } else {
+            R = SC().hasRefl ? starRadius<D>(SC().reflecting, pt, ws.epsilon_shell_for_reflecting_boundary,
+                                             distAbs, ws.silhouette_precision, flip, S, err)
+                             : distAbs;
+            if (SC().hasRefl && ws.epsilon_shell_for_reflecting_boundary <= distAbs)
+                R = fmaxf(kRadiusShrink * R, ws.epsilon_shell_for_reflecting_boundary);
+        }
+        fsr = R;
+        return true;
+    }
+
+    // second kernel of a step, from the radius fsr that waveRadius left; false when the walk ended
+    ZG_D bool waveAdvance() {
+        const zgpu_walk_settings& ws = SC().ws;
+        const float R = fsr;
+        steps++;
+        g.update(pt, R);
+        V<D> dir = sampleSphere<D>(rng);
+        if (onRefl && dot(nrm, dir) > 0.0f) dir = -dir;
+        V<D> origin = onRefl ? offsetPoint<D>(pt, -nrm) : pt;
+        V<D> hitPt, hitN;
+        float hitDist;
+        bool hit = false;
+        if (SC().hasRefl) {
+            RayHit<D> h = intersectRay<D>(SC().reflecting, origin, dir, R, false, S, err);
+            if (h.slot >= 0) {
+                hit = true;
+                hitDist = h.t;
+                hitPt = origin + h.t * dir;
+                hitN = primNormal<D>(loadPrim<D>(SC().reflecting, h.slot));
+            }
+        }
+        if (!hit) {
+            hitPt = origin + R * dir;
+            hitDist = R;
+            hitN = vzero<D>();
+        }
+        if (SC().hasRefl && !ws.ignore_reflecting_boundary_contribution) {
+            float u[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) u[i] = rng.uniform();
+            V<D> bpt, bn;
+            float pdf;
+            if (sampleBoundary<D>(SC().reflecting, pt, R, u, bpt, bn, pdf)) {
+                V<D> toS = bpt - pt;
+                float dS = len(toS);
+                float alpha = onRefl ? 2.0f : 1.0f;
+                bool aligned = false;
+                if (ws.solve_double_sided) {
+                    toS = (1.0f / dS) * toS;
+                    if (flip) {
+                        aligned = true;
+                    } else if (dot(toS, bn) < -ws.silhouette_precision) {
+                        bool fs = true;
+                        if (alpha > 1.0f) fs = dot(toS, nrm) < -ws.silhouette_precision;
+                        if (fs) aligned = true;
+                    }
+                }
+                V<D> bnA = aligned ? -bn : bn;
+                if (pdf > 0.0f && dS < R) {
+                    V<D> p1 = onRefl ? offsetPoint<D>(pt, -nrm) : pt;
+                    V<D> p2 = offsetPoint<D>(bpt, -bnA);
+                    V<D> seg = p2 - p1;
+                    float sl = len(seg);
+                    bool occluded = false;
+                    if (sl > 0.0f) {
+                        RayHit<D> oh = intersectRay<D>(SC().reflecting, p1, (1.0f / sl) * seg, sl, true, S, err);
+                        occluded = oh.slot >= 0;
+                    }
+                    if (!occluded) {
+                        float r = fmaxf(kRClamp, dS);
+                        float G = g.evaluate(r);
+                        float h = pde.robin(bpt, bn, ws.solve_double_sided && aligned);
+                        totRefl += thr * alpha * G * h / pdf;
+                    }
+                }
+            }
+        }
+        if (!ws.ignore_source_contribution) {
+            float r = g.sampleRadius(rng);
+            if (r <= hitDist) totSrc += thr * g.norm() * pde.source(pt + r * dir);
+        }
+        prevDist = hitDist;
+        prevDir = dir;
+        pt = hitPt;
+        nrm = hitN;
+        onRefl = hit;
+        cpValid = false;
+        float stepThr;
+        if (onRefl && prevDist > kFltEps) {
+            float kappa = 0.0f;
+            V<D> n = nrm;
+            if (!SC().pde.are_robin_conditions_pure_neumann) {
+                bool f2 = false;
+                if (ws.solve_double_sided) { f2 = dot(prevDir, nrm) < 0.0f; if (f2) n = -n; }
+                kappa = pde.robinCoeff(pt, ws.solve_double_sided && f2);
+            }
+            float refl = g.reflectance(prevDist, prevDir, n, kappa);
+            float maxRefl = SC().pde.are_robin_coeffs_nonnegative ? 1.0f : 2.0f;
+            stepThr = fminf(fmaxf(refl, 0.0f), maxRefl);
+        } else {
+            stepThr = g.directionSampledPoissonKernel(pt);
+        }
+        thr *= stepThr;
+        if (!onRefl && outsideBox(SC(), pt.v, D)) return terminate(kEscaped);
+        if (weightWindow()) return terminate(kRussianRoulette);
+        wlen++;
+        if (wlen >= ws.max_walk_length) return terminate(kExceeded);
+        if (SC().pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        firstStep = false;   // the closest-point query that ends the step runs in the next waveRadius
+        return true;
+    }
 };
 
 constexpr int kWalkThreads = 128;

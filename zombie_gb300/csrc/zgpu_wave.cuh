@@ -1,0 +1,254 @@
+// zgpu_wave.cuh -- the sorted-wavefront schedule of the Walk on Stars walk loop.
+//
+// The persistent walk kernel gives every lane one walk from start to end: after a few steps
+// the 32 walks of a warp are spread over the domain, their traversals visit unrelated tree
+// nodes, and the warp runs each query as long as its slowest lane.  This schedule keeps a
+// pool of walk states as fixed-size records in device memory instead and runs the walk loop
+// as iterations of six launches:
+//   1. waveKeyKernel: each live record's Morton cell of its position (a 256 x 256 grid in 2D,
+//      32^3 in 3D over the domain box) and its rank within the cell (one atomicAdd on the
+//      cell's count);
+//   2. waveScanKernel (one block): exclusive sum of the cell counts, the pool's live count,
+//      and the range of new walk ids that fills the free slots;
+//   3. waveScatterKernel: copies each live record to its cell's range of the other buffer, so
+//      the pool is ordered by cell and the warps of the next two kernels run neighbouring
+//      walks, whose traversals share their nodes;
+//   4. waveRefillKernel: starts new walks (consecutive ids, so consecutive walks of a point)
+//      in the free slots after the sorted ones and marks the rest free;
+//   5.-6. wavePhaseKernel<0> and <1>: one walk step over the live slots, split at the star
+//      radius (Walker::waveRadius / waveAdvance).
+// A walk's random numbers and arithmetic are those of the persistent kernel; only the order
+// in which walks finish, and so the order of the FP64 sums per point, differs.
+// A step reads its record four times and writes it three times (key, scatter, two phases):
+// about 0.5 KB of HBM traffic per walk step in 2D, which buys coherent queries.
+#pragma once
+
+#include "zgpu_kernels.cuh"
+
+namespace zg {
+
+constexpr int kWaveScanThreads = 1024;
+
+namespace detail {
+
+ZG_D uint32_t spreadBits2(uint32_t v) {   // 8 bits -> every second of 16
+    v = (v | (v << 4)) & 0x0F0Fu;
+    v = (v | (v << 2)) & 0x3333u;
+    v = (v | (v << 1)) & 0x5555u;
+    return v;
+}
+ZG_D uint32_t spreadBits3(uint32_t v) {   // 5 bits -> every third of 15
+    v = (v | (v << 8)) & 0x100Fu;
+    v = (v | (v << 4)) & 0x10C3u;
+    v = (v | (v << 2)) & 0x1249u;
+    return v;
+}
+
+template <int D>
+ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
+    constexpr int bits = D == 2 ? 8 : 5;
+    constexpr float cells = (float)(1 << bits);
+    uint32_t c[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const float ext = sc.domainMax[i] - sc.domainMin[i];
+        float t = ext > 0.0f ? (x[i] - sc.domainMin[i]) * (cells / ext) : 0.0f;
+        t = fminf(fmaxf(t, 0.0f), cells - 1.0f);   // NaN -> 0
+        c[i] = (uint32_t)t;
+    }
+    if (D == 2) return spreadBits2(c[0]) | (spreadBits2(c[1]) << 1);
+    return spreadBits3(c[0]) | (spreadBits3(c[1]) << 1) | (spreadBits3(c[D - 1]) << 2);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
+    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
+    constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
+    const long long live = W.ctr[kWaveLive];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W.pool; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t k = kWaveCells;
+        if (i < live) {
+            const float4* r = W.src + i * vec;
+            const float4 a = r[0], b = r[pw / 4];
+            const float pwv[4] = {b.x, b.y, b.z, b.w};
+            if (__float_as_int(pwv[pw % 4]) >= 0) {
+                const float x[3] = {a.x, a.y, a.z};
+                k = waveCell<D>(P.sc, x);
+            }
+        }
+        W.key[i] = k;
+        W.rank[i] = k < kWaveCells ? atomicAdd(W.count + k, 1u) : 0u;
+    }
+}
+
+// one block: exclusive sum of the cell counts, then the refill range (a template only so that
+// each translation unit's instance stays its own)
+template <int D>
+__global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
+    constexpr int n = kWaveCells;
+    constexpr int per = n / kWaveScanThreads;
+    __shared__ uint32_t warpSum[kWaveScanThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    uint32_t local[per];
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < per; j++) { local[j] = W.count[t * per + j]; s += local[j]; }
+    uint32_t incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warpSum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = warpSum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += v;
+        }
+        warpSum[lane] = w;   // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = incl - s + (wid > 0 ? warpSum[wid - 1] : 0u);
+#pragma unroll
+    for (int j = 0; j < per; j++) {
+        W.offset[t * per + j] = run;
+        run += local[j];
+        W.count[t * per + j] = 0u;
+    }
+    if (t == kWaveScanThreads - 1) {
+        const long long sorted = (long long)run;   // every live record has a cell
+        W.offset[n] = run;
+        const long long total = __ldg(P.walkStart + P.nPoints);
+        const long long next = W.ctr[kWaveNext];
+        long long fresh = W.pool - sorted;
+        if (fresh > total - next) fresh = total - next;
+        if (fresh < 0) fresh = 0;
+        W.ctr[kWaveSorted] = sorted;
+        W.ctr[kWaveFirstNew] = next;
+        W.ctr[kWaveNext] = next + fresh;
+        W.ctr[kWaveLive] = sorted + fresh;
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
+    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
+    constexpr int vec = WalkerT::kWaveVec;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W.pool; i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t k = W.key[i];
+        if (k >= kWaveCells) continue;
+        const long long d = (long long)W.offset[k] + W.rank[i];
+        const float4* r = W.src + i * vec;
+        float4* o = W.dst + d * vec;
+#pragma unroll
+        for (int v = 0; v < vec; v++) o[v] = r[v];
+    }
+}
+
+// new walks in slots [sorted, live), free marks in [live, pool)
+template <int D, bool SCREENED>
+__global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
+    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
+    constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
+    int stackNode[kMaxStack];
+    float stackKey[kMaxStack];
+    TravStack S{stackNode, stackKey, 1, P.stackEntries};
+    WalkerT walker(P, S);
+    walker.splitSlots = nullptr;
+    const long long sorted = W.ctr[kWaveSorted], live = W.ctr[kWaveLive], first = W.ctr[kWaveFirstNew];
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long wbase = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; wbase < W.pool;
+         wbase += warps * 32) {
+        const long long slot = wbase + lane;
+        if (wbase + 32 <= sorted) continue;   // the whole warp's slots hold sorted walks
+        const long long lo = wbase > sorted ? wbase : sorted;
+        if (lo < live) {
+            // the point of the warp's first new walk, then each lane's by a short forward scan
+            const long long id0 = first + (lo - sorted);
+            const int p0 = warpFindPoint(P, id0, lane);
+            if (slot >= lo && slot < live) {
+                const long long id = first + (slot - sorted);
+                int p = p0;
+                while (__ldg(P.walkStart + p + 1) <= id) p++;
+                walker.start(id, p);
+                walker.waveStore(W.dst + slot * vec);
+            }
+        }
+        if (slot >= live && slot < W.pool && slot >= sorted)
+            reinterpret_cast<int*>(W.dst + slot * vec)[pw] = -1;
+    }
+}
+
+template <int D, bool SCREENED, int PHASE>
+__global__ void __launch_bounds__(kWalkThreads, ZG_WALK_MIN_BLOCKS) wavePhaseKernel(const __grid_constant__ SolveParams P,
+                                                                                      const WaveParams W) {
+    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
+    constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
+    int stackNode[kMaxStack];
+    float stackKey[kMaxStack];
+    TravStack S{stackNode, stackKey, 1, P.stackEntries};
+    WalkerT walker(P, S);
+    walker.splitSlots = nullptr;
+    const long long live = W.ctr[kWaveLive];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < live; i += (long long)gridDim.x * blockDim.x) {
+        float4* r = W.dst + i * vec;
+        if (reinterpret_cast<const int*>(r)[pw] < 0) continue;
+        walker.waveLoad(r);
+        const bool alive = PHASE == 0 ? walker.waveRadius() : walker.waveAdvance();
+        if (alive) walker.waveStore(r);
+        else reinterpret_cast<int*>(r)[pw] = -1;
+    }
+    unsigned long long v[4] = {walker.steps, walker.escaped, walker.exceeded, walker.rr};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    uint32_t e = walker.err;
+    for (int o = 16; o > 0; o >>= 1) e |= __shfl_xor_sync(kFull, e, o);
+    if ((threadIdx.x & 31) == 0) {
+        if (v[0]) atomicAdd(P.counters + kCtrSteps, v[0]);
+        if (v[1]) atomicAdd(P.counters + kCtrEscaped, v[1]);
+        if (v[2]) atomicAdd(P.counters + kCtrExceeded, v[2]);
+        if (v[3]) atomicAdd(P.counters + kCtrRR, v[3]);
+        if (e) atomicOr(P.errorWord, e);
+    }
+}
+
+}  // namespace detail
+
+// launchers of one wavefront iteration, instantiated with the Walk on Stars kernels
+template <int D>
+struct WaveLaunch {
+    static constexpr int kVec = detail::Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>::kWaveVec;
+    static const void* phase(bool screened, int k) {
+        if (screened) return k == 0 ? (const void*)detail::wavePhaseKernel<D, true, 0> : (const void*)detail::wavePhaseKernel<D, true, 1>;
+        return k == 0 ? (const void*)detail::wavePhaseKernel<D, false, 0> : (const void*)detail::wavePhaseKernel<D, false, 1>;
+    }
+    static int blocksPerSM(bool screened) {
+        int a = 0, b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, phase(screened, 0), detail::kWalkThreads, 0) != cudaSuccess) a = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, phase(screened, 1), detail::kWalkThreads, 0) != cudaSuccess) b = 1;
+        a = a < b ? a : b;
+        return a > 0 ? a : 1;
+    }
+    static cudaError_t iterate(const SolveParams& p, const WaveParams& w, int blocks, int numSMs, cudaStream_t s) {
+        const bool screened = p.sc.pde.absorption_coeff > 0.0f;
+        const int sortBlocks = numSMs * 8;
+        detail::waveKeyKernel<D><<<sortBlocks, 256, 0, s>>>(p, w);
+        detail::waveScanKernel<D><<<1, kWaveScanThreads, 0, s>>>(p, w);
+        detail::waveScatterKernel<D><<<sortBlocks, 256, 0, s>>>(w);
+        if (screened) detail::waveRefillKernel<D, true><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+        else detail::waveRefillKernel<D, false><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+        void* args[] = {const_cast<SolveParams*>(&p), const_cast<WaveParams*>(&w)};
+        for (int k = 0; k < 2; k++) {
+            cudaError_t e = cudaLaunchKernel(phase(screened, k), dim3(blocks), dim3(detail::kWalkThreads), args, 0, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace zg
