@@ -598,6 +598,7 @@ def run_gpu(args):
     kernel_ms = []
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
     with ClockSampler(local) as clk:
         walk_ms = 0.0
         for i in range(args.steps):
@@ -610,6 +611,7 @@ def run_gpu(args):
             walk_ms += ev0.elapsed_time(ev1)
             kernel_ms.append(rep.kernel_ms)
             total_steps += rep.total_steps
+            launches += rep.kernel_launches
         torch.cuda.synchronize()
     if dist:
         tdist.barrier()
@@ -678,7 +680,7 @@ def run_gpu(args):
             "rmse_vs_exact": g["rmse"], "mean_walk_length": g["mean_walk_length"],
             "e2e": ({"value": e2e_val, "unit": "walk-steps/s", "h2d_bytes_per_step": int(h2d),
                      "d2h_bytes_per_step": int(d2h)} if e2e_val is not None else None),
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_step": per_step_bytes, "kernel_ms": mean_kernel_ms,

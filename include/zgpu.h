@@ -344,13 +344,19 @@ int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* posi
 /*
  * WalkOnSpheres<T,DIM>::solve (point_estimation/walk_on_spheres.h:38-44, batch over points
  * :132-168) and WalkOnStars<T,DIM>::solve (point_estimation/walk_on_stars.h:40-46, :151-187).
- * Runs every walk of every point in one persistent wavefront kernel and merges the walk
- * estimates into `stats`.  options/report may be NULL.
+ * Runs every walk of every point, in one persistent kernel or (Walk on Stars,
+ * options->schedule) as a sorted wavefront of walk records, and merges the walk estimates
+ * into `stats`.  options/report may be NULL.
  */
 int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries,
                const zgpu_pde* pde, const zgpu_walk_settings* settings,
                const zgpu_sample_points* points, zgpu_sample_statistics* stats,
                const zgpu_solve_options* options, zgpu_solve_report* report);
+
+/* Kernel launches issued by the last solve on `ctx` (zgpu_solve, zgpu_solve_batched,
+ * zgpu_solve_cached): prepare, the walk-id scan, the walk kernel or 6 per wavefront
+ * iteration, the cache pass and finalize.  No counterpart in the reference. */
+int zgpu_last_solve_launches(zgpu_context* ctx, int64_t* launches);
 
 /*
  * Batched many-solve: `n_scenes` independent problems of one dimension (2D or 3D) in one

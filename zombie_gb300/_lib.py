@@ -54,6 +54,7 @@ def lib():
         L.zgpu_query_occluded.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32]
         L.zgpu_query_sample_boundary.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, i32]
         L.zgpu_solve.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
+        L.zgpu_last_solve_launches.argtypes = [vp, vp]
         L.zgpu_solve_batched.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp]
         L.zgpu_autotune.argtypes = [vp, i32, vp, vp, vp, vp, i32, i32, vp, C.POINTER(C.c_float)]
         L.zgpu_solve_static.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp]

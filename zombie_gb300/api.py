@@ -933,7 +933,8 @@ def _check_branch_weight(w):
 
 # ------------------------------------------------------------------------- solvers
 class SolveReport:
-    def __init__(self, r):
+    def __init__(self, r, kernel_launches=None):
+        self.kernel_launches = kernel_launches   # kernels the solve launched (zgpu_last_solve_launches)
         self.total_steps = r.total_steps
         self.total_walks = r.total_walks
         self.escaped_walks = r.escaped_walks
@@ -977,7 +978,9 @@ class _Solver:
             check(lib().zgpu_solve_cached(self.ctx.h, self.solver_id, C.byref(q), C.byref(p), C.byref(ws),
                                           C.byref(sp), C.byref(st), optp, cache.h, float(cache_min_distance),
                                           C.byref(rep)))
-        self.last_report = SolveReport(rep)
+        launches = C.c_int64()
+        check(lib().zgpu_last_solve_launches(self.ctx.h, C.byref(launches)))
+        self.last_report = SolveReport(rep, launches.value)
         return self.last_report
 
     def autotune(self, pde, walk_settings, arrays, sample_points=4096, sample_walks=16):

@@ -79,6 +79,7 @@ struct zgpu_context {
     // autotuner results by scene signature
     std::map<std::string, zgpu_solve_options> tuned;
     std::vector<Buf> gridBufs;   // device copies of host-memory PDE grids
+    long long lastLaunches = 0;  // kernel launches of the last solve (zgpu_last_solve_launches)
 };
 
 struct zgpu_boundary {
@@ -739,10 +740,13 @@ int wideTwin(zgpu_boundary* b, zgpu_boundary** out) {
 // The sorted-wavefront Walk on Stars loop (zgpu_wave.cuh): iterations of sort, refill and
 // the two step kernels over a pool of walk records until no walk is left.  The host reads the
 // live count every kWaveCheck iterations (the iterations between run on an empty pool).
-constexpr long long kWavePool = 1LL << 21;
+#ifndef ZG_WAVE_POOL_LOG2
+#define ZG_WAVE_POOL_LOG2 23
+#endif
+constexpr long long kWavePool = 1LL << ZG_WAVE_POOL_LOG2;
 constexpr int kWaveCheck = 8;
 
-int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s) {
+int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, long long* iterations) {
     using C = zgpu_context;
     SolveParams P = P0;
     P.splitStack = nullptr;   // no split scratch: a split reports kErrSplitOverflow
@@ -760,9 +764,9 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s) {
     ZG_TRY(scratch<uint32_t>(ctx, C::kWaveRank, (size_t)pool, &w.rank));
     ZG_TRY(scratch<uint32_t>(ctx, C::kWaveCount, (size_t)kWaveCells, &w.count));
     ZG_TRY(scratch<uint32_t>(ctx, C::kWaveOffset, (size_t)kWaveCells + 1, &w.offset));
-    ZG_TRY(scratch<long long>(ctx, C::kWaveCtr, 4, &w.ctr));
+    ZG_TRY(scratch<long long>(ctx, C::kWaveCtr, kWaveCtrs, &w.ctr));
     ZG_CUDA(cudaMemsetAsync(w.count, 0, kWaveCells * sizeof(uint32_t), s));
-    ZG_CUDA(cudaMemsetAsync(w.ctr, 0, 4 * sizeof(long long), s));
+    ZG_CUDA(cudaMemsetAsync(w.ctr, 0, kWaveCtrs * sizeof(long long), s));
     w.pool = pool;
     const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.sc.pde.absorption_coeff > 0.0f);
     // a slot holds one walk for at most max_walk_length + 1 iterations, so every walk has
@@ -771,6 +775,7 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s) {
     const double maxIter = rounds * ((double)P.sc.ws.max_walk_length + 1.0) + 2.0 * kWaveCheck;
     float4* src = a;
     float4* dst = b;
+    *iterations = 0;
     for (long long it = 0;;) {
         for (int k = 0; k < kWaveCheck; k++, it++) {
             w.src = src;
@@ -778,6 +783,7 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s) {
             ZG_CUDA(launchWaveIteration(P, w, D, blocks, ctx->numSMs, s));
             std::swap(src, dst);
         }
+        *iterations = it;
         long long live = 0;
         ZG_CUDA(cudaMemcpyAsync(&live, w.ctr + kWaveLive, sizeof(long long), cudaMemcpyDeviceToHost, s));
         ZG_CUDA(cudaStreamSynchronize(s));
@@ -944,6 +950,10 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     int blocks = ctx->numSMs * perSM;
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
 
+    // kernel launches of this solve: prepare, the walk-id scan (3 kernels, 1 without points),
+    // the walk kernel or the wavefront iterations (6 kernels each), the cache pass, finalize
+    long long waveIterations = 0;
+    ctx->lastLaunches = 0;
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
     if (opt && opt->use_graph && !cache) {
         // the four launches as one CUDA graph: re-captured when anything they read changed
@@ -987,7 +997,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (P.coop) P.stackEntries = 0;     // the prepare kernel above used the per-thread stacks
     if (n > 0) {
-        if (useWave) ZG_TRY(runWave(ctx, P, D, s));
+        if (useWave) ZG_TRY(runWave(ctx, P, D, s, &waveIterations));
         else ZG_CUDA(launchWalk(P, D, blocks, threads, s));
     }
     if (cache && n > 0)
@@ -997,6 +1007,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(launchFinalize(P, D, s));
     }
     ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
+    ctx->lastLaunches = n > 0 ? 5 + (useWave ? 6 * waveIterations : 1) + (cache ? 1 : 0) : 1;
     ZG_TRY(stageOut<double>(ctx, P.statMean, stats->solution_mean, (size_t)n, mem));
     ZG_TRY(stageOut<double>(ctx, P.statM2, stats->solution_m2, (size_t)n, mem));
     ZG_TRY(stageOut<int>(ctx, P.statN, stats->n_solution_estimates, (size_t)n, mem));
@@ -1039,6 +1050,12 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
 }  // namespace
 
 extern "C" {
+
+int zgpu_last_solve_launches(zgpu_context* ctx, int64_t* launches) {
+    if (!ctx || !launches) return fail(ZGPU_ERR_INVALID_ARG, "NULL required argument");
+    *launches = ctx->lastLaunches;
+    return ZGPU_OK;
+}
 
 int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q, const zgpu_pde* pde,
                const zgpu_walk_settings* ws, const zgpu_sample_points* pts, zgpu_sample_statistics* stats,

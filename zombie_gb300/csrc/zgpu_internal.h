@@ -101,12 +101,19 @@ struct WaveParams {
     uint32_t* rank;           // [pool] the record's place in its cell
     uint32_t* count;          // [kWaveCells] records per cell (zeroed by the scan)
     uint32_t* offset;         // [kWaveCells + 1] first slot of each cell in dst
-    long long* ctr;           // [0] next walk id, [1] sorted live records, [2] first new id, [3] live slots
+    long long* ctr;           // [0] next walk id, [1] sorted live records, [2] first new id, [3] live slots,
+                              // [4] live slots of the previous iteration
     long long pool;           // records per buffer
 };
 
-enum : int { kWaveNext = 0, kWaveSorted = 1, kWaveFirstNew = 2, kWaveLive = 3 };
-constexpr int kWaveCells = 1 << 16;   // cells of the sort (2D 256^2; 3D uses the first 32^3)
+enum : int { kWaveNext = 0, kWaveSorted = 1, kWaveFirstNew = 2, kWaveLive = 3, kWavePrevLive = 4, kWaveCtrs = 8 };
+// cells of the sort: a 2^kWaveBits2D square grid in 2D, 2^kWaveBits3D cubed in 3D
+#ifndef ZG_WAVE_BITS_2D
+#define ZG_WAVE_BITS_2D 8
+#endif
+constexpr int kWaveBits2D = ZG_WAVE_BITS_2D;
+constexpr int kWaveBits3D = 5;
+constexpr int kWaveCells = 1 << (2 * kWaveBits2D > 3 * kWaveBits3D ? 2 * kWaveBits2D : 3 * kWaveBits3D);
 
 constexpr int kSplitStack = 8;
 // Walk on Spheres in 3D answers closest-point queries with a whole warp from this many

@@ -5,8 +5,8 @@
 // nodes, and the warp runs each query as long as its slowest lane.  This schedule keeps a
 // pool of walk states as fixed-size records in device memory instead and runs the walk loop
 // as iterations of six launches:
-//   1. waveKeyKernel: each live record's Morton cell of its position (a 256 x 256 grid in 2D,
-//      32^3 in 3D over the domain box) and its rank within the cell (one atomicAdd on the
+//   1. waveKeyKernel: each live record's Morton cell of its position (a 2^kWaveBits2D square
+//      grid in 2D, 2^kWaveBits3D cubed in 3D, over the domain box) and its rank within the cell (one atomicAdd on the
 //      cell's count);
 //   2. waveScanKernel (one block): exclusive sum of the cell counts, the pool's live count,
 //      and the range of new walk ids that fills the free slots;
@@ -28,13 +28,18 @@
 namespace zg {
 
 constexpr int kWaveScanThreads = 1024;
+// resident blocks per SM the two step kernels are compiled for
+#ifndef ZG_WAVE_MIN_BLOCKS
+#define ZG_WAVE_MIN_BLOCKS 10
+#endif
 
 namespace detail {
 
-ZG_D uint32_t spreadBits2(uint32_t v) {   // 8 bits -> every second of 16
-    v = (v | (v << 4)) & 0x0F0Fu;
-    v = (v | (v << 2)) & 0x3333u;
-    v = (v | (v << 1)) & 0x5555u;
+ZG_D uint32_t spreadBits2(uint32_t v) {   // up to 16 bits -> every second bit
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
     return v;
 }
 ZG_D uint32_t spreadBits3(uint32_t v) {   // 5 bits -> every third of 15
@@ -46,7 +51,7 @@ ZG_D uint32_t spreadBits3(uint32_t v) {   // 5 bits -> every third of 15
 
 template <int D>
 ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
-    constexpr int bits = D == 2 ? 8 : 5;
+    constexpr int bits = D == 2 ? kWaveBits2D : kWaveBits3D;
     constexpr float cells = (float)(1 << bits);
     uint32_t c[D];
 #pragma unroll
@@ -60,24 +65,38 @@ ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
     return spreadBits3(c[0]) | (spreadBits3(c[1]) << 1) | (spreadBits3(c[D - 1]) << 2);
 }
 
+// cell and in-cell rank of the records [0, live) of src; lanes of a warp that share a cell
+// (most of them: the records are in cell order from the previous sort) take their ranks
+// from one atomicAdd
 template <int D>
 __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
     const long long live = W.ctr[kWaveLive];
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W.pool; i += (long long)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < live; base += stride) {
+        const long long i = base + lane;
         uint32_t k = kWaveCells;
         if (i < live) {
             const float4* r = W.src + i * vec;
-            const float4 a = r[0], b = r[pw / 4];
-            const float pwv[4] = {b.x, b.y, b.z, b.w};
+            const float4 q = r[pw / 4];
+            const float pwv[4] = {q.x, q.y, q.z, q.w};
             if (__float_as_int(pwv[pw % 4]) >= 0) {
+                const float4 a = r[0];
                 const float x[3] = {a.x, a.y, a.z};
                 k = waveCell<D>(P.sc, x);
             }
         }
-        W.key[i] = k;
-        W.rank[i] = k < kWaveCells ? atomicAdd(W.count + k, 1u) : 0u;
+        const unsigned peers = __match_any_sync(kFull, k);
+        const int leader = __ffs(peers) - 1;
+        uint32_t first = 0;
+        if (lane == leader && k < kWaveCells) first = atomicAdd(W.count + k, (uint32_t)__popc(peers));
+        first = __shfl_sync(kFull, first, leader);
+        if (i < live) {
+            W.key[i] = k;
+            W.rank[i] = first + __popc(peers & ((1u << lane) - 1u));
+        }
     }
 }
 
@@ -86,13 +105,14 @@ __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ Sol
 template <int D>
 __global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     constexpr int n = kWaveCells;
-    constexpr int per = n / kWaveScanThreads;
+    constexpr int per4 = n / kWaveScanThreads / 4;   // uint4 per thread
+    static_assert(per4 >= 1 && per4 * 4 * kWaveScanThreads == n, "cells per scan thread");
     __shared__ uint32_t warpSum[kWaveScanThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    uint32_t local[per];
+    const uint4* cnt4 = reinterpret_cast<const uint4*>(W.count) + (size_t)t * per4;
     uint32_t s = 0;
 #pragma unroll
-    for (int j = 0; j < per; j++) { local[j] = W.count[t * per + j]; s += local[j]; }
+    for (int j = 0; j < per4; j++) { const uint4 c = cnt4[j]; s += c.x + c.y + c.z + c.w; }
     uint32_t incl = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -112,11 +132,18 @@ __global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_
     }
     __syncthreads();
     uint32_t run = incl - s + (wid > 0 ? warpSum[wid - 1] : 0u);
+    uint4* off4 = reinterpret_cast<uint4*>(W.offset) + (size_t)t * per4;
+    uint4* zero4 = reinterpret_cast<uint4*>(W.count) + (size_t)t * per4;
 #pragma unroll
-    for (int j = 0; j < per; j++) {
-        W.offset[t * per + j] = run;
-        run += local[j];
-        W.count[t * per + j] = 0u;
+    for (int j = 0; j < per4; j++) {
+        const uint4 c = cnt4[j];
+        uint4 o;
+        o.x = run; run += c.x;
+        o.y = run; run += c.y;
+        o.z = run; run += c.z;
+        o.w = run; run += c.w;
+        off4[j] = o;
+        zero4[j] = make_uint4(0u, 0u, 0u, 0u);
     }
     if (t == kWaveScanThreads - 1) {
         const long long sorted = (long long)run;   // every live record has a cell
@@ -126,6 +153,7 @@ __global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_
         long long fresh = W.pool - sorted;
         if (fresh > total - next) fresh = total - next;
         if (fresh < 0) fresh = 0;
+        W.ctr[kWavePrevLive] = W.ctr[kWaveLive];
         W.ctr[kWaveSorted] = sorted;
         W.ctr[kWaveFirstNew] = next;
         W.ctr[kWaveNext] = next + fresh;
@@ -137,7 +165,8 @@ template <int D>
 __global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
     constexpr int vec = WalkerT::kWaveVec;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W.pool; i += (long long)gridDim.x * blockDim.x) {
+    const long long n = W.ctr[kWavePrevLive];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const uint32_t k = W.key[i];
         if (k >= kWaveCells) continue;
         const long long d = (long long)W.offset[k] + W.rank[i];
@@ -148,11 +177,12 @@ __global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
     }
 }
 
-// new walks in slots [sorted, live), free marks in [live, pool)
+// new walks in the slots [sorted, live) after the sorted records (slots from live on are
+// never read: every kernel stops at the live count)
 template <int D, bool SCREENED>
 __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
-    constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
+    constexpr int vec = WalkerT::kWaveVec;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
     TravStack S{stackNode, stackKey, 1, P.stackEntries};
@@ -161,30 +191,24 @@ __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_co
     const long long sorted = W.ctr[kWaveSorted], live = W.ctr[kWaveLive], first = W.ctr[kWaveFirstNew];
     const int lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long wbase = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; wbase < W.pool;
-         wbase += warps * 32) {
-        const long long slot = wbase + lane;
-        if (wbase + 32 <= sorted) continue;   // the whole warp's slots hold sorted walks
-        const long long lo = wbase > sorted ? wbase : sorted;
-        if (lo < live) {
-            // the point of the warp's first new walk, then each lane's by a short forward scan
-            const long long id0 = first + (lo - sorted);
-            const int p0 = warpFindPoint(P, id0, lane);
-            if (slot >= lo && slot < live) {
-                const long long id = first + (slot - sorted);
-                int p = p0;
-                while (__ldg(P.walkStart + p + 1) <= id) p++;
-                walker.start(id, p);
-                walker.waveStore(W.dst + slot * vec);
-            }
+    for (long long lo = sorted + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; lo < live;
+         lo += warps * 32) {
+        // the point of the warp's first new walk, then each lane's by a short forward scan
+        const long long id0 = first + (lo - sorted);
+        const int p0 = warpFindPoint(P, id0, lane);
+        const long long slot = lo + lane;
+        if (slot < live) {
+            const long long id = first + (slot - sorted);
+            int p = p0;
+            while (__ldg(P.walkStart + p + 1) <= id) p++;
+            walker.start(id, p);
+            walker.waveStore(W.dst + slot * vec);
         }
-        if (slot >= live && slot < W.pool && slot >= sorted)
-            reinterpret_cast<int*>(W.dst + slot * vec)[pw] = -1;
     }
 }
 
 template <int D, bool SCREENED, int PHASE>
-__global__ void __launch_bounds__(kWalkThreads, ZG_WALK_MIN_BLOCKS) wavePhaseKernel(const __grid_constant__ SolveParams P,
+__global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKernel(const __grid_constant__ SolveParams P,
                                                                                       const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
