@@ -203,12 +203,12 @@ typedef struct zgpu_solve_options {
     int32_t bvh_width;         /* 0 / 4: the boundaries' own trees; 8: an 8-wide tree of a 3D
                                   absorbing boundary built on the host (built once, on first use,
                                   from the boundary's copy of its mesh) */
-    int32_t schedule;          /* Walk on Stars walk loop: 0 auto, 1 the persistent kernel (one
-                                  lane per walk from start to end), 2 the sorted wavefront (walk
-                                  states in device memory, sorted by position every step; single
-                                  scene, solutions only, no cache, graph or warp-wide queries,
-                                  non-negative Robin coefficients, splitting threshold >= 2).
-                                  Auto picks the wavefront for 2D solves it can serve. */
+    int32_t schedule;          /* walk loop: 0 auto, 1 the persistent kernel (one lane per walk
+                                  from start to end), 2 the sorted wavefront (walk states in device
+                                  memory, sorted by position every step; single scene, solutions
+                                  only, no cache, graph or warp-wide queries, non-negative Robin
+                                  coefficients, splitting threshold >= 2).  Auto picks the wavefront
+                                  for the 2D Walk on Stars solves it can serve. */
 } zgpu_solve_options;
 
 /* counters returned by a solve */

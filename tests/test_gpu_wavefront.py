@@ -1,4 +1,4 @@
-"""The sorted-wavefront schedule of the Walk on Stars loop against the persistent walk kernel.
+"""The sorted-wavefront schedule of the walk loop against the persistent walk kernel.
 
 Both schedules run the same walks: each walk keeps its pcg32 stream and its arithmetic, and
 the wavefront only moves the closest-point query from the end of a step to the start of the
@@ -6,7 +6,8 @@ next.  On the same inputs they must therefore agree walk for walk: the same esti
 walk lengths and step / escape / length-limit / Russian-roulette counters, and per-point
 means equal up to the order of the FP64 sums (walks finish in another order).  The oracle
 parity of the wavefront itself is covered by the solver tests, whose 2D Walk on Stars cases
-run on it under the automatic schedule.
+run on it under the automatic schedule; Walk on Spheres on the wavefront is held to the
+persistent kernel here, whose oracle parity the solver tests cover.
 """
 import numpy as np
 import pytest
@@ -15,6 +16,13 @@ from zombie_gb300 import _abi as A
 from zombie_gb300 import problems as P
 
 pytestmark = pytest.mark.gpu
+
+
+def _wos_source_rr():
+    pr = P.laplace_wos_2d(n_segments=512, grid=16, spp=256)
+    pr.pde = P.make_pde(pr.solution, sigma=2.0, source=True)      # f = 2u: sampled source points
+    pr.settings = P.default_walk_settings(rr=0.9)
+    return pr
 
 
 def _double_sided():
@@ -30,8 +38,11 @@ CASES = {
                                                        ("dirichlet", "source")),
     "double_sided_2d": _double_sided,
     "robin_rr_3d": lambda: P.robin_wost_3d(level=4, n_points=400, spp=128),
-    # more walks (3.4M) than the pool holds (2^21): slots are refilled over many rounds
-    "mixed_2d_pool_rounds": lambda: P.mixed_wost_2d(n_segments=1024, grid=80, spp=1024),
+    "wos_laplace_2d": lambda: P.laplace_wos_2d(n_segments=1024, grid=32, spp=128),
+    "wos_source_rr_2d": _wos_source_rr,
+    "wos_screened_3d": lambda: P.screened_wos_3d(level=4, n_points=400, spp=128),
+    # more walks (9.9M) than the pool holds (2^23): slots are refilled over many rounds
+    "mixed_2d_pool_rounds": lambda: P.mixed_wost_2d(n_segments=1024, grid=136, spp=1024),
 }
 
 
@@ -105,12 +116,16 @@ def test_wavefront_refuses_what_it_cannot_serve(zgpu):
             gp.solve(gp.device_arrays(), options=opt)
         return e.value.status
 
-    # Walk on Spheres has no wavefront schedule
-    assert refused(GpuProblem(P.laplace_wos_2d(n_segments=256, grid=8, spp=8))) == A.ZGPU_ERR_UNSUPPORTED
     gp = GpuProblem(P.mixed_wost_2d(n_segments=512, grid=8, spp=8))
     assert refused(gp, use_graph=1) == A.ZGPU_ERR_UNSUPPORTED
     assert refused(gp, query_mode=A.ZGPU_QUERY_MODE_WARP) == A.ZGPU_ERR_UNSUPPORTED
     assert refused(gp, schedule=3) == A.ZGPU_ERR_INVALID_ARG
+    # gradient walks keep to the persistent kernel
+    opt = A.SolveOptions()
+    opt.schedule = A.ZGPU_SCHEDULE_WAVEFRONT
+    with pytest.raises(ZgpuError) as e:
+        gp.solve(gp.device_arrays(gradients=True), options=opt)
+    assert e.value.status == A.ZGPU_ERR_UNSUPPORTED
     # walk splitting needs split scratch the wavefront does not keep
     pr = P.mixed_wost_2d(n_segments=512, grid=8, spp=8)
     pr.settings = P.default_walk_settings(splitting=1.5)

@@ -737,8 +737,8 @@ int wideTwin(zgpu_boundary* b, zgpu_boundary** out) {
 
 // zgpu_solve, zgpu_solve_cached and zgpu_solve_batched.  nScenes > 1: points->scene_id
 // selects each point's row of q / pde / ws.
-// The sorted-wavefront Walk on Stars loop (zgpu_wave.cuh): iterations of sort, refill and
-// the two step kernels over a pool of walk records until no walk is left.  The host reads the
+// The sorted-wavefront walk loop (zgpu_wave.cuh): iterations of sort, refill and the step
+// kernels over a pool of walk records until no walk is left.  The host reads the
 // live count every kWaveCheck iterations (the iterations between run on an empty pool).
 #ifndef ZG_WAVE_POOL_LOG2
 #define ZG_WAVE_POOL_LOG2 23
@@ -768,7 +768,7 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, lon
     ZG_CUDA(cudaMemsetAsync(w.count, 0, kWaveCells * sizeof(uint32_t), s));
     ZG_CUDA(cudaMemsetAsync(w.ctr, 0, kWaveCtrs * sizeof(long long), s));
     w.pool = pool;
-    const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.sc.pde.absorption_coeff > 0.0f);
+    const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.solver, P.sc.pde.absorption_coeff > 0.0f);
     // a slot holds one walk for at most max_walk_length + 1 iterations, so every walk has
     // started after ceil(total / pool) such rounds and ended one round later
     const double rounds = (double)((total + pool - 1) / pool + 1);
@@ -929,20 +929,21 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     // interior points under the reflectance bounds, the case the warp-wide traversal serves
     if (solver == ZGPU_SOLVER_WALK_ON_STARS && P.sc.hasRefl && q->reflecting->kind == ZGPU_BOUNDARY_ROBIN && !batched)
         P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
-    // the Walk on Stars loop's schedule: the sorted wavefront serves single-scene solution
-    // solves without neural cache, graph replay, split scratch or warp-wide queries
+    // the walk loop's schedule: the sorted wavefront serves single-scene solution solves without
+    // neural cache, graph replay, split scratch or warp-wide queries
     const int schedule = opt ? opt->schedule : ZGPU_SCHEDULE_AUTO;
     if (schedule < ZGPU_SCHEDULE_AUTO || schedule > ZGPU_SCHEDULE_WAVEFRONT)
         return fail(ZGPU_ERR_INVALID_ARG, "schedule must be 0, 1 or 2");
-    const bool waveServes = solver == ZGPU_SOLVER_WALK_ON_STARS && !batched && !gradients && !cache &&
-                            !(opt && opt->use_graph) && queryMode != ZGPU_QUERY_MODE_WARP &&
-                            P.sc.pde.are_robin_coeffs_nonnegative && P.sc.ws.splitting_threshold >= 2.0f;
+    const bool waveServes = !batched && !gradients && !cache && !(opt && opt->use_graph) &&
+                            queryMode != ZGPU_QUERY_MODE_WARP && P.sc.pde.are_robin_coeffs_nonnegative &&
+                            P.sc.ws.splitting_threshold >= 2.0f;
     if (schedule == ZGPU_SCHEDULE_WAVEFRONT && !waveServes)
-        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves Walk on Stars solves of one scene, solutions "
-                                          "only, without cache, graph or warp-wide queries, with non-negative Robin "
-                                          "coefficients and splitting_threshold >= 2");
-    const bool useWave = waveServes && (schedule == ZGPU_SCHEDULE_WAVEFRONT || (schedule == ZGPU_SCHEDULE_AUTO && D == 2));
-    if (useWave) P.coopStar = 0;
+        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves solves of one scene, solutions only, without "
+                                          "cache, graph or warp-wide queries, with non-negative Robin coefficients "
+                                          "and splitting_threshold >= 2");
+    const bool waveAuto = D == 2 && solver == ZGPU_SOLVER_WALK_ON_STARS;
+    const bool useWave = waveServes && (schedule == ZGPU_SCHEDULE_WAVEFRONT || (schedule == ZGPU_SCHEDULE_AUTO && waveAuto));
+    if (useWave) P.coop = P.coopStar = 0;
     if (P.coop) P.stackEntries = 0;
     int perSM = opt && opt->blocks_per_sm > 0 ? opt->blocks_per_sm
                                               : walkKernelMaxBlocksPerSM(D, solver, threads, P);
@@ -951,7 +952,8 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
 
     // kernel launches of this solve: prepare, the walk-id scan (3 kernels, 1 without points),
-    // the walk kernel or the wavefront iterations (6 kernels each), the cache pass, finalize
+    // the walk kernel or the wavefront iterations (6 kernels each, 5 for Walk on Spheres), the
+    // cache pass, finalize
     long long waveIterations = 0;
     ctx->lastLaunches = 0;
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
@@ -1007,7 +1009,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(launchFinalize(P, D, s));
     }
     ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
-    ctx->lastLaunches = n > 0 ? 5 + (useWave ? 6 * waveIterations : 1) + (cache ? 1 : 0) : 1;
+    ctx->lastLaunches = n > 0 ? 5 + (useWave ? waveLaunchesPerIteration(solver) * waveIterations : 1) + (cache ? 1 : 0) : 1;
     ZG_TRY(stageOut<double>(ctx, P.statMean, stats->solution_mean, (size_t)n, mem));
     ZG_TRY(stageOut<double>(ctx, P.statM2, stats->solution_m2, (size_t)n, mem));
     ZG_TRY(stageOut<int>(ctx, P.statN, stats->n_solution_estimates, (size_t)n, mem));

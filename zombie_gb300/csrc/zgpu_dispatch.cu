@@ -9,8 +9,10 @@ extern template struct WalkLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>;
 extern template struct WalkLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>;
 extern template struct WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>;
 extern template struct WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>;
-extern template struct WaveLaunch<2>;
-extern template struct WaveLaunch<3>;
+extern template struct WaveLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>;
+extern template struct WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>;
+extern template struct WaveLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>;
+extern template struct WaveLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>;
 
 namespace detail {
 // ------------------------------------------------------------------------- scan
@@ -80,13 +82,21 @@ cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, c
     return wos ? WalkLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::walk(p, blocks, threads, s)
                : WalkLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::walk(p, blocks, threads, s);
 }
+#define ZG_WAVE_DISPATCH(dim, solver, CALL)                                                          \
+    ((dim) == 2 ? ((solver) == ZGPU_SOLVER_WALK_ON_SPHERES ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>::CALL \
+                                                          : WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::CALL)   \
+                : ((solver) == ZGPU_SOLVER_WALK_ON_SPHERES ? WaveLaunch<3, ZGPU_SOLVER_WALK_ON_SPHERES>::CALL \
+                                                          : WaveLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::CALL))
 cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s) {
-    return dim == 2 ? WaveLaunch<2>::iterate(p, w, blocks, numSMs, s) : WaveLaunch<3>::iterate(p, w, blocks, numSMs, s);
+    return ZG_WAVE_DISPATCH(dim, p.solver, iterate(p, w, blocks, numSMs, s));
 }
-int waveBlocksPerSM(int dim, bool screened) {
-    return dim == 2 ? WaveLaunch<2>::blocksPerSM(screened) : WaveLaunch<3>::blocksPerSM(screened);
+int waveBlocksPerSM(int dim, int solver, bool screened) { return ZG_WAVE_DISPATCH(dim, solver, blocksPerSM(screened)); }
+int waveRecordVec(int dim) { return dim == 2 ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::kVec : WaveLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::kVec; }
+int waveLaunchesPerIteration(int solver) {
+    return solver == ZGPU_SOLVER_WALK_ON_SPHERES ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>::kLaunches
+                                                 : WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::kLaunches;
 }
-int waveRecordVec(int dim) { return dim == 2 ? WaveLaunch<2>::kVec : WaveLaunch<3>::kVec; }
+#undef ZG_WAVE_DISPATCH
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p) {
     const bool wos = solver == ZGPU_SOLVER_WALK_ON_SPHERES;
     const size_t smem = walkSmemBytes(p, threads);

@@ -127,11 +127,12 @@ cudaError_t launchPrepare(const SolveParams& p, int dim, cudaStream_t s);
 cudaError_t launchScan(long long* data, int64_t n, long long* blockSums, cudaStream_t s);
 cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, cudaStream_t s);
 cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
-// one iteration of the sorted-wavefront Walk on Stars loop (zgpu_wave.cuh); blocks: of the
-// two step kernels (numSMs x waveBlocksPerSM)
+// one iteration of the sorted-wavefront walk loop (zgpu_wave.cuh); blocks: of the step
+// kernels (numSMs x waveBlocksPerSM)
 cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s);
-int waveBlocksPerSM(int dim, bool screened);
+int waveBlocksPerSM(int dim, int solver, bool screened);
 int waveRecordVec(int dim);
+int waveLaunchesPerIteration(int solver);
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p);
 // validates a PDE's field kinds and grids (hostGrids: grid values may be in host memory)
 int checkPdeFields(const zgpu_pde* pde, int D, bool hostGrids);

@@ -790,6 +790,39 @@ struct Walker {
         firstStep = false;   // the closest-point query that ends the step runs in the next waveRadius
         return true;
     }
+
+    // a Walk on Spheres step on the wavefront schedule: stepWoS's statements in its order, the
+    // closest-point query that ends the previous step first; false when the walk ended
+    ZG_D bool waveStepWoS() {
+        if (P.stepBudget > 0 && ++iters > P.stepBudget) { err |= kErrBudget; return false; }
+        const zgpu_walk_settings& ws = SC().ws;
+        if (!firstStep) closestQuery();
+        if (!(distAbs > ws.epsilon_shell_for_absorbing_boundary)) return terminate(kReached);
+        steps++;
+        g.update(pt, distAbs);
+        if (!ws.ignore_source_contribution) {
+            float src;
+            if (SC().pde.is_source_constant) {
+                src = g.norm() * pde.source(pt);
+            } else {
+                V<D> d = sampleSphere<D>(rng);
+                float r = g.sampleRadius(rng);
+                src = g.norm() * pde.source(pt + r * d);
+            }
+            totSrc += thr * src;
+        }
+        V<D> dir = sampleSphere<D>(rng);
+        pt = pt + distAbs * dir;
+        cpValid = false;
+        thr *= g.directionSampledPoissonKernel(pt);
+        if (outsideBox(SC(), pt.v, D)) return terminate(kEscaped);
+        if (weightWindow()) return terminate(kRussianRoulette);
+        wlen++;
+        if (wlen >= ws.max_walk_length) return terminate(kExceeded);
+        if (SC().pde.absorption_coeff > 0.0f && ws.steps_before_applying_tikhonov == wlen) g.yukawa = true;
+        firstStep = false;
+        return true;
+    }
 };
 
 constexpr int kWalkThreads = 128;

@@ -2,4 +2,4 @@
 #include "zgpu_wave.cuh"
 
 template struct zg::WalkLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>;
-template struct zg::WaveLaunch<2>;
+template struct zg::WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>;

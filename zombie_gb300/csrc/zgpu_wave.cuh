@@ -1,4 +1,4 @@
-// zgpu_wave.cuh -- the sorted-wavefront schedule of the Walk on Stars walk loop.
+// zgpu_wave.cuh -- the sorted-wavefront schedule of the walk loop (Walk on Stars and Walk on Spheres).
 //
 // The persistent walk kernel gives every lane one walk from start to end: after a few steps
 // the 32 walks of a warp are spread over the domain, their traversals visit unrelated tree
@@ -15,8 +15,9 @@
 //      walks, whose traversals share their nodes;
 //   4. waveRefillKernel: starts new walks (consecutive ids, so consecutive walks of a point)
 //      in the free slots after the sorted ones and marks the rest free;
-//   5.-6. wavePhaseKernel<0> and <1>: one walk step over the live slots, split at the star
-//      radius (Walker::waveRadius / waveAdvance).
+//   5.-6. wavePhaseKernel<0> and <1>: one Walk on Stars step over the live slots, split at
+//      the star radius (Walker::waveRadius / waveAdvance); Walk on Spheres runs its step as
+//      one kernel, wavePhaseKernel<2> (Walker::waveStepWoS).
 // A walk's random numbers and arithmetic are those of the persistent kernel; only the order
 // in which walks finish, and so the order of the FP64 sums per point, differs.
 // A step reads its record four times and writes it three times (key, scatter, two phases):
@@ -68,7 +69,7 @@ ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
 // cell and in-cell rank of the records [0, live) of src; lanes of a warp that share a cell
 // (most of them: the records are in cell order from the previous sort) take their ranks
 // from one atomicAdd
-template <int D>
+template <int D, int SOLVER>
 __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ Sol
 
 // one block: exclusive sum of the cell counts, then the refill range (a template only so that
 // each translation unit's instance stays its own)
-template <int D>
+template <int D, int SOLVER>
 __global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     constexpr int n = kWaveCells;
     constexpr int per4 = n / kWaveScanThreads / 4;   // uint4 per thread
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(kWaveScanThreads) waveScanKernel(const __grid_
     }
 }
 
-template <int D>
+template <int D, int SOLVER>
 __global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
     constexpr int vec = WalkerT::kWaveVec;
@@ -179,9 +180,9 @@ __global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
 
 // new walks in the slots [sorted, live) after the sorted records (slots from live on are
 // never read: every kernel stops at the live count)
-template <int D, bool SCREENED>
+template <int D, int SOLVER, bool SCREENED>
 __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
-    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
+    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
     constexpr int vec = WalkerT::kWaveVec;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
@@ -207,10 +208,11 @@ __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_co
     }
 }
 
-template <int D, bool SCREENED, int PHASE>
+// PHASE 0 / 1: the two kernels of a Walk on Stars step; 2: a Walk on Spheres step
+template <int D, int SOLVER, bool SCREENED, int PHASE>
 __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKernel(const __grid_constant__ SolveParams P,
                                                                                       const WaveParams W) {
-    using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, SCREENED, false, false>;
+    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
@@ -222,7 +224,10 @@ __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKer
         float4* r = W.dst + i * vec;
         if (reinterpret_cast<const int*>(r)[pw] < 0) continue;
         walker.waveLoad(r);
-        const bool alive = PHASE == 0 ? walker.waveRadius() : walker.waveAdvance();
+        bool alive;
+        if constexpr (PHASE == 0) alive = walker.waveRadius();
+        else if constexpr (PHASE == 1) alive = walker.waveAdvance();
+        else alive = walker.waveStepWoS();
         if (alive) walker.waveStore(r);
         else reinterpret_cast<int*>(r)[pw] = -1;
     }
@@ -243,31 +248,43 @@ __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKer
 
 }  // namespace detail
 
-// launchers of one wavefront iteration, instantiated with the Walk on Stars kernels
-template <int D>
+// launchers of one wavefront iteration, instantiated with each solver's walk kernels
+template <int D, int SOLVER>
 struct WaveLaunch {
-    static constexpr int kVec = detail::Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>::kWaveVec;
+    static constexpr bool kStars = SOLVER == ZGPU_SOLVER_WALK_ON_STARS;
+    static constexpr int kVec = detail::Walker<D, SOLVER, false, false, false>::kWaveVec;
+    static constexpr int kStepKernels = kStars ? 2 : 1;
+    static constexpr int kLaunches = 4 + kStepKernels;   // per iteration
     static const void* phase(bool screened, int k) {
-        if (screened) return k == 0 ? (const void*)detail::wavePhaseKernel<D, true, 0> : (const void*)detail::wavePhaseKernel<D, true, 1>;
-        return k == 0 ? (const void*)detail::wavePhaseKernel<D, false, 0> : (const void*)detail::wavePhaseKernel<D, false, 1>;
+        if constexpr (!kStars) {
+            return screened ? (const void*)detail::wavePhaseKernel<D, SOLVER, true, 2>
+                            : (const void*)detail::wavePhaseKernel<D, SOLVER, false, 2>;
+        } else {
+            if (screened) return k == 0 ? (const void*)detail::wavePhaseKernel<D, SOLVER, true, 0>
+                                        : (const void*)detail::wavePhaseKernel<D, SOLVER, true, 1>;
+            return k == 0 ? (const void*)detail::wavePhaseKernel<D, SOLVER, false, 0>
+                          : (const void*)detail::wavePhaseKernel<D, SOLVER, false, 1>;
+        }
     }
     static int blocksPerSM(bool screened) {
-        int a = 0, b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, phase(screened, 0), detail::kWalkThreads, 0) != cudaSuccess) a = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, phase(screened, 1), detail::kWalkThreads, 0) != cudaSuccess) b = 1;
-        a = a < b ? a : b;
-        return a > 0 ? a : 1;
+        int best = 1 << 30;
+        for (int k = 0; k < kStepKernels; k++) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, phase(screened, k), detail::kWalkThreads, 0) != cudaSuccess) b = 1;
+            best = b < best ? b : best;
+        }
+        return best > 0 ? best : 1;
     }
     static cudaError_t iterate(const SolveParams& p, const WaveParams& w, int blocks, int numSMs, cudaStream_t s) {
         const bool screened = p.sc.pde.absorption_coeff > 0.0f;
         const int sortBlocks = numSMs * 8;
-        detail::waveKeyKernel<D><<<sortBlocks, 256, 0, s>>>(p, w);
-        detail::waveScanKernel<D><<<1, kWaveScanThreads, 0, s>>>(p, w);
-        detail::waveScatterKernel<D><<<sortBlocks, 256, 0, s>>>(w);
-        if (screened) detail::waveRefillKernel<D, true><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
-        else detail::waveRefillKernel<D, false><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+        detail::waveKeyKernel<D, SOLVER><<<sortBlocks, 256, 0, s>>>(p, w);
+        detail::waveScanKernel<D, SOLVER><<<1, kWaveScanThreads, 0, s>>>(p, w);
+        detail::waveScatterKernel<D, SOLVER><<<sortBlocks, 256, 0, s>>>(w);
+        if (screened) detail::waveRefillKernel<D, SOLVER, true><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+        else detail::waveRefillKernel<D, SOLVER, false><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
         void* args[] = {const_cast<SolveParams*>(&p), const_cast<WaveParams*>(&w)};
-        for (int k = 0; k < 2; k++) {
+        for (int k = 0; k < kStepKernels; k++) {
             cudaError_t e = cudaLaunchKernel(phase(screened, k), dim3(blocks), dim3(detail::kWalkThreads), args, 0, s);
             if (e != cudaSuccess) return e;
         }
