@@ -1164,6 +1164,9 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
                 o.blocks_per_sm = perSMC[pi];
                 o.query_mode = qm;
                 o.bvh_width = wi == 0 ? 4 : 8;
+                // the knobs are the persistent kernel's; the sample is too small to judge the
+                // wavefront, whose iterations are launch-bound until the pool fills
+                o.schedule = ZGPU_SCHEDULE_PERSISTENT;
                 double rate = 0.0;
                 for (int rep = 0; rep < 2; rep++) {
                     std::fill(cnt.begin(), cnt.end(), 0);
@@ -1178,6 +1181,7 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
                 }
                 if (rate > bestRate) { bestRate = rate; best = o; }
             }
+    best.schedule = ZGPU_SCHEDULE_AUTO;   // solves keep the automatic schedule
     ctx->tuned[sig] = best;
     *out = best;
     if (best_rate) *best_rate = (float)(bestRate * 1e3);
