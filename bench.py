@@ -658,15 +658,16 @@ def run_gpu(args):
         mean_kernel_ms = float(np.mean(kernel_ms))
         steps_per_launch = total_steps / args.steps / (ws if dist else 1)
         achieved = per_step_bytes * steps_per_launch / (mean_kernel_ms / 1e3) / 1e9
-        # DRAM bytes of one launch and the issue-side counters, from the committed ncu summary
-        # of this workload's walk kernel (ncu cannot run inside the timed bench)
-        traffic, counters = None, None
+        # DRAM bytes of one solve's walk loop and the issue-side counters, from the committed ncu
+        # summary of this workload (ncu cannot run inside the timed bench)
+        traffic, counters, wave = None, None, rep.kernel_launches > 6
         tp = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
         if os.path.exists(tp):
             prof = json.load(open(tp))
-            traffic = prof.get("dram_bytes_per_launch")
-            counters = {k: prof[k] for k in ("threads_per_warp_instruction", "warp_execution_efficiency",
-                                              "issue_active_pct", "l1_hit_pct", "l2_hit_pct", "source") if k in prof}
+            if prof.get("schedule", "persistent") == ("wavefront" if wave else "persistent"):
+                traffic = prof.get("dram_bytes_per_solve", prof.get("dram_bytes_per_launch"))
+                counters = {k: prof[k] for k in ("threads_per_warp_instruction", "warp_execution_efficiency",
+                                                  "issue_active_pct", "l1_hit_pct", "l2_hit_pct", "source") if k in prof}
         cpu = cpu_baseline(pr, args.workload, args.cpu_points) if not args.skip_cpu else None
         line = {
             "metric": "walk-steps/s", "value": value, "unit": "walk-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -684,9 +685,13 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_step": per_step_bytes, "kernel_ms": mean_kernel_ms,
-                         "limiter": "instruction issue under divergence; the scene is L1/L2-resident, so "
-                                    "achieved is tree bytes consumed per second, not DRAM bandwidth",
-                         "traffic_source": "committed ncu capture of one launch of this workload (profiles/)",
+                         "kernel": ("the sorted-wavefront walk loop: sort, refill and step kernels over "
+                                    f"{rep.kernel_launches} launches per solve; time and bytes are per solve"
+                                    if wave else "the persistent walk kernel, one launch per solve"),
+                         "limiter": "instruction issue under divergence in the traversals; the scene is "
+                                    "L1/L2-resident, so achieved is tree bytes consumed per second, not DRAM "
+                                    "bandwidth",
+                         "traffic_source": "committed ncu capture of one solve of this workload (profiles/)",
                          "ncu": counters},
             "clocks": clk.summary(),
             "cpu_baseline": cpu,

@@ -354,8 +354,9 @@ int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* quer
                const zgpu_solve_options* options, zgpu_solve_report* report);
 
 /* Kernel launches issued by the last solve on `ctx` (zgpu_solve, zgpu_solve_batched,
- * zgpu_solve_cached): prepare, the walk-id scan, the walk kernel or 6 per wavefront
- * iteration, the cache pass and finalize.  No counterpart in the reference. */
+ * zgpu_solve_cached): prepare, the walk-id scan, the walk kernel or the wavefront's
+ * iterations (6 launches each, 5 for Walk on Spheres) and its drain, the cache pass and
+ * finalize.  No counterpart in the reference. */
 int zgpu_last_solve_launches(zgpu_context* ctx, int64_t* launches);
 
 /*

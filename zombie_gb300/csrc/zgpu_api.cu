@@ -745,8 +745,11 @@ int wideTwin(zgpu_boundary* b, zgpu_boundary** out) {
 #endif
 constexpr long long kWavePool = 1LL << ZG_WAVE_POOL_LOG2;
 constexpr int kWaveCheck = 8;
+#ifndef ZG_WAVE_DRAIN_FACTOR
+#define ZG_WAVE_DRAIN_FACTOR 1
+#endif
 
-int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, long long* iterations) {
+int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, long long* launches) {
     using C = zgpu_context;
     SolveParams P = P0;
     P.splitStack = nullptr;   // no split scratch: a split reports kErrSplitOverflow
@@ -773,21 +776,31 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, lon
     // started after ceil(total / pool) such rounds and ended one round later
     const double rounds = (double)((total + pool - 1) / pool + 1);
     const double maxIter = rounds * ((double)P.sc.ws.max_walk_length + 1.0) + 2.0 * kWaveCheck;
+    // the tail: once every walk has started and at most this many records are live (one per
+    // resident thread of the step kernels), the drain kernel runs them to their ends
+    const long long drainAt = (long long)blocks * 128 * ZG_WAVE_DRAIN_FACTOR;
     float4* src = a;
     float4* dst = b;
-    *iterations = 0;
+    *launches = 0;
     for (long long it = 0;;) {
         for (int k = 0; k < kWaveCheck; k++, it++) {
             w.src = src;
             w.dst = dst;
             ZG_CUDA(launchWaveIteration(P, w, D, blocks, ctx->numSMs, s));
+            *launches += waveLaunchesPerIteration(P.solver);
             std::swap(src, dst);
         }
-        *iterations = it;
-        long long live = 0;
-        ZG_CUDA(cudaMemcpyAsync(&live, w.ctr + kWaveLive, sizeof(long long), cudaMemcpyDeviceToHost, s));
+        long long c[kWaveCtrs];
+        ZG_CUDA(cudaMemcpyAsync(c, w.ctr, sizeof(c), cudaMemcpyDeviceToHost, s));
         ZG_CUDA(cudaStreamSynchronize(s));
+        const long long live = c[kWaveLive];
         if (live == 0) break;
+        if (c[kWaveNext] >= total && live <= drainAt) {
+            w.dst = src;   // the records the last iteration left
+            ZG_CUDA(launchWaveDrain(P, w, D, blocks, s));
+            *launches += 1;
+            break;
+        }
         if ((double)it > maxIter)
             return fail(ZGPU_ERR_DEVICE_STATE, "the wavefront schedule still had %lld live walks after %lld iterations",
                         live, it);
@@ -952,9 +965,9 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_TRY(scratch<float4>(ctx, C::kSplitScratch, (size_t)blocks * threads * 3 * kSplitStack, &P.splitStack));
 
     // kernel launches of this solve: prepare, the walk-id scan (3 kernels, 1 without points),
-    // the walk kernel or the wavefront iterations (6 kernels each, 5 for Walk on Spheres), the
-    // cache pass, finalize
-    long long waveIterations = 0;
+    // the walk kernel or the wavefront iterations (6 kernels each, 5 for Walk on Spheres) and
+    // its drain, the cache pass, finalize
+    long long waveLaunches = 0;
     ctx->lastLaunches = 0;
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
     if (opt && opt->use_graph && !cache) {
@@ -999,7 +1012,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (P.coop) P.stackEntries = 0;     // the prepare kernel above used the per-thread stacks
     if (n > 0) {
-        if (useWave) ZG_TRY(runWave(ctx, P, D, s, &waveIterations));
+        if (useWave) ZG_TRY(runWave(ctx, P, D, s, &waveLaunches));
         else ZG_CUDA(launchWalk(P, D, blocks, threads, s));
     }
     if (cache && n > 0)
@@ -1009,7 +1022,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(launchFinalize(P, D, s));
     }
     ZG_CUDA(cudaEventRecord(ctx->ev[3], s));
-    ctx->lastLaunches = n > 0 ? 5 + (useWave ? waveLaunchesPerIteration(solver) * waveIterations : 1) + (cache ? 1 : 0) : 1;
+    ctx->lastLaunches = n > 0 ? 5 + (useWave ? waveLaunches : 1) + (cache ? 1 : 0) : 1;
     ZG_TRY(stageOut<double>(ctx, P.statMean, stats->solution_mean, (size_t)n, mem));
     ZG_TRY(stageOut<double>(ctx, P.statM2, stats->solution_m2, (size_t)n, mem));
     ZG_TRY(stageOut<int>(ctx, P.statN, stats->n_solution_estimates, (size_t)n, mem));

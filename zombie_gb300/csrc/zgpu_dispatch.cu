@@ -90,6 +90,9 @@ cudaError_t launchWalk(const SolveParams& p, int dim, int blocks, int threads, c
 cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s) {
     return ZG_WAVE_DISPATCH(dim, p.solver, iterate(p, w, blocks, numSMs, s));
 }
+cudaError_t launchWaveDrain(const SolveParams& p, const WaveParams& w, int dim, int blocks, cudaStream_t s) {
+    return ZG_WAVE_DISPATCH(dim, p.solver, drain(p, w, blocks, s));
+}
 int waveBlocksPerSM(int dim, int solver, bool screened) { return ZG_WAVE_DISPATCH(dim, solver, blocksPerSM(screened)); }
 int waveRecordVec(int dim) { return dim == 2 ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::kVec : WaveLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::kVec; }
 int waveLaunchesPerIteration(int solver) {

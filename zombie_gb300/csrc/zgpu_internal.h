@@ -130,6 +130,8 @@ cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
 // one iteration of the sorted-wavefront walk loop (zgpu_wave.cuh); blocks: of the step
 // kernels (numSMs x waveBlocksPerSM)
 cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s);
+// the live records of w.dst to the end of their walks (the wavefront's tail)
+cudaError_t launchWaveDrain(const SolveParams& p, const WaveParams& w, int dim, int blocks, cudaStream_t s);
 int waveBlocksPerSM(int dim, int solver, bool screened);
 int waveRecordVec(int dim);
 int waveLaunchesPerIteration(int solver);

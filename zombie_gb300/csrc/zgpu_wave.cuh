@@ -18,6 +18,9 @@
 //   5.-6. wavePhaseKernel<0> and <1>: one Walk on Stars step over the live slots, split at
 //      the star radius (Walker::waveRadius / waveAdvance); Walk on Spheres runs its step as
 //      one kernel, wavePhaseKernel<2> (Walker::waveStepWoS).
+// Once every walk has started and no more live records are left than the step kernels have
+// resident threads, waveDrainKernel runs each remaining record to the end of its walk in a
+// loop: the walks finishing last would otherwise take hundreds of iterations of launches.
 // A walk's random numbers and arithmetic are those of the persistent kernel; only the order
 // in which walks finish, and so the order of the FP64 sums per point, differs.
 // A step reads its record four times and writes it three times (key, scatter, two phases):
@@ -246,6 +249,45 @@ __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKer
     }
 }
 
+// the tail: once every walk has started and the live records are few, each thread runs its
+// records to the end of their walks (no sort, no per-step launch); the same step members,
+// so the same walks
+template <int D, int SOLVER, bool SCREENED>
+__global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) waveDrainKernel(const __grid_constant__ SolveParams P,
+                                                                                      const WaveParams W) {
+    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
+    constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
+    int stackNode[kMaxStack];
+    float stackKey[kMaxStack];
+    TravStack S{stackNode, stackKey, 1, P.stackEntries};
+    WalkerT walker(P, S);
+    walker.splitSlots = nullptr;
+    const long long live = W.ctr[kWaveLive];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < live; i += (long long)gridDim.x * blockDim.x) {
+        const float4* r = W.dst + i * vec;
+        if (reinterpret_cast<const int*>(r)[pw] < 0) continue;
+        walker.waveLoad(r);
+        if constexpr (SOLVER == ZGPU_SOLVER_WALK_ON_STARS) {
+            while (walker.waveRadius() && walker.waveAdvance()) {}
+        } else {
+            while (walker.waveStepWoS()) {}
+        }
+    }
+    unsigned long long v[4] = {walker.steps, walker.escaped, walker.exceeded, walker.rr};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(kFull, v[k], o);
+    uint32_t e = walker.err;
+    for (int o = 16; o > 0; o >>= 1) e |= __shfl_xor_sync(kFull, e, o);
+    if ((threadIdx.x & 31) == 0) {
+        if (v[0]) atomicAdd(P.counters + kCtrSteps, v[0]);
+        if (v[1]) atomicAdd(P.counters + kCtrEscaped, v[1]);
+        if (v[2]) atomicAdd(P.counters + kCtrExceeded, v[2]);
+        if (v[3]) atomicAdd(P.counters + kCtrRR, v[3]);
+        if (e) atomicOr(P.errorWord, e);
+    }
+}
+
 }  // namespace detail
 
 // launchers of one wavefront iteration, instantiated with each solver's walk kernels
@@ -288,6 +330,13 @@ struct WaveLaunch {
             cudaError_t e = cudaLaunchKernel(phase(screened, k), dim3(blocks), dim3(detail::kWalkThreads), args, 0, s);
             if (e != cudaSuccess) return e;
         }
+        return cudaGetLastError();
+    }
+    // the records [0, live) of w.dst to the end of their walks
+    static cudaError_t drain(const SolveParams& p, const WaveParams& w, int blocks, cudaStream_t s) {
+        const bool screened = p.sc.pde.absorption_coeff > 0.0f;
+        if (screened) detail::waveDrainKernel<D, SOLVER, true><<<blocks, detail::kWalkThreads, 0, s>>>(p, w);
+        else detail::waveDrainKernel<D, SOLVER, false><<<blocks, detail::kWalkThreads, 0, s>>>(p, w);
         return cudaGetLastError();
     }
 };
