@@ -205,10 +205,10 @@ typedef struct zgpu_solve_options {
                                   from the boundary's copy of its mesh) */
     int32_t schedule;          /* walk loop: 0 auto, 1 the persistent kernel (one lane per walk
                                   from start to end), 2 the sorted wavefront (walk states in device
-                                  memory, sorted by position every step; single scene, solutions
-                                  only, no cache, graph or warp-wide queries, non-negative Robin
-                                  coefficients, splitting threshold >= 2).  Auto picks the wavefront
-                                  for the 2D Walk on Stars solves it can serve. */
+                                  memory, sorted by position every step; solutions only, no cache,
+                                  graph or warp-wide queries, non-negative Robin coefficients,
+                                  splitting threshold >= 2; batched solves too).  Auto picks the
+                                  wavefront for the 2D Walk on Stars solves it can serve. */
 } zgpu_solve_options;
 
 /* counters returned by a solve */

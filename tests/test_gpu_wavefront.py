@@ -75,6 +75,27 @@ def test_wavefront_runs_the_persistent_kernels_walks(zgpu, case):
     assert np.allclose(a["solution_m2"], b["solution_m2"], rtol=1e-8, atol=1e-10)
 
 
+def test_batched_wavefront_runs_the_persistent_kernels_walks(zgpu):
+    """A batched many-solve on the wavefront (records sorted by scene, then by cell in the
+    scene's box) runs the walks of the persistent batched kernel."""
+    from zombie_gb300.runner import GpuBatch
+    batch = GpuBatch(P.batched_scenes(n_scenes=5, seed=3, point_scale=0.004, segments=(256, 4096)))
+    out = {}
+    for sched in (A.ZGPU_SCHEDULE_PERSISTENT, A.ZGPU_SCHEDULE_WAVEFRONT):
+        opt = A.SolveOptions()
+        opt.schedule = sched
+        arrays = batch.device_arrays()
+        rep = batch.solve(arrays, options=opt)
+        assert rep.error_word == 0 and rep.total_steps > 0
+        out[sched] = (rep, {k: arrays[k].cpu().numpy() for k in ("solution_mean", "n_solution_estimates",
+                                                                  "total_walk_length")})
+    (ra, a), (rb, b) = out[A.ZGPU_SCHEDULE_PERSISTENT], out[A.ZGPU_SCHEDULE_WAVEFRONT]
+    assert (ra.total_steps, ra.escaped_walks, ra.exceeded_walks) == (rb.total_steps, rb.escaped_walks, rb.exceeded_walks)
+    assert np.array_equal(a["n_solution_estimates"], b["n_solution_estimates"])
+    assert np.array_equal(a["total_walk_length"], b["total_walk_length"])
+    assert np.allclose(a["solution_mean"], b["solution_mean"], rtol=1e-9, atol=1e-12)
+
+
 def test_automatic_schedule_picks_the_wavefront_in_2d(zgpu):
     """Auto (0) runs 2D Walk on Stars on the wavefront: its statistics are the wavefront's."""
     from zombie_gb300.runner import GpuProblem

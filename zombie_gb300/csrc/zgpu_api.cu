@@ -771,7 +771,19 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, lon
     ZG_CUDA(cudaMemsetAsync(w.count, 0, kWaveCells * sizeof(uint32_t), s));
     ZG_CUDA(cudaMemsetAsync(w.ctr, 0, kWaveCtrs * sizeof(long long), s));
     w.pool = pool;
-    const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.solver, P.sc.pde.absorption_coeff > 0.0f);
+    const bool batched = P.sceneId != nullptr;
+    const bool screened = batched ? P.batchScreened != 0 : P.sc.pde.absorption_coeff > 0.0f;
+    const int blocks = ctx->numSMs * waveBlocksPerSM(D, P.solver, screened, batched);
+    // the sort's cells: one Morton grid over the domain box; a batched solve puts the scene id
+    // above a coarser grid over each scene's own box, within the same 2^16 cells
+    w.axisBits = D == 2 ? kWaveBits2D : kWaveBits3D;
+    w.sceneMask = 0u;
+    if (batched) {
+        int sceneBits = 0;
+        while (sceneBits < 16 && (1LL << sceneBits) < (long long)P.nScenes) sceneBits++;
+        w.axisBits = std::min(w.axisBits, (16 - sceneBits) / D);
+        w.sceneMask = (uint32_t)((1u << sceneBits) - 1u);
+    }
     // a slot holds one walk for at most max_walk_length + 1 iterations, so every walk has
     // started after ceil(total / pool) such rounds and ended one round later
     const double rounds = (double)((total + pool - 1) / pool + 1);
@@ -942,18 +954,20 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     // interior points under the reflectance bounds, the case the warp-wide traversal serves
     if (solver == ZGPU_SOLVER_WALK_ON_STARS && P.sc.hasRefl && q->reflecting->kind == ZGPU_BOUNDARY_ROBIN && !batched)
         P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
-    // the walk loop's schedule: the sorted wavefront serves single-scene solution solves without
-    // neural cache, graph replay, split scratch or warp-wide queries
+    // the walk loop's schedule: the sorted wavefront serves solution solves (one scene or a
+    // batch) without neural cache, graph replay, split scratch or warp-wide queries
     const int schedule = opt ? opt->schedule : ZGPU_SCHEDULE_AUTO;
     if (schedule < ZGPU_SCHEDULE_AUTO || schedule > ZGPU_SCHEDULE_WAVEFRONT)
         return fail(ZGPU_ERR_INVALID_ARG, "schedule must be 0, 1 or 2");
-    const bool waveServes = !batched && !gradients && !cache && !(opt && opt->use_graph) &&
-                            queryMode != ZGPU_QUERY_MODE_WARP && P.sc.pde.are_robin_coeffs_nonnegative &&
-                            P.sc.ws.splitting_threshold >= 2.0f;
+    bool scenesServe = true;   // every scene: non-negative Robin coefficients, no splitting
+    for (int k = 0; k < nScenes; k++)
+        scenesServe = scenesServe && pde[k].are_robin_coeffs_nonnegative && ws[k].splitting_threshold >= 2.0f;
+    const bool waveServes = !gradients && !cache && !(opt && opt->use_graph) && queryMode != ZGPU_QUERY_MODE_WARP &&
+                            scenesServe;
     if (schedule == ZGPU_SCHEDULE_WAVEFRONT && !waveServes)
-        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves solves of one scene, solutions only, without "
-                                          "cache, graph or warp-wide queries, with non-negative Robin coefficients "
-                                          "and splitting_threshold >= 2");
+        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves solutions only, without cache, graph or "
+                                          "warp-wide queries, with non-negative Robin coefficients and "
+                                          "splitting_threshold >= 2");
     const bool waveAuto = D == 2 && solver == ZGPU_SOLVER_WALK_ON_STARS;
     const bool useWave = waveServes && (schedule == ZGPU_SCHEDULE_WAVEFRONT || (schedule == ZGPU_SCHEDULE_AUTO && waveAuto));
     if (useWave) P.coop = P.coopStar = 0;

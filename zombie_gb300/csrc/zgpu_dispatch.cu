@@ -93,7 +93,9 @@ cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int d
 cudaError_t launchWaveDrain(const SolveParams& p, const WaveParams& w, int dim, int blocks, cudaStream_t s) {
     return ZG_WAVE_DISPATCH(dim, p.solver, drain(p, w, blocks, s));
 }
-int waveBlocksPerSM(int dim, int solver, bool screened) { return ZG_WAVE_DISPATCH(dim, solver, blocksPerSM(screened)); }
+int waveBlocksPerSM(int dim, int solver, bool screened, bool batched) {
+    return ZG_WAVE_DISPATCH(dim, solver, blocksPerSM(screened, batched));
+}
 int waveRecordVec(int dim) { return dim == 2 ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_STARS>::kVec : WaveLaunch<3, ZGPU_SOLVER_WALK_ON_STARS>::kVec; }
 int waveLaunchesPerIteration(int solver) {
     return solver == ZGPU_SOLVER_WALK_ON_SPHERES ? WaveLaunch<2, ZGPU_SOLVER_WALK_ON_SPHERES>::kLaunches

@@ -104,6 +104,8 @@ struct WaveParams {
     long long* ctr;           // [0] next walk id, [1] sorted live records, [2] first new id, [3] live slots,
                               // [4] live slots of the previous iteration
     long long pool;           // records per buffer
+    int axisBits;             // sort grid: 2^axisBits cells per axis (per scene of a batched solve)
+    uint32_t sceneMask;       // batched solves: scene id bits above the cell (mask of the id)
 };
 
 enum : int { kWaveNext = 0, kWaveSorted = 1, kWaveFirstNew = 2, kWaveLive = 3, kWavePrevLive = 4, kWaveCtrs = 8 };
@@ -132,7 +134,7 @@ cudaError_t launchFinalize(const SolveParams& p, int dim, cudaStream_t s);
 cudaError_t launchWaveIteration(const SolveParams& p, const WaveParams& w, int dim, int blocks, int numSMs, cudaStream_t s);
 // the live records of w.dst to the end of their walks (the wavefront's tail)
 cudaError_t launchWaveDrain(const SolveParams& p, const WaveParams& w, int dim, int blocks, cudaStream_t s);
-int waveBlocksPerSM(int dim, int solver, bool screened);
+int waveBlocksPerSM(int dim, int solver, bool screened, bool batched);
 int waveRecordVec(int dim);
 int waveLaunchesPerIteration(int solver);
 int walkKernelMaxBlocksPerSM(int dim, int solver, int threads, const SolveParams& p);

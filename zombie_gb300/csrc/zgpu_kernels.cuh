@@ -631,6 +631,11 @@ struct Walker {
         rng.state = (uint64_t)__float_as_uint(w[o + 6]) | ((uint64_t)__float_as_uint(w[o + 7]) << 32);
         rng.inc = (uint64_t)__float_as_uint(w[o + 8]) | ((uint64_t)__float_as_uint(w[o + 9]) << 32);
         point = __float_as_int(w[o + 10]);
+        if constexpr (BATCHED) {   // the walk's row of the scene table, as start() sets it
+            sc = P.scenes + __ldg(P.sceneId + point);
+            pde.p = &sc->pde;
+            g.sqrtLambda = sqrtf(fmaxf(sc->pde.absorption_coeff, 0.0f));
+        }
         wlen = __float_as_int(w[o + 11]);
         cpSeed = __float_as_int(w[o + 12]);
         const int f = __float_as_int(w[o + 13]);

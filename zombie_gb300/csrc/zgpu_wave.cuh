@@ -53,10 +53,10 @@ ZG_D uint32_t spreadBits3(uint32_t v) {   // 5 bits -> every third of 15
     return v;
 }
 
+// Morton cell of x in a 2^bits-per-axis grid over the scene's domain box
 template <int D>
-ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
-    constexpr int bits = D == 2 ? kWaveBits2D : kWaveBits3D;
-    constexpr float cells = (float)(1 << bits);
+ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x, int bits) {
+    const float cells = (float)(1 << bits);
     uint32_t c[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
@@ -71,8 +71,8 @@ ZG_D uint32_t waveCell(const SceneDesc& sc, const float* x) {
 
 // cell and in-cell rank of the records [0, live) of src; lanes of a warp that share a cell
 // (most of them: the records are in cell order from the previous sort) take their ranks
-// from one atomicAdd
-template <int D, int SOLVER>
+// from one atomicAdd.  A batched solve's key is its scene above the cell in the scene's box.
+template <int D, int SOLVER, bool BATCHED>
 __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
     using WalkerT = Walker<D, ZGPU_SOLVER_WALK_ON_STARS, false, false, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
@@ -86,10 +86,16 @@ __global__ void __launch_bounds__(256) waveKeyKernel(const __grid_constant__ Sol
             const float4* r = W.src + i * vec;
             const float4 q = r[pw / 4];
             const float pwv[4] = {q.x, q.y, q.z, q.w};
-            if (__float_as_int(pwv[pw % 4]) >= 0) {
+            const int point = __float_as_int(pwv[pw % 4]);
+            if (point >= 0) {
                 const float4 a = r[0];
                 const float x[3] = {a.x, a.y, a.z};
-                k = waveCell<D>(P.sc, x);
+                if constexpr (BATCHED) {
+                    const int scene = __ldg(P.sceneId + point);
+                    k = ((uint32_t)scene & W.sceneMask) << (D * W.axisBits) | waveCell<D>(P.scenes[scene], x, W.axisBits);
+                } else {
+                    k = waveCell<D>(P.sc, x, W.axisBits);
+                }
             }
         }
         const unsigned peers = __match_any_sync(kFull, k);
@@ -183,9 +189,9 @@ __global__ void __launch_bounds__(256) waveScatterKernel(const WaveParams W) {
 
 // new walks in the slots [sorted, live) after the sorted records (slots from live on are
 // never read: every kernel stops at the live count)
-template <int D, int SOLVER, bool SCREENED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED>
 __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_constant__ SolveParams P, const WaveParams W) {
-    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
+    using WalkerT = Walker<D, SOLVER, SCREENED, BATCHED, false>;
     constexpr int vec = WalkerT::kWaveVec;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
@@ -212,10 +218,10 @@ __global__ void __launch_bounds__(kWalkThreads) waveRefillKernel(const __grid_co
 }
 
 // PHASE 0 / 1: the two kernels of a Walk on Stars step; 2: a Walk on Spheres step
-template <int D, int SOLVER, bool SCREENED, int PHASE>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED, int PHASE>
 __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKernel(const __grid_constant__ SolveParams P,
                                                                                       const WaveParams W) {
-    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
+    using WalkerT = Walker<D, SOLVER, SCREENED, BATCHED, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
@@ -252,10 +258,10 @@ __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) wavePhaseKer
 // the tail: once every walk has started and the live records are few, each thread runs its
 // records to the end of their walks (no sort, no per-step launch); the same step members,
 // so the same walks
-template <int D, int SOLVER, bool SCREENED>
+template <int D, int SOLVER, bool SCREENED, bool BATCHED>
 __global__ void __launch_bounds__(kWalkThreads, ZG_WAVE_MIN_BLOCKS) waveDrainKernel(const __grid_constant__ SolveParams P,
                                                                                       const WaveParams W) {
-    using WalkerT = Walker<D, SOLVER, SCREENED, false, false>;
+    using WalkerT = Walker<D, SOLVER, SCREENED, BATCHED, false>;
     constexpr int vec = WalkerT::kWaveVec, pw = WalkerT::kWavePointWord;
     int stackNode[kMaxStack];
     float stackKey[kMaxStack];
@@ -297,46 +303,57 @@ struct WaveLaunch {
     static constexpr int kVec = detail::Walker<D, SOLVER, false, false, false>::kWaveVec;
     static constexpr int kStepKernels = kStars ? 2 : 1;
     static constexpr int kLaunches = 4 + kStepKernels;   // per iteration
-    static const void* phase(bool screened, int k) {
-        if constexpr (!kStars) {
-            return screened ? (const void*)detail::wavePhaseKernel<D, SOLVER, true, 2>
-                            : (const void*)detail::wavePhaseKernel<D, SOLVER, false, 2>;
-        } else {
-            if (screened) return k == 0 ? (const void*)detail::wavePhaseKernel<D, SOLVER, true, 0>
-                                        : (const void*)detail::wavePhaseKernel<D, SOLVER, true, 1>;
-            return k == 0 ? (const void*)detail::wavePhaseKernel<D, SOLVER, false, 0>
-                          : (const void*)detail::wavePhaseKernel<D, SOLVER, false, 1>;
-        }
+    template <bool SCREENED, bool BATCHED>
+    static const void* phaseOf(int k) {
+        if constexpr (!kStars) return (const void*)detail::wavePhaseKernel<D, SOLVER, SCREENED, BATCHED, 2>;
+        else return k == 0 ? (const void*)detail::wavePhaseKernel<D, SOLVER, SCREENED, BATCHED, 0>
+                           : (const void*)detail::wavePhaseKernel<D, SOLVER, SCREENED, BATCHED, 1>;
     }
-    static int blocksPerSM(bool screened) {
+    static const void* phase(bool screened, bool batched, int k) {
+        if (batched) return screened ? phaseOf<true, true>(k) : phaseOf<false, true>(k);
+        return screened ? phaseOf<true, false>(k) : phaseOf<false, false>(k);
+    }
+    template <bool SCREENED, bool BATCHED>
+    static void refill(const SolveParams& p, const WaveParams& w, int numSMs, cudaStream_t s) {
+        detail::waveRefillKernel<D, SOLVER, SCREENED, BATCHED><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+    }
+    template <bool SCREENED, bool BATCHED>
+    static void drainWith(const SolveParams& p, const WaveParams& w, int blocks, cudaStream_t s) {
+        detail::waveDrainKernel<D, SOLVER, SCREENED, BATCHED><<<blocks, detail::kWalkThreads, 0, s>>>(p, w);
+    }
+    static bool screenedOf(const SolveParams& p) {
+        return p.sceneId ? p.batchScreened != 0 : p.sc.pde.absorption_coeff > 0.0f;
+    }
+    static int blocksPerSM(bool screened, bool batched) {
         int best = 1 << 30;
         for (int k = 0; k < kStepKernels; k++) {
             int b = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, phase(screened, k), detail::kWalkThreads, 0) != cudaSuccess) b = 1;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, phase(screened, batched, k), detail::kWalkThreads, 0) != cudaSuccess) b = 1;
             best = b < best ? b : best;
         }
         return best > 0 ? best : 1;
     }
     static cudaError_t iterate(const SolveParams& p, const WaveParams& w, int blocks, int numSMs, cudaStream_t s) {
-        const bool screened = p.sc.pde.absorption_coeff > 0.0f;
+        const bool screened = screenedOf(p), batched = p.sceneId != nullptr;
         const int sortBlocks = numSMs * 8;
-        detail::waveKeyKernel<D, SOLVER><<<sortBlocks, 256, 0, s>>>(p, w);
+        if (batched) detail::waveKeyKernel<D, SOLVER, true><<<sortBlocks, 256, 0, s>>>(p, w);
+        else detail::waveKeyKernel<D, SOLVER, false><<<sortBlocks, 256, 0, s>>>(p, w);
         detail::waveScanKernel<D, SOLVER><<<1, kWaveScanThreads, 0, s>>>(p, w);
         detail::waveScatterKernel<D, SOLVER><<<sortBlocks, 256, 0, s>>>(w);
-        if (screened) detail::waveRefillKernel<D, SOLVER, true><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
-        else detail::waveRefillKernel<D, SOLVER, false><<<numSMs * 8, detail::kWalkThreads, 0, s>>>(p, w);
+        if (batched) { if (screened) refill<true, true>(p, w, numSMs, s); else refill<false, true>(p, w, numSMs, s); }
+        else { if (screened) refill<true, false>(p, w, numSMs, s); else refill<false, false>(p, w, numSMs, s); }
         void* args[] = {const_cast<SolveParams*>(&p), const_cast<WaveParams*>(&w)};
         for (int k = 0; k < kStepKernels; k++) {
-            cudaError_t e = cudaLaunchKernel(phase(screened, k), dim3(blocks), dim3(detail::kWalkThreads), args, 0, s);
+            cudaError_t e = cudaLaunchKernel(phase(screened, batched, k), dim3(blocks), dim3(detail::kWalkThreads), args, 0, s);
             if (e != cudaSuccess) return e;
         }
         return cudaGetLastError();
     }
     // the records [0, live) of w.dst to the end of their walks
     static cudaError_t drain(const SolveParams& p, const WaveParams& w, int blocks, cudaStream_t s) {
-        const bool screened = p.sc.pde.absorption_coeff > 0.0f;
-        if (screened) detail::waveDrainKernel<D, SOLVER, true><<<blocks, detail::kWalkThreads, 0, s>>>(p, w);
-        else detail::waveDrainKernel<D, SOLVER, false><<<blocks, detail::kWalkThreads, 0, s>>>(p, w);
+        const bool screened = screenedOf(p), batched = p.sceneId != nullptr;
+        if (batched) { if (screened) drainWith<true, true>(p, w, blocks, s); else drainWith<false, true>(p, w, blocks, s); }
+        else { if (screened) drainWith<true, false>(p, w, blocks, s); else drainWith<false, false>(p, w, blocks, s); }
         return cudaGetLastError();
     }
 };

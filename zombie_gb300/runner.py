@@ -129,7 +129,9 @@ class GpuBatch:
         check(lib().zgpu_solve_batched(self.ctx.h, self.solver_id, len(self.problems), self.q, self.pde, self.ws,
                                        C.byref(sp), C.byref(st), C.byref(opt) if opt is not None else None,
                                        C.byref(rep)))
-        return SolveReport(rep)
+        launches = C.c_int64()
+        check(lib().zgpu_last_solve_launches(self.ctx.h, C.byref(launches)))
+        return SolveReport(rep, launches.value)
 
     def exact(self):
         return np.concatenate([g.problem.exact() for g in self.problems])
