@@ -6,15 +6,16 @@
 // pool of walk states as fixed-size records in device memory instead and runs the walk loop
 // as iterations of six launches:
 //   1. waveKeyKernel: each live record's Morton cell of its position (a 2^kWaveBits2D square
-//      grid in 2D, 2^kWaveBits3D cubed in 3D, over the domain box) and its rank within the cell (one atomicAdd on the
-//      cell's count);
+//      grid in 2D, 2^kWaveBits3D cubed in 3D, over the domain box; a batched solve puts the
+//      scene id above a coarser grid over the scene's own box) and its rank within the cell
+//      (one atomicAdd on the cell's count per group of warp lanes sharing the cell);
 //   2. waveScanKernel (one block): exclusive sum of the cell counts, the pool's live count,
 //      and the range of new walk ids that fills the free slots;
 //   3. waveScatterKernel: copies each live record to its cell's range of the other buffer, so
 //      the pool is ordered by cell and the warps of the next two kernels run neighbouring
 //      walks, whose traversals share their nodes;
 //   4. waveRefillKernel: starts new walks (consecutive ids, so consecutive walks of a point)
-//      in the free slots after the sorted ones and marks the rest free;
+//      in the slots after the sorted records, up to the new live count;
 //   5.-6. wavePhaseKernel<0> and <1>: one Walk on Stars step over the live slots, split at
 //      the star radius (Walker::waveRadius / waveAdvance); Walk on Spheres runs its step as
 //      one kernel, wavePhaseKernel<2> (Walker::waveStepWoS).
@@ -32,7 +33,8 @@
 namespace zg {
 
 constexpr int kWaveScanThreads = 1024;
-// resident blocks per SM the two step kernels are compiled for
+// resident blocks per SM the step kernels are compiled for (48 registers); measured on the
+// default 2D Walk on Stars workload: 10 ahead of 8 (-1.4%) and 6 (-3%)
 #ifndef ZG_WAVE_MIN_BLOCKS
 #define ZG_WAVE_MIN_BLOCKS 10
 #endif
