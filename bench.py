@@ -931,7 +931,7 @@ def main():
     ap.add_argument("--bvh-width", type=int, default=0, help="solve option bvh_width (8: 8-wide 3D absorbing tree)")
     ap.add_argument("--query-mode", type=int, default=0, help="solve option query_mode (1 lane, 2 warp per query)")
     ap.add_argument("--schedule", type=int, default=0,
-                    help="solve option schedule of the Walk on Stars loop (0 auto, 1 persistent, 2 wavefront)")
+                    help="solve option schedule of the walk loop (0 auto, 1 persistent, 2 wavefront)")
     ap.add_argument("--autotune", action="store_true", help="run zgpu_autotune on the workload before timing")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) solves of extra lines")
     ap.add_argument("--cpu-points", type=int, default=0,
