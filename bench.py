@@ -77,6 +77,20 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def reduce_over_ranks(seconds, units, dist, device):
+    """Whole-job figures of a weak-scaling run: the slowest rank's time and the units all ranks
+    processed (without a process group: the rank's own)."""
+    if not dist:
+        return seconds, units
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    tdist.all_reduce(u, op=tdist.ReduceOp.SUM)
+    return float(t[0]), float(u[0])
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -621,11 +635,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
     if dist:
         tdist.barrier()
-    t = torch.tensor([walk_ms, float(total_steps)], dtype=torch.float64, device="cuda")
-    if dist:
-        tmax = t.clone(); tdist.all_reduce(tmax[0:1], op=tdist.ReduceOp.MAX)
-        tdist.all_reduce(t[1:2], op=tdist.ReduceOp.SUM)
-        walk_ms, total_steps = float(tmax[0]), float(t[1])
+    walk_ms, total_steps = reduce_over_ranks(walk_ms, total_steps, dist, "cuda")
     g = summarize(dev, pr.exact())
     value = total_steps / (walk_ms / 1e3)
     ms_per_step = walk_ms / args.steps
@@ -652,10 +662,8 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     e2e_val = e2e_steps / e2e_s if e2e_steps else None
     if dist:
-        tt = torch.tensor([e2e_s, float(e2e_steps)], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(tt[0:1], op=tdist.ReduceOp.MAX)
-        tdist.all_reduce(tt[1:2], op=tdist.ReduceOp.SUM)
-        e2e_val = float(tt[1]) / float(tt[0])
+        e2e_all_s, e2e_all_steps = reduce_over_ranks(e2e_s, e2e_steps, True, "cuda")
+        e2e_val = e2e_all_steps / e2e_all_s
 
     line = None
     if rank == 0:
