@@ -193,7 +193,8 @@ typedef struct zgpu_sample_statistics {
 typedef struct zgpu_solve_options {
     int32_t block_size;        /* 0 -> autotuned / default */
     int32_t blocks_per_sm;     /* 0 -> occupancy-derived */
-    int32_t use_graph;         /* capture prepare+walk+finalize in a CUDA graph and replay */
+    int32_t use_graph;         /* capture prepare+walk+finalize in a CUDA graph and replay (the
+                                  wavefront schedule: chunks of its iterations) */
     int32_t query_mode;        /* closest-point queries of Walk on Spheres and Robin star radii of
                                   Walk on Stars: 0 auto, 1 one lane per query, 2 the whole warp
                                   per query (large scenes) */
@@ -205,10 +206,11 @@ typedef struct zgpu_solve_options {
                                   from the boundary's copy of its mesh) */
     int32_t schedule;          /* walk loop: 0 auto, 1 the persistent kernel (one lane per walk
                                   from start to end), 2 the sorted wavefront (walk states in device
-                                  memory, sorted by position every step; solutions only, no cache,
-                                  graph or warp-wide queries, non-negative Robin coefficients,
-                                  splitting threshold >= 2; batched solves too).  Auto picks the
-                                  wavefront for the 2D Walk on Stars solves it can serve. */
+                                  memory, sorted by position every step; solutions only, no cache
+                                  or warp-wide queries, non-negative Robin coefficients, splitting
+                                  threshold >= 2; batched solves too; with use_graph its iterations
+                                  replay from a captured graph).  Auto picks the wavefront for the
+                                  2D Walk on Stars solves it can serve. */
 } zgpu_solve_options;
 
 /* counters returned by a solve */

@@ -106,6 +106,19 @@ def test_automatic_schedule_picks_the_wavefront_in_2d(zgpu):
     assert np.array_equal(a["total_walk_length"], b["total_walk_length"])
 
 
+def test_wavefront_replayed_from_its_graph_runs_the_same_walks(zgpu):
+    """use_graph on the wavefront: chunks of iterations replayed from a captured graph (the
+    capture reused by the second solve) run the walks of the launched iterations."""
+    from zombie_gb300.runner import GpuProblem
+    gp = GpuProblem(P.mixed_wost_2d(n_segments=1024, grid=40, spp=256))
+    ref, rr = _solve(gp, A.ZGPU_SCHEDULE_WAVEFRONT)
+    for _ in range(2):
+        got, rg = _solve(gp, A.ZGPU_SCHEDULE_WAVEFRONT, use_graph=1)
+        assert rg.total_steps == rr.total_steps and rg.kernel_launches == rr.kernel_launches
+        assert np.array_equal(ref["total_walk_length"], got["total_walk_length"])
+        assert np.allclose(ref["solution_mean"], got["solution_mean"], rtol=1e-9, atol=1e-12)
+
+
 def test_wavefront_step_budget_drops_the_same_walks(zgpu):
     from zombie_gb300._lib import ZgpuError
     from zombie_gb300.runner import GpuProblem
@@ -138,7 +151,6 @@ def test_wavefront_refuses_what_it_cannot_serve(zgpu):
         return e.value.status
 
     gp = GpuProblem(P.mixed_wost_2d(n_segments=512, grid=8, spp=8))
-    assert refused(gp, use_graph=1) == A.ZGPU_ERR_UNSUPPORTED
     assert refused(gp, query_mode=A.ZGPU_QUERY_MODE_WARP) == A.ZGPU_ERR_UNSUPPORTED
     assert refused(gp, schedule=3) == A.ZGPU_ERR_INVALID_ARG
     # gradient walks keep to the persistent kernel

@@ -76,6 +76,10 @@ struct zgpu_context {
     // parameters (pointers, sizes, settings) are those it was captured with
     cudaGraphExec_t graphExec = nullptr;
     std::vector<unsigned char> graphKey;
+    // use_graph on the wavefront: one captured chunk of kWaveCheck iterations, replayed
+    // between the host's live-count checks while its parameters are those it was captured with
+    cudaGraphExec_t waveGraphExec = nullptr;
+    std::vector<unsigned char> waveGraphKey;
     // autotuner results by scene signature
     std::map<std::string, zgpu_solve_options> tuned;
     std::vector<Buf> gridBufs;   // device copies of host-memory PDE grids
@@ -234,6 +238,7 @@ int zgpu_context_destroy(zgpu_context* c) {
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
     if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
+    if (c->waveGraphExec) cudaGraphExecDestroy(c->waveGraphExec);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return ZGPU_OK;
@@ -749,7 +754,7 @@ constexpr int kWaveCheck = 8;
 #define ZG_WAVE_DRAIN_FACTOR 1
 #endif
 
-int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, long long* launches) {
+int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, bool useGraph, long long* launches) {
     using C = zgpu_context;
     SolveParams P = P0;
     P.splitStack = nullptr;   // no split scratch: a split reports kErrSplitOverflow
@@ -791,24 +796,56 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, lon
     // the tail: once every walk has started and at most this many records are live (one per
     // resident thread of the step kernels), the drain kernel runs them to their ends
     const long long drainAt = (long long)blocks * 128 * ZG_WAVE_DRAIN_FACTOR;
-    float4* src = a;
-    float4* dst = b;
+    // a chunk of kWaveCheck iterations (an even number: the buffers are where they started
+    // after it), launched one by one or replayed from its captured graph
+    auto chunk = [&]() -> cudaError_t {
+        float4* cs = a;
+        float4* cd = b;
+        for (int k = 0; k < kWaveCheck; k++) {
+            w.src = cs;
+            w.dst = cd;
+            cudaError_t e = launchWaveIteration(P, w, D, blocks, ctx->numSMs, s);
+            if (e != cudaSuccess) return e;
+            std::swap(cs, cd);
+        }
+        return cudaSuccess;
+    };
+    if (useGraph) {
+        std::vector<unsigned char> key(sizeof(SolveParams) + sizeof(WaveParams) + 2 * sizeof(int));
+        WaveParams wk = w;
+        wk.src = a;
+        wk.dst = b;
+        const int dims[2] = {D, blocks};
+        std::memcpy(key.data(), &P, sizeof(P));
+        std::memcpy(key.data() + sizeof(P), &wk, sizeof(wk));
+        std::memcpy(key.data() + sizeof(P) + sizeof(wk), dims, sizeof(dims));
+        if (!ctx->waveGraphExec || ctx->waveGraphKey != key) {
+            if (ctx->waveGraphExec) { cudaGraphExecDestroy(ctx->waveGraphExec); ctx->waveGraphExec = nullptr; }
+            cudaGraph_t g = nullptr;
+            ZG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            cudaError_t e = chunk();
+            cudaError_t e2 = cudaStreamEndCapture(s, &g);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->waveGraphExec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            ZG_CUDA(e);
+            ctx->waveGraphKey = key;
+        }
+    }
+    static_assert(kWaveCheck % 2 == 0, "a chunk leaves the records in the buffer it started from");
     *launches = 0;
     for (long long it = 0;;) {
-        for (int k = 0; k < kWaveCheck; k++, it++) {
-            w.src = src;
-            w.dst = dst;
-            ZG_CUDA(launchWaveIteration(P, w, D, blocks, ctx->numSMs, s));
-            *launches += waveLaunchesPerIteration(P.solver);
-            std::swap(src, dst);
-        }
+        if (useGraph) ZG_CUDA(cudaGraphLaunch(ctx->waveGraphExec, s));
+        else ZG_CUDA(chunk());
+        it += kWaveCheck;
+        *launches += (long long)kWaveCheck * waveLaunchesPerIteration(P.solver);
         long long c[kWaveCtrs];
         ZG_CUDA(cudaMemcpyAsync(c, w.ctr, sizeof(c), cudaMemcpyDeviceToHost, s));
         ZG_CUDA(cudaStreamSynchronize(s));
         const long long live = c[kWaveLive];
         if (live == 0) break;
         if (c[kWaveNext] >= total && live <= drainAt) {
-            w.dst = src;   // the records the last iteration left
+            w.dst = a;   // the records the last iteration left (a chunk ends where it began)
             ZG_CUDA(launchWaveDrain(P, w, D, blocks, s));
             *launches += 1;
             break;
@@ -955,19 +992,18 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     if (solver == ZGPU_SOLVER_WALK_ON_STARS && P.sc.hasRefl && q->reflecting->kind == ZGPU_BOUNDARY_ROBIN && !batched)
         P.coopStar = queryMode == 2 || (queryMode == 0 && D == 3 && q->reflecting->nPrims >= kCoopStarMinPrims);
     // the walk loop's schedule: the sorted wavefront serves solution solves (one scene or a
-    // batch) without neural cache, graph replay, split scratch or warp-wide queries
+    // batch) without neural cache, split scratch or warp-wide queries; with use_graph it
+    // replays its iterations from a captured graph
     const int schedule = opt ? opt->schedule : ZGPU_SCHEDULE_AUTO;
     if (schedule < ZGPU_SCHEDULE_AUTO || schedule > ZGPU_SCHEDULE_WAVEFRONT)
         return fail(ZGPU_ERR_INVALID_ARG, "schedule must be 0, 1 or 2");
     bool scenesServe = true;   // every scene: non-negative Robin coefficients, no splitting
     for (int k = 0; k < nScenes; k++)
         scenesServe = scenesServe && pde[k].are_robin_coeffs_nonnegative && ws[k].splitting_threshold >= 2.0f;
-    const bool waveServes = !gradients && !cache && !(opt && opt->use_graph) && queryMode != ZGPU_QUERY_MODE_WARP &&
-                            scenesServe;
+    const bool waveServes = !gradients && !cache && queryMode != ZGPU_QUERY_MODE_WARP && scenesServe;
     if (schedule == ZGPU_SCHEDULE_WAVEFRONT && !waveServes)
-        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves solutions only, without cache, graph or "
-                                          "warp-wide queries, with non-negative Robin coefficients and "
-                                          "splitting_threshold >= 2");
+        return fail(ZGPU_ERR_UNSUPPORTED, "the wavefront schedule serves solutions only, without cache or warp-wide "
+                                          "queries, with non-negative Robin coefficients and splitting_threshold >= 2");
     const bool waveAuto = D == 2 && solver == ZGPU_SOLVER_WALK_ON_STARS;
     const bool useWave = waveServes && (schedule == ZGPU_SCHEDULE_WAVEFRONT || (schedule == ZGPU_SCHEDULE_AUTO && waveAuto));
     if (useWave) P.coop = P.coopStar = 0;
@@ -984,7 +1020,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     long long waveLaunches = 0;
     ctx->lastLaunches = 0;
     ZG_CUDA(cudaEventRecord(ctx->ev[0], s));
-    if (opt && opt->use_graph && !cache) {
+    if (opt && opt->use_graph && !cache && !useWave) {
         // the four launches as one CUDA graph: re-captured when anything they read changed
         SolveParams Pwalk = P;
         if (Pwalk.coop) Pwalk.stackEntries = 0;
@@ -1026,7 +1062,7 @@ int solveImpl(zgpu_context* ctx, int solver, int nScenes, const zgpu_geometric_q
     ZG_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (P.coop) P.stackEntries = 0;     // the prepare kernel above used the per-thread stacks
     if (n > 0) {
-        if (useWave) ZG_TRY(runWave(ctx, P, D, s, &waveLaunches));
+        if (useWave) ZG_TRY(runWave(ctx, P, D, s, opt && opt->use_graph, &waveLaunches));
         else ZG_CUDA(launchWalk(P, D, blocks, threads, s));
     }
     if (cache && n > 0)
