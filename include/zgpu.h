@@ -382,7 +382,7 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
  * returns with *best_steps_per_s = -1.  There is no walks-per-thread knob: the persistent
  * walk kernel refills each lane from a global walk counter whenever its walk ends, so a lane
  * runs as many walks as the load demands.  The candidates run on the persistent kernel (the
- * sample is too small to judge the wavefront schedule) and the options returned keep the
+ * sample is too small to measure the wavefront schedule fairly) and the options returned keep the
  * automatic schedule.
  */
 int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries, const zgpu_pde* pde,

@@ -790,9 +790,9 @@ int runWave(zgpu_context* ctx, const SolveParams& P0, int D, cudaStream_t s, boo
         w.sceneMask = (uint32_t)((1u << sceneBits) - 1u);
     }
     // a slot holds one walk for at most max_walk_length + 1 iterations, so every walk has
-    // started after ceil(total / pool) such rounds and ended one round later
-    const double rounds = (double)((total + pool - 1) / pool + 1);
-    const double maxIter = rounds * ((double)P.sc.ws.max_walk_length + 1.0) + 2.0 * kWaveCheck;
+    // started after ceil(total / pool) such periods and ended one period later
+    const double periods = (double)((total + pool - 1) / pool + 1);
+    const double maxIter = periods * ((double)P.sc.ws.max_walk_length + 1.0) + 2.0 * kWaveCheck;
     // the tail: once every walk has started and at most this many records are live (one per
     // resident thread of the step kernels), the drain kernel runs them to their ends
     const long long drainAt = (long long)blocks * 128 * ZG_WAVE_DRAIN_FACTOR;
@@ -1227,7 +1227,7 @@ int zgpu_autotune(zgpu_context* ctx, int solver, const zgpu_geometric_queries* q
                 o.blocks_per_sm = perSMC[pi];
                 o.query_mode = qm;
                 o.bvh_width = wi == 0 ? 4 : 8;
-                // the knobs are the persistent kernel's; the sample is too small to judge the
+                // the knobs are the persistent kernel's; the sample is too small to measure the
                 // wavefront, whose iterations are launch-bound until the pool fills
                 o.schedule = ZGPU_SCHEDULE_PERSISTENT;
                 double rate = 0.0;
