@@ -381,7 +381,8 @@ int zgpu_solve_batched(zgpu_context* ctx, int solver, int n_scenes,
  * (dimension, solver, log2 primitive counts, reflecting kind, screening); a cached answer
  * returns with *best_steps_per_s = -1.  There is no walks-per-thread knob: the persistent
  * walk kernel refills each lane from a global walk counter whenever its walk ends, so a lane
- * runs as many walks as the load demands.  The candidates run on the persistent kernel (the
+ * runs as many walks as the load demands, and the wavefront keeps a fixed pool of 2^23 walks
+ * in flight (about 43 per resident thread).  The candidates run on the persistent kernel (the
  * sample is too small to measure the wavefront schedule fairly) and the options returned keep the
  * automatic schedule.
  */
