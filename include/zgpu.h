@@ -346,9 +346,9 @@ int zgpu_boundary_create_on_device(zgpu_context* ctx, int dim, const float* posi
 /*
  * WalkOnSpheres<T,DIM>::solve (point_estimation/walk_on_spheres.h:38-44, batch over points
  * :132-168) and WalkOnStars<T,DIM>::solve (point_estimation/walk_on_stars.h:40-46, :151-187).
- * Runs every walk of every point, in one persistent kernel or (Walk on Stars,
- * options->schedule) as a sorted wavefront of walk records, and merges the walk estimates
- * into `stats`.  options/report may be NULL.
+ * Runs every walk of every point, in one persistent kernel or (options->schedule; the
+ * default for 2D Walk on Stars) as a sorted wavefront of walk records, and merges the walk
+ * estimates into `stats`.  options/report may be NULL.
  */
 int zgpu_solve(zgpu_context* ctx, int solver, const zgpu_geometric_queries* queries,
                const zgpu_pde* pde, const zgpu_walk_settings* settings,
