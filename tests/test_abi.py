@@ -39,6 +39,24 @@ def test_struct_layouts_match_header():
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"
 
 
+def test_constants_match_header():
+    """Every ZGPU_* constant of the ctypes layer has the header's value (macros and enums)."""
+    names = [k for k in dir(A) if k.startswith("ZGPU_") and isinstance(getattr(A, k), int)]
+    lines = ['#include <stdio.h>', '#include "zgpu.h"', "int main(void) {"]
+    lines += [f'printf("{k} %lld\\n", (long long)({k}));' for k in names]
+    lines.append("return 0; }")
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "consts.c")
+        exe = os.path.join(d, "consts")
+        open(src, "w").write("\n".join(lines))
+        subprocess.check_call(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), src, "-o", exe])
+        out = subprocess.check_output([exe], text=True).split("\n")
+    got = dict(l.rsplit(" ", 1) for l in out if l)
+    assert len(got) == len(names) > 30
+    for k in names:
+        assert int(got[k]) == getattr(A, k), k
+
+
 def test_header_compiles_as_cpp():
     with tempfile.TemporaryDirectory() as d:
         src = os.path.join(d, "h.cpp")
